@@ -1,0 +1,334 @@
+"""Benchmark: Mrays/s of the path-tracing hot path at 1080p on one GB300 (N GPUs = replicas).
+
+Workload (default "spheres_1080p"): 1920x1080, 64 spp, config estimator (depth <= 16, Russian
+roulette from depth 3, survival 0.8), 200 displaced level-5 icospheres (4,096,000 triangles)
++ ground + a homogeneous volume box (sigma_t 0.5, albedo 0.8) + two area lights.  One step =
+LBVH build over the resident triangles + the full 64-spp render.  Synthetic, seeded inputs
+(PCG32); scene data (~0.5 GB of BVH + leaf records) is larger than L2.
+
+  value      Mrays/s with the scene resident in HBM (closest-hit queries / device time)
+  e2e        same metric through the C ABI with host buffers: scene upload from pinned host
+             memory, build, render, image read-back, scene release — every step
+  roofline   the render kernel: algorithmic bytes per ray (oracle-counted traversal work of the
+             workload, cudapathtracing_gb300/workload_constants.json) x rays / kernel time
+  cpu_baseline  the reference's CPU implementation (oracle/_ref where built, else the oracle
+             port) on a bounded sample of the same workload
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl cpt|reference] [--workload ...]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+WORKLOADS = {
+    "spheres_1080p": dict(spp=64, estimator=1, max_depth=16, rr_depth=3, rr_prob=0.8),
+    "cornell_512": dict(spp=16, estimator=0, max_depth=0, rr_depth=0, rr_prob=0.7),
+}
+
+
+def make_scene(name: str):
+    from cudapathtracing_gb300 import procedural as P
+    if name == "spheres_1080p":
+        return P.spheres_scene()
+    if name == "cornell_512":
+        return P.cornell_box(width=512)
+    raise SystemExit(f"unknown workload {name}")
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class ClockSampler:
+    """nvidia-smi samples (200 ms) during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4) if len(s) > 3 + k and s[3 + k] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+class CpuReference:
+    """The reference's CPU path on a band of whole rows of the workload (its STATIC estimator,
+    1 spp, PCG32 seed 0), starting a third of the way up the image.  Runs oracle/_ref (the
+    reference's own code) where it was built, else the oracle's restatement of it, which traces
+    the same paths bit for bit (so the port's ray count is used for both)."""
+
+    def __init__(self, desc, threads: int = 0):
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        from cudapathtracing_gb300 import abi
+        O.build(ref=False)
+        self.O, self.abi = O, abi
+        self.threads = threads or os.cpu_count() or 1
+        self.desc = desc
+        self.port = O.OracleScene(desc)
+        self.ref = O.RefScene(desc) if O.ref_lib() is not None else None
+        self.kind = "reference" if self.ref is not None else "port"
+        self.r0 = desc.camera.height // 3
+        self.rows = 1
+        self.rays = 0
+
+    def _port(self):
+        prm = self.abi.render_params(spp=1, estimator=self.abi.ESTIMATOR_REFERENCE, seed=0, row_begin=self.r0,
+                                     row_end=self.r0 + self.rows)
+        t0 = time.perf_counter()
+        rays = self.port.render(prm, threads=self.threads)["rays"]
+        return rays, time.perf_counter() - t0
+
+    def calibrate(self, seconds: float, max_rows: int = 64) -> None:
+        """Grows the band until one run takes about `seconds`."""
+        H = self.desc.camera.height
+        while True:
+            self.rays, t = self._port()
+            if t >= seconds / 2 or self.rows >= max_rows or self.r0 + 2 * self.rows > H:
+                break
+            self.rows *= 2
+
+    def run(self) -> float:
+        """One timed run of the band; returns Mrays/s."""
+        if self.ref is not None:
+            t0 = time.perf_counter()
+            self.ref.render(1, seed=0, row_begin=self.r0, row_end=self.r0 + self.rows, threads=self.threads)
+            t = time.perf_counter() - t0
+        else:
+            self.rays, t = self._port()
+        self.last_s = t
+        return self.rays / t / 1e6
+
+    def info(self, value: float) -> dict:
+        return dict(value=round(value, 4), unit="Mrays/s", cores=self.threads, kind=self.kind,
+                    sample=f"rows {self.r0}..{self.r0 + self.rows - 1} x {self.desc.camera.width} px x 1 spp of "
+                           f"the workload, reference estimator, {self.rays} rays per run")
+
+
+def cpu_reference_sample(desc, seconds: float = 15.0):
+    c = CpuReference(desc)
+    c.calibrate(seconds)
+    v = c.run()
+    return v, c.info(v)
+
+
+def run_reference_arm(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    desc = make_scene(args.workload)
+    cref = CpuReference(desc)
+    cref.calibrate(seconds=8.0, max_rows=16)
+    vals = []
+    for step in range(args.warmup + args.steps):
+        v = cref.run()
+        if step >= args.warmup:
+            vals.append(v)
+    value = float(np.mean(vals))
+    info = cref.info(value)
+    line = {"impl": "reference", "metric": "Mrays/s @1080p", "value": round(value, 4), "unit": "Mrays/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": args.workload, "width": desc.camera.width, "height": desc.camera.height,
+                       "triangles": desc.num_triangles, "sample": info["sample"]},
+            "cpu_baseline": info,
+            "e2e": {"value": round(value, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="cpt", choices=["cpt", "reference"])
+    ap.add_argument("--workload", default="spheres_1080p", choices=sorted(WORKLOADS))
+    ap.add_argument("--integrator", default="megakernel", choices=["megakernel", "wavefront"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference_arm(args)
+
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from cudapathtracing_gb300 import _lib, abi, api
+    from cudapathtracing_gb300 import build as cbuild
+    if not os.path.exists(_lib.LIB_PATH):
+        cbuild.build()
+    wl = WORKLOADS[args.workload]
+    integ = abi.INTEGRATOR_WAVEFRONT if args.integrator == "wavefront" else abi.INTEGRATOR_MEGAKERNEL
+    desc = make_scene(args.workload)
+    W, H = desc.camera.width, desc.camera.height
+    ctx = api.Context(local)
+    stream = torch.cuda.current_stream()
+    scene = api.Scene(ctx, desc)
+    scene.buildBVH(stream.cuda_stream)
+    rgb = torch.zeros((H, W, 3), device="cuda")
+    rgba = torch.zeros((H, W, 4), dtype=torch.uint8, device="cuda")
+    seed = 1000 * rank
+
+    def step(i):
+        st = scene.buildBVH(stream.cuda_stream)
+        r = scene.render(rgb=rgb, rgba8=rgba, stream=stream.cuda_stream, integrator=integ, seed=seed + i, **wl)
+        return st, r
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for i in range(args.warmup):
+        step(i)
+    barrier()
+    launches0 = _lib.lib().cpt_launch_count()
+    rays = 0
+    kernel_ms = []
+    build_ms = []
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        for i in range(args.steps):
+            st, r = step(args.warmup + i)
+            rays += r["rays"]
+            kernel_ms.append(r["ms"])
+            build_ms.append(st.ms_total)
+        ev1.record(stream)
+        barrier()
+    launches = _lib.lib().cpt_launch_count() - launches0
+    elapsed = ev0.elapsed_time(ev1) / 1e3
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([elapsed, float(rays)], device="cuda", dtype=torch.float64)
+        tmax = t.clone()
+        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+        elapsed, rays = float(tmax[0]), int(t[1])
+    value = rays / elapsed / 1e6
+
+    # ---- e2e through the C ABI with host buffers (pinned)
+    tri_pinned = torch.from_numpy(desc.tri_vertices).pin_memory()
+    desc_e2e = desc
+    desc_e2e.tri_vertices = tri_pinned.numpy()
+    host_rgb = torch.zeros((H, W, 3), dtype=torch.float32).pin_memory().numpy()
+    host_rgba = torch.zeros((H, W, 4), dtype=torch.uint8).pin_memory().numpy()
+    e2e_steps = max(1, min(args.steps, 2))
+    e2e_rays = 0
+    barrier()
+    t0 = time.perf_counter()
+    for i in range(e2e_steps):
+        s2 = api.Scene(ctx, desc_e2e)
+        s2.buildBVH()
+        r2 = s2.render(rgb=host_rgb, rgba8=host_rgba, integrator=integ, seed=seed + i, **wl)
+        e2e_rays += r2["rays"]
+        s2.close()
+    barrier()
+    e2e_t = time.perf_counter() - t0
+    h2d = desc.tri_vertices.nbytes + desc.tri_material.nbytes + 9 * 0
+    d2h = host_rgb.nbytes + host_rgba.nbytes
+
+    if rank != 0:
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return
+
+    consts = json.load(open(os.path.join(ROOT, "cudapathtracing_gb300", "workload_constants.json")))[args.workload]
+    bpr = consts["bytes_per_ray"]
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(peaks_path):
+        peak = json.load(open(peaks_path))["hbm_gbs"]
+        peak_src = "measured"
+    else:
+        peak, peak_src = 6800.0, "fallback"
+    k_ms = float(np.mean(kernel_ms))
+    rays_per_launch = rays / world / args.steps
+    achieved = rays_per_launch * bpr / (k_ms / 1e3) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", f"traffic_{args.workload}.json")
+    if os.path.exists(tpath):
+        traffic = json.load(open(tpath)).get("bytes_per_launch")
+
+    cpu = None
+    if not args.no_cpu_baseline:
+        try:
+            _, cpu = cpu_reference_sample(desc, seconds=15.0)
+        except Exception as e:  # the baseline is reported, never required
+            cpu = {"value": None, "unit": "Mrays/s", "cores": 0, "kind": "port", "sample": f"failed: {e}"}
+
+    line = {
+        "metric": "Mrays/s @1080p", "value": round(value, 3), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(elapsed / args.steps * 1e3, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": args.workload, "width": W, "height": H, "spp": wl["spp"],
+                   "triangles": desc.num_triangles, "integrator": args.integrator,
+                   "estimator": "config" if wl["estimator"] == 1 else "reference",
+                   "max_depth": wl["max_depth"], "rr_depth": wl["rr_depth"], "rr_prob": wl["rr_prob"],
+                   "step": "LBVH build + full render", "l2": "inputs larger than L2 (BVH + leaf records)",
+                   "build_ms": round(float(np.mean(build_ms)), 3), "rays_per_step": int(rays_per_launch),
+                   "parallelism": f"replicas x{world}"},
+        "e2e": {"value": round(e2e_rays / e2e_t / 1e6, 3), "unit": "Mrays/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "steps": e2e_steps},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": traffic, "kernel": "k_render",
+                     "kernel_ms": round(k_ms, 3), "bytes_per_ray": round(bpr, 1), "peak_source": peak_src},
+        "cpu_baseline": cpu,
+        "clocks": clk.summary(),
+        "gpu_launches": int(launches),
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

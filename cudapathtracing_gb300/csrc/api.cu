@@ -1,0 +1,696 @@
+// api.cu — the C ABI of libcpt.so (include/cpt.h): contexts, scenes, LBVH build/export,
+// closest-hit queries and rendering.  Scene memory is owned by the library; caller
+// buffers are borrowed for the duration of a call.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "cpt_internal.h"
+
+namespace cpt {
+
+static thread_local std::string g_last_error;
+static std::atomic<uint64_t> g_launches(0);
+
+void add_launches(uint64_t k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+cpt_status fail(cpt_status st, const std::string& msg)
+{
+    set_error(msg);
+    return st;
+}
+
+cpt_status cuda_fail(cudaError_t e, const char* what)
+{
+    cpt_status st = (e == cudaErrorMemoryAllocation) ? CPT_ERR_OUT_OF_MEMORY : CPT_ERR_CUDA;
+    return fail(st, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+struct IniScene;
+cpt_status ini_load(const char* path, IniScene** out);
+const cpt_scene_desc* ini_desc(const IniScene* s);
+void ini_free(IniScene* s);
+
+}  // namespace cpt
+
+using namespace cpt;
+
+struct cpt_context {
+    int device;
+    int sm_count;
+    int render_block_x, render_block_y;
+};
+
+struct cpt_scene {
+    cpt_context* ctx;
+    uint32_t n_lights, n_spheres, n_tris, n;
+    cpt_camera camera;
+    DevCamera cam;
+    double bmin[3], bmax[3];
+    bool tri_is_f64;
+    bool built;
+    // inputs on the device
+    float* tri_f32;
+    double* tri_f64;
+    float* tri_n;
+    uint32_t* tri_mat;
+    float4* spheres;
+    uint32_t* sphere_mat;
+    DevLight* lights;
+    DevMaterial* mats;
+    double* extra_c;
+    float4* extra_box;
+    // LBVH
+    uint64_t* keys;
+    uint32_t* order;
+    int2* child;
+    int2* range;
+    float4* node_box;
+    float4* leaf_box;
+    void* scratch;
+    size_t scratch_bytes;
+    // traversal layout
+    float4* nodes;
+    float4* leaf_rec;
+    // misc
+    unsigned long long* ray_counter;
+    int* err;
+};
+
+namespace {
+
+template <typename T>
+cpt_status dalloc(T** p, size_t count)
+{
+    *p = nullptr;
+    if (count == 0) return CPT_OK;
+    CPT_CUDA(cudaMalloc((void**)p, count * sizeof(T)));
+    return CPT_OK;
+}
+
+template <typename T>
+void dfree(T*& p)
+{
+    if (p) cudaFree((void*)p);
+    p = nullptr;
+}
+
+void free_scene(cpt_scene* s)
+{
+    dfree(s->tri_f32); dfree(s->tri_f64); dfree(s->tri_n); dfree(s->tri_mat); dfree(s->spheres);
+    dfree(s->sphere_mat); dfree(s->lights); dfree(s->mats); dfree(s->extra_c); dfree(s->extra_box);
+    dfree(s->keys); dfree(s->order); dfree(s->child); dfree(s->range); dfree(s->node_box); dfree(s->leaf_box);
+    dfree(s->scratch); dfree(s->nodes); dfree(s->leaf_rec); dfree(s->ray_counter); dfree(s->err);
+}
+
+// ---- reference double maths for the host-side derived quantities
+struct D3 { double x, y, z; };
+inline D3 d3(const double* p) { return D3{p[0], p[1], p[2]}; }
+inline D3 operator+(D3 a, D3 b) { return D3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline D3 operator-(D3 a, D3 b) { return D3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline D3 operator*(D3 v, double t) { return D3{v.x * t, v.y * t, v.z * t}; }
+inline D3 operator/(D3 v, double t) { return D3{v.x / t, v.y / t, v.z / t}; }
+inline double dot(D3 a, D3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline D3 cross(D3 a, D3 b) { return D3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+inline D3 unit(D3 v) { return v / std::sqrt(v.x * v.x + v.y * v.y + v.z * v.z); }
+inline double mmin(double a, double b) { return a < b ? a : b; }
+inline double mmax(double a, double b) { return a > b ? a : b; }
+inline float3 tof(D3 v) { return make_float3((float)v.x, (float)v.y, (float)v.z); }
+inline float rd(double x) { float f = (float)x; return (double)f > x ? std::nextafter(f, -INFINITY) : f; }
+inline float ru(double x) { float f = (float)x; return (double)f < x ? std::nextafter(f, INFINITY) : f; }
+
+// Camera ctor (Camera.cu:5-40) in double, then rounded to FP32.
+DevCamera make_camera(const cpt_camera& c)
+{
+    DevCamera k;
+    int width = c.width;
+    double hh = width / c.aspect_ratio;
+    int height = hh < 1 ? 1 : (int)hh;
+    D3 from = d3(c.look_from), at = d3(c.look_at), up = D3{0, 1, 0};
+    double focal = std::sqrt(dot(from - at, from - at));
+    double theta = c.vfov_deg * 3.14159265358979323846 / 180.0;
+    double h = std::tan(theta / 2);
+    double vh = 2.0 * h * focal;
+    double vw = (double)width / height * vh;
+    D3 w = unit(from - at);
+    D3 u = unit(cross(up, w));
+    D3 v = cross(w, u);
+    D3 hor = u * vw, ver = v * vh;
+    D3 dh = hor / width, dv = ver / height;
+    D3 ul = from - hor / 2 - ver / 2 - w * focal;
+    D3 pc = ul + dh / 2 + dv / 2;
+    k.look_from = tof(from);
+    k.pixel_center = tof(pc);
+    k.delta_h = tof(dh);
+    k.delta_v = tof(dv);
+    k.background = tof(d3(c.background));
+    k.width = width;
+    k.height = height;
+    return k;
+}
+
+// Light frame and padded box (Light ctor Hittable.cuh:359-365, Hittable(Light) :424-454).
+void light_derived(const cpt_light& L, DevLight& dl, double box[6])
+{
+    D3 c = d3(L.center);
+    D3 n = unit(d3(L.normal));
+    D3 eu = std::fabs(n.x) > 0.9 ? unit(cross(D3{0, 1, 0}, n)) : unit(cross(D3{1, 0, 0}, n));
+    D3 ev = unit(cross(n, eu));
+    D3 N = unit(n);
+    D3 T = std::fabs(N.x) > 0.9 ? unit(cross(D3{0, 1, 0}, N)) : unit(cross(D3{1, 0, 0}, N));
+    D3 B = unit(cross(N, T));
+    D3 k[4] = {c + T * (L.width / 2) + B * (L.height / 2), c + T * (L.width / 2) + B * (-L.height / 2),
+               c + T * (-L.width / 2) + B * (L.height / 2), c + T * (-L.width / 2) + B * (-L.height / 2)};
+    D3 mn = k[0], mx = k[0];
+    for (int i = 1; i < 4; ++i) {
+        mn = D3{mmin(mn.x, k[i].x), mmin(mn.y, k[i].y), mmin(mn.z, k[i].z)};
+        mx = D3{mmax(mx.x, k[i].x), mmax(mx.y, k[i].y), mmax(mx.z, k[i].z)};
+    }
+    box[0] = mn.x - 0.0001; box[1] = mn.y - 0.0001; box[2] = mn.z - 0.0001;
+    box[3] = mx.x + 0.0001; box[4] = mx.y + 0.0001; box[5] = mx.z + 0.0001;
+    std::memset(&dl, 0, sizeof dl);
+    dl.center = tof(c);
+    dl.normal = tof(n);
+    dl.eu = tof(eu);
+    dl.ev = tof(ev);
+    dl.w = (float)L.width;
+    dl.h = (float)L.height;
+    dl.visible = L.visible ? 1 : 0;
+    dl.color = tof(d3(L.color));
+}
+
+cpt_status validate(const cpt_scene_desc* d)
+{
+    if (!d) return fail(CPT_ERR_INVALID_ARGUMENT, "scene description is NULL");
+    if (d->num_lights && !d->lights) return fail(CPT_ERR_INVALID_ARGUMENT, "lights pointer is NULL");
+    if (d->num_spheres && !d->spheres) return fail(CPT_ERR_INVALID_ARGUMENT, "spheres pointer is NULL");
+    if (d->num_triangles) {
+        if (!d->tri_vertices == !d->tri_vertices_f64)
+            return fail(CPT_ERR_INVALID_ARGUMENT, "exactly one of tri_vertices / tri_vertices_f64 must be set");
+        if (!d->tri_material) return fail(CPT_ERR_INVALID_ARGUMENT, "tri_material is NULL");
+    }
+    if (d->num_materials == 0 || !d->materials) return fail(CPT_ERR_INVALID_ARGUMENT, "no materials");
+    for (uint32_t i = 0; i < d->num_spheres; ++i)
+        if (d->spheres[i].material >= d->num_materials)
+            return fail(CPT_ERR_INVALID_ARGUMENT, "sphere material index out of range");
+    for (uint32_t i = 0; i < d->num_triangles; ++i)
+        if (d->tri_material[i] >= d->num_materials)
+            return fail(CPT_ERR_INVALID_ARGUMENT, "triangle material index out of range");
+    uint64_t n = (uint64_t)d->num_lights + d->num_spheres + d->num_triangles;
+    if (n > 0x7fffffffull) return fail(CPT_ERR_INVALID_ARGUMENT, "too many primitives");
+    if (d->camera.width <= 0 || d->camera.aspect_ratio <= 0.0)
+        return fail(CPT_ERR_INVALID_ARGUMENT, "camera width and aspect ratio must be positive");
+    double hh = d->camera.width / d->camera.aspect_ratio;
+    int h = hh < 1 ? 1 : (int)hh;
+    if (d->camera.height != h) return fail(CPT_ERR_INVALID_ARGUMENT, "camera height must be (int)(width / aspect_ratio)");
+    return CPT_OK;
+}
+
+template <typename T>
+cpt_status upload(T** dst, const T* src, size_t count)
+{
+    cpt_status st = dalloc(dst, count);
+    if (st != CPT_OK) return st;
+    if (count) CPT_CUDA(cudaMemcpy(*dst, src, count * sizeof(T), cudaMemcpyHostToDevice));
+    return CPT_OK;
+}
+
+cpt_status create_scene(cpt_context* ctx, const cpt_scene_desc* d, cpt_scene** out)
+{
+    cpt_status st = validate(d);
+    if (st != CPT_OK) return st;
+    CPT_CUDA(cudaSetDevice(ctx->device));
+    cpt_scene* s = new cpt_scene;
+    std::memset(s, 0, sizeof *s);
+    s->ctx = ctx;
+    s->n_lights = d->num_lights;
+    s->n_spheres = d->num_spheres;
+    s->n_tris = d->num_triangles;
+    s->n = s->n_lights + s->n_spheres + s->n_tris;
+    s->camera = d->camera;
+    s->cam = make_camera(d->camera);
+    for (int a = 0; a < 3; ++a) { s->bmin[a] = d->bounds_min[a]; s->bmax[a] = d->bounds_max[a]; }
+    s->tri_is_f64 = d->tri_vertices_f64 != nullptr;
+    uint32_t ne = s->n_lights + s->n_spheres;
+    std::vector<double> extra_c(3 * (size_t)ne);
+    std::vector<float4> extra_box(2 * (size_t)ne);
+    std::vector<DevLight> lights(s->n_lights);
+    for (uint32_t i = 0; i < s->n_lights; ++i) {
+        double b[6];
+        light_derived(d->lights[i], lights[i], b);
+        for (int a = 0; a < 3; ++a) extra_c[3 * i + a] = d->lights[i].center[a];
+        extra_box[2 * i] = make_float4(rd(b[0]), rd(b[1]), rd(b[2]), 0.f);
+        extra_box[2 * i + 1] = make_float4(ru(b[3]), ru(b[4]), ru(b[5]), 0.f);
+    }
+    std::vector<float4> sph(s->n_spheres);
+    std::vector<uint32_t> sph_mat(s->n_spheres);
+    for (uint32_t i = 0; i < s->n_spheres; ++i) {   // Hittable(Sphere): centre, unpadded box (Hittable.cuh:418-422)
+        const cpt_sphere& S = d->spheres[i];
+        uint32_t e = s->n_lights + i;
+        double r = S.radius;
+        double lo[3], hi[3];
+        for (int a = 0; a < 3; ++a) {
+            extra_c[3 * e + a] = S.center[a];
+            double p0 = S.center[a] - r, p1 = S.center[a] + r;
+            lo[a] = mmin(p0, p1);
+            hi[a] = mmax(p0, p1);
+        }
+        extra_box[2 * e] = make_float4(rd(lo[0]), rd(lo[1]), rd(lo[2]), 0.f);
+        extra_box[2 * e + 1] = make_float4(ru(hi[0]), ru(hi[1]), ru(hi[2]), 0.f);
+        sph[i] = make_float4((float)S.center[0], (float)S.center[1], (float)S.center[2], (float)S.radius);
+        sph_mat[i] = S.material;
+    }
+    std::vector<DevMaterial> mats(d->num_materials);
+    for (uint32_t i = 0; i < d->num_materials; ++i) {
+        const cpt_material& m = d->materials[i];
+        DevMaterial& dm = mats[i];
+        std::memset(&dm, 0, sizeof dm);
+        dm.color = make_float3((float)m.color[0], (float)m.color[1], (float)m.color[2]);
+        dm.ax = (float)m.alpha_x;
+        dm.ay = (float)m.alpha_y;
+        dm.type = m.type;
+        dm.eta = (float)m.eta;
+        dm.sigma_t = (float)m.sigma_t;
+        dm.albedo = (float)m.albedo;
+    }
+    size_t T = s->n_tris;
+#define CPT_TRY(x)             \
+    do {                       \
+        st = (x);              \
+        if (st != CPT_OK) {    \
+            free_scene(s);     \
+            delete s;          \
+            return st;         \
+        }                      \
+    } while (0)
+    if (s->tri_is_f64)
+        CPT_TRY(upload(&s->tri_f64, d->tri_vertices_f64, 9 * T));
+    else
+        CPT_TRY(upload(&s->tri_f32, d->tri_vertices, 9 * T));
+    if (d->tri_normals) CPT_TRY(upload(&s->tri_n, d->tri_normals, 9 * T));
+    CPT_TRY(upload(&s->tri_mat, d->tri_material, T));
+    CPT_TRY(upload(&s->spheres, sph.data(), sph.size()));
+    CPT_TRY(upload(&s->sphere_mat, sph_mat.data(), sph_mat.size()));
+    CPT_TRY(upload(&s->lights, lights.data(), lights.size()));
+    CPT_TRY(upload(&s->mats, mats.data(), mats.size()));
+    CPT_TRY(upload(&s->extra_c, extra_c.data(), extra_c.size()));
+    CPT_TRY(upload(&s->extra_box, extra_box.data(), extra_box.size()));
+    uint32_t n = s->n;
+    uint32_t ni = n > 1 ? n - 1 : 0;
+    CPT_TRY(dalloc(&s->keys, n));
+    CPT_TRY(dalloc(&s->order, n));
+    CPT_TRY(dalloc(&s->child, ni));
+    CPT_TRY(dalloc(&s->range, ni));
+    CPT_TRY(dalloc(&s->node_box, 2 * (size_t)ni));
+    CPT_TRY(dalloc(&s->leaf_box, 2 * (size_t)n));
+    CPT_TRY(dalloc(&s->nodes, 4 * (size_t)ni));
+    CPT_TRY(dalloc(&s->leaf_rec, 3 * (size_t)n));
+    s->scratch_bytes = lbvh_scratch_bytes(n);
+    CPT_TRY(dalloc((char**)&s->scratch, s->scratch_bytes));
+    CPT_TRY(dalloc(&s->ray_counter, 1));
+    CPT_TRY(dalloc(&s->err, 1));
+#undef CPT_TRY
+    CPT_CUDA(cudaMemset(s->err, 0, sizeof(int)));
+    *out = s;
+    return CPT_OK;
+}
+
+SceneView view_of(const cpt_scene* s)
+{
+    SceneView v;
+    std::memset(&v, 0, sizeof v);
+    v.n_prims = (int)s->n;
+    v.n_lights = (int)s->n_lights;
+    v.n_spheres = (int)s->n_spheres;
+    v.n_tris = (int)s->n_tris;
+    v.n_internal = s->n > 1 ? (int)s->n - 1 : 0;
+    v.nodes = s->nodes;
+    v.leaf_rec = s->leaf_rec;
+    v.tri_mat = s->tri_mat;
+    v.tri_n = s->tri_n;
+    v.spheres = s->spheres;
+    v.sphere_mat = s->sphere_mat;
+    v.lights = s->lights;
+    v.mats = s->mats;
+    v.cam = s->cam;
+    return v;
+}
+
+LbvhBuffers buffers_of(cpt_scene* s)
+{
+    LbvhBuffers b;
+    b.keys = s->keys;
+    b.order = s->order;
+    b.child = s->child;
+    b.range = s->range;
+    b.node_box = s->node_box;
+    b.leaf_box = s->leaf_box;
+    return b;
+}
+
+// Reads and clears the device error word (synchronises the stream).
+cpt_status check_device_error(cpt_scene* s, cudaStream_t stream)
+{
+    int e = 0;
+    CPT_CUDA(cudaMemcpyAsync(&e, s->err, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    CPT_CUDA(cudaStreamSynchronize(stream));
+    if (e) {
+        CPT_CUDA(cudaMemsetAsync(s->err, 0, sizeof(int), stream));
+        if (e & CPT_DEVERR_STACK) return fail(CPT_ERR_STACK_OVERFLOW, "traversal stack limit exceeded");
+        return fail(CPT_ERR_TIMEOUT, "a device loop reached its iteration limit");
+    }
+    return CPT_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- exported API
+CPT_EXPORT int cpt_abi_version(void) { return CPT_ABI_VERSION; }
+
+CPT_EXPORT uint64_t cpt_launch_count(void) { return g_launches.load(); }
+
+CPT_EXPORT const char* cpt_last_error_string(void) { return g_last_error.c_str(); }
+
+CPT_EXPORT cpt_status cpt_context_create(int device, cpt_context** out)
+{
+    if (!out) return fail(CPT_ERR_INVALID_ARGUMENT, "cpt_context_create: out is NULL");
+    *out = nullptr;
+    int count = 0;
+    CPT_CUDA(cudaGetDeviceCount(&count));
+    if (device < 0 || device >= count) return fail(CPT_ERR_INVALID_ARGUMENT, "cpt_context_create: no such device");
+    CPT_CUDA(cudaSetDevice(device));
+    cpt_context* c = new cpt_context;
+    c->device = device;
+    CPT_CUDA(cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device));
+    c->render_block_x = 16;
+    c->render_block_y = 8;
+    *out = c;
+    return CPT_OK;
+}
+
+CPT_EXPORT cpt_status cpt_context_destroy(cpt_context* ctx)
+{
+    delete ctx;
+    return CPT_OK;
+}
+
+// Internal tuning knob (the autotuner's setter): render block shape.
+CPT_EXPORT cpt_status cpt_context_set_render_block(cpt_context* ctx, int bx, int by)
+{
+    if (!ctx || bx <= 0 || by <= 0 || (bx * by) % 32 || bx * by > 1024)
+        return fail(CPT_ERR_INVALID_ARGUMENT, "render block must be a positive multiple of 32 threads, <= 1024");
+    ctx->render_block_x = bx;
+    ctx->render_block_y = by;
+    return CPT_OK;
+}
+
+CPT_EXPORT cpt_status cpt_scene_create(cpt_context* ctx, const cpt_scene_desc* desc, cpt_scene** out)
+{
+    if (!ctx || !out) return fail(CPT_ERR_INVALID_ARGUMENT, "cpt_scene_create: null argument");
+    *out = nullptr;
+    return create_scene(ctx, desc, out);
+}
+
+CPT_EXPORT cpt_status cpt_scene_load_ini(cpt_context* ctx, const char* path, cpt_scene** out)
+{
+    if (!ctx || !out) return fail(CPT_ERR_INVALID_ARGUMENT, "cpt_scene_load_ini: null argument");
+    *out = nullptr;
+    IniScene* ini = nullptr;
+    cpt_status st = ini_load(path, &ini);
+    if (st != CPT_OK) return st;
+    st = create_scene(ctx, ini_desc(ini), out);
+    ini_free(ini);
+    return st;
+}
+
+CPT_EXPORT cpt_status cpt_ini_load(const char* path, cpt_ini_scene** out)
+{
+    return ini_load(path, (IniScene**)out);
+}
+
+CPT_EXPORT cpt_status cpt_ini_describe(const cpt_ini_scene* ini, cpt_scene_desc* out)
+{
+    if (!ini || !out) return fail(CPT_ERR_INVALID_ARGUMENT, "cpt_ini_describe: null argument");
+    *out = *ini_desc((const IniScene*)ini);
+    return CPT_OK;
+}
+
+CPT_EXPORT cpt_status cpt_ini_free(cpt_ini_scene* ini)
+{
+    ini_free((IniScene*)ini);
+    return CPT_OK;
+}
+
+CPT_EXPORT cpt_status cpt_scene_destroy(cpt_scene* s)
+{
+    if (!s) return CPT_OK;
+    free_scene(s);
+    delete s;
+    return CPT_OK;
+}
+
+CPT_EXPORT cpt_status cpt_scene_info(const cpt_scene* s, uint32_t* nl, uint32_t* ns, uint32_t* nt, cpt_camera* cam)
+{
+    if (!s) return fail(CPT_ERR_INVALID_ARGUMENT, "cpt_scene_info: scene is NULL");
+    if (nl) *nl = s->n_lights;
+    if (ns) *ns = s->n_spheres;
+    if (nt) *nt = s->n_tris;
+    if (cam) *cam = s->camera;
+    return CPT_OK;
+}
+
+CPT_EXPORT cpt_status cpt_scene_update_triangles(cpt_scene* s, const float* tri, uint32_t first, uint32_t count,
+                                                 void* stream)
+{
+    if (!s || (!tri && count)) return fail(CPT_ERR_INVALID_ARGUMENT, "cpt_scene_update_triangles: null argument");
+    if ((uint64_t)first + count > s->n_tris) return fail(CPT_ERR_INVALID_ARGUMENT, "triangle range out of bounds");
+    if (s->tri_is_f64) return fail(CPT_ERR_UNSUPPORTED, "scene has FP64 vertices; update with FP32 is not supported");
+    if (count)
+        CPT_CUDA(cudaMemcpyAsync(s->tri_f32 + 9ull * first, tri, 9ull * count * sizeof(float), cudaMemcpyHostToDevice,
+                                 (cudaStream_t)stream));
+    return CPT_OK;
+}
+
+CPT_EXPORT cpt_status cpt_lbvh_build(cpt_scene* s, void* stream_, cpt_bvh_stats* stats)
+{
+    if (!s) return fail(CPT_ERR_INVALID_ARGUMENT, "cpt_lbvh_build: scene is NULL");
+    cudaStream_t stream = (cudaStream_t)stream_;
+    CPT_CUDA(cudaSetDevice(s->ctx->device));
+    LbvhTimings tm = {0, 0, 0, 0};
+    cudaEvent_t e0, e1;
+    if (stats) {
+        CPT_CUDA(cudaEventCreate(&e0));
+        CPT_CUDA(cudaEventCreate(&e1));
+    }
+    uint32_t ne = s->n_lights + s->n_spheres;
+    cpt_status st = lbvh_build(ne, s->extra_c, s->extra_box, s->n_tris, s->tri_f32, s->tri_f64, s->bmin, s->bmax,
+                               buffers_of(s), s->scratch, s->scratch_bytes, stream, stats ? &tm : nullptr);
+    if (st != CPT_OK) return st;
+    if (stats) CPT_CUDA(cudaEventRecord(e0, stream));
+    st = build_trace_layout(s->n, s->n_lights, s->n_spheres, s->child, s->node_box, s->leaf_box, s->order, s->tri_f32,
+                            s->tri_f64, s->spheres, s->nodes, s->leaf_rec, stream);
+    if (st != CPT_OK) return st;
+    s->built = true;
+    if (stats) {
+        CPT_CUDA(cudaEventRecord(e1, stream));
+        CPT_CUDA(cudaEventSynchronize(e1));
+        std::memset(stats, 0, sizeof *stats);
+        stats->num_prims = s->n;
+        stats->ms_prep = tm.ms_prep;
+        stats->ms_sort = tm.ms_sort;
+        stats->ms_emit = tm.ms_emit;
+        stats->ms_refit = tm.ms_refit;
+        CPT_CUDA(cudaEventElapsedTime(&stats->ms_collapse, e0, e1));
+        stats->ms_total = tm.ms_prep + tm.ms_sort + tm.ms_emit + tm.ms_refit + stats->ms_collapse;
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+    }
+    return CPT_OK;
+}
+
+CPT_EXPORT cpt_status cpt_lbvh_refit(cpt_scene* s, void* stream_, cpt_bvh_stats* stats)
+{
+    if (!s) return fail(CPT_ERR_INVALID_ARGUMENT, "cpt_lbvh_refit: scene is NULL");
+    if (!s->built) return fail(CPT_ERR_NOT_BUILT, "cpt_lbvh_refit: build the LBVH first");
+    cudaStream_t stream = (cudaStream_t)stream_;
+    cudaEvent_t e0, e1;
+    if (stats) {
+        CPT_CUDA(cudaEventCreate(&e0));
+        CPT_CUDA(cudaEventCreate(&e1));
+        CPT_CUDA(cudaEventRecord(e0, stream));
+    }
+    uint32_t ne = s->n_lights + s->n_spheres;
+    cpt_status st = lbvh_leaf_boxes(ne, s->extra_box, s->n_tris, s->tri_f32, s->tri_f64, s->order, s->leaf_box, s->n, stream);
+    if (st != CPT_OK) return st;
+    st = lbvh_refit(s->n, buffers_of(s), s->scratch, s->scratch_bytes, stream);
+    if (st != CPT_OK) return st;
+    st = build_trace_layout(s->n, s->n_lights, s->n_spheres, s->child, s->node_box, s->leaf_box, s->order, s->tri_f32,
+                            s->tri_f64, s->spheres, s->nodes, s->leaf_rec, stream);
+    if (st != CPT_OK) return st;
+    if (stats) {
+        CPT_CUDA(cudaEventRecord(e1, stream));
+        CPT_CUDA(cudaEventSynchronize(e1));
+        std::memset(stats, 0, sizeof *stats);
+        stats->num_prims = s->n;
+        CPT_CUDA(cudaEventElapsedTime(&stats->ms_refit, e0, e1));
+        stats->ms_total = stats->ms_refit;
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+    }
+    return CPT_OK;
+}
+
+CPT_EXPORT cpt_status cpt_lbvh_export(const cpt_scene* s, uint64_t* keys, uint32_t* order, int32_t* child_a,
+                                      int32_t* child_b, float* node_boxes, float* leaf_boxes)
+{
+    if (!s) return fail(CPT_ERR_INVALID_ARGUMENT, "cpt_lbvh_export: scene is NULL");
+    if (!s->built) return fail(CPT_ERR_NOT_BUILT, "cpt_lbvh_export: build the LBVH first");
+    CPT_CUDA(cudaSetDevice(s->ctx->device));
+    CPT_CUDA(cudaDeviceSynchronize());
+    size_t n = s->n, ni = n > 1 ? n - 1 : 0;
+    if (keys) CPT_CUDA(cudaMemcpy(keys, s->keys, n * 8, cudaMemcpyDeviceToHost));
+    if (order) CPT_CUDA(cudaMemcpy(order, s->order, n * 4, cudaMemcpyDeviceToHost));
+    if ((child_a || child_b) && ni) {
+        std::vector<int2> c(ni);
+        CPT_CUDA(cudaMemcpy(c.data(), s->child, ni * sizeof(int2), cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < ni; ++i) {
+            if (child_a) child_a[i] = c[i].x;
+            if (child_b) child_b[i] = c[i].y;
+        }
+    }
+    auto boxes = [&](const float4* src, size_t cnt, float* dst) -> cpt_status {
+        std::vector<float4> b(2 * cnt);
+        if (cnt) CPT_CUDA(cudaMemcpy(b.data(), src, 2 * cnt * sizeof(float4), cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < cnt; ++i) {
+            float v[6] = {b[2 * i].x, b[2 * i].y, b[2 * i].z, b[2 * i + 1].x, b[2 * i + 1].y, b[2 * i + 1].z};
+            std::memcpy(dst + 6 * i, v, sizeof v);
+        }
+        return CPT_OK;
+    };
+    if (node_boxes) {
+        cpt_status st = boxes(s->node_box, ni, node_boxes);
+        if (st != CPT_OK) return st;
+    }
+    if (leaf_boxes) {
+        cpt_status st = boxes(s->leaf_box, n, leaf_boxes);
+        if (st != CPT_OK) return st;
+    }
+    return CPT_OK;
+}
+
+CPT_EXPORT cpt_status cpt_trace_closest(cpt_scene* s, const cpt_ray* rays, uint64_t n, cpt_hit* hits, int on_device,
+                                        void* stream_)
+{
+    if (!s || (n && (!rays || !hits))) return fail(CPT_ERR_INVALID_ARGUMENT, "cpt_trace_closest: null argument");
+    if (!s->built && s->n) return fail(CPT_ERR_NOT_BUILT, "cpt_trace_closest: build the LBVH first");
+    if (n == 0) return CPT_OK;
+    cudaStream_t stream = (cudaStream_t)stream_;
+    CPT_CUDA(cudaSetDevice(s->ctx->device));
+    SceneView v = view_of(s);
+    if (on_device) {
+        cpt_status st = launch_trace(v, rays, n, hits, s->err, stream);
+        if (st != CPT_OK) return st;
+        return CPT_OK;
+    }
+    cpt_ray* dr = nullptr;
+    cpt_hit* dh = nullptr;
+    CPT_CUDA(cudaMallocAsync((void**)&dr, n * sizeof(cpt_ray), stream));
+    CPT_CUDA(cudaMallocAsync((void**)&dh, n * sizeof(cpt_hit), stream));
+    CPT_CUDA(cudaMemcpyAsync(dr, rays, n * sizeof(cpt_ray), cudaMemcpyHostToDevice, stream));
+    cpt_status st = launch_trace(v, dr, n, dh, s->err, stream);
+    if (st == CPT_OK) CPT_CUDA(cudaMemcpyAsync(hits, dh, n * sizeof(cpt_hit), cudaMemcpyDeviceToHost, stream));
+    cudaFreeAsync(dr, stream);
+    cudaFreeAsync(dh, stream);
+    if (st != CPT_OK) return st;
+    return check_device_error(s, stream);
+}
+
+CPT_EXPORT cpt_status cpt_render(cpt_scene* s, const cpt_render_params* p, const cpt_render_output* out, void* stream_,
+                                 cpt_render_stats* stats)
+{
+    if (!s || !p || !out || !out->rgb) return fail(CPT_ERR_INVALID_ARGUMENT, "cpt_render: null argument");
+    if (!s->built && s->n) return fail(CPT_ERR_NOT_BUILT, "cpt_render: build the LBVH first");
+    if (p->spp <= 0) return fail(CPT_ERR_INVALID_ARGUMENT, "cpt_render: spp must be positive");
+    if (p->estimator != CPT_ESTIMATOR_REFERENCE && p->estimator != CPT_ESTIMATOR_CONFIG)
+        return fail(CPT_ERR_INVALID_ARGUMENT, "cpt_render: unknown estimator");
+    if (p->integrator != CPT_INTEGRATOR_MEGAKERNEL && p->integrator != CPT_INTEGRATOR_WAVEFRONT)
+        return fail(CPT_ERR_INVALID_ARGUMENT, "cpt_render: unknown integrator");
+    if (p->estimator == CPT_ESTIMATOR_CONFIG && !(p->rr_prob > 0.f && p->rr_prob <= 1.f))
+        return fail(CPT_ERR_INVALID_ARGUMENT, "cpt_render: rr_prob must be in (0, 1]");
+    int W = s->cam.width, H = s->cam.height;
+    int r0 = p->row_begin, r1 = p->row_end;
+    if (r0 == 0 && r1 == 0) r1 = H;
+    if (r0 < 0 || r1 > H || r0 > r1) return fail(CPT_ERR_INVALID_ARGUMENT, "cpt_render: bad row range");
+    cudaStream_t stream = (cudaStream_t)stream_;
+    CPT_CUDA(cudaSetDevice(s->ctx->device));
+    size_t np = (size_t)W * H;
+    float* rgb = out->rgb;
+    uint8_t* rgba8 = out->rgba8;
+    float* gbuf = out->gbuffer;
+    bool host = !out->on_device;
+    if (host) {
+        CPT_CUDA(cudaMallocAsync((void**)&rgb, np * 12, stream));
+        if (p->flags & CPT_RENDER_ACCUMULATE)
+            CPT_CUDA(cudaMemcpyAsync(rgb, out->rgb, np * 12, cudaMemcpyHostToDevice, stream));
+        if (out->rgba8) CPT_CUDA(cudaMallocAsync((void**)&rgba8, np * 4, stream));
+        if (out->gbuffer) CPT_CUDA(cudaMallocAsync((void**)&gbuf, np * 32, stream));
+    }
+    RenderArgs a;
+    a.spp = p->spp;
+    a.estimator = p->estimator;
+    a.max_depth = p->max_depth;
+    a.rr_depth = p->rr_depth;
+    a.rr_prob = p->rr_prob;
+    a.seed = p->seed;
+    a.row_begin = r0;
+    a.row_end = r1;
+    a.flags = p->flags;
+    a.rgb = rgb;
+    a.rgba8 = rgba8;
+    a.gbuf = gbuf;
+    a.ray_counter = s->ray_counter;
+    a.err = s->err;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (stats) {
+        CPT_CUDA(cudaEventCreate(&e0));
+        CPT_CUDA(cudaEventCreate(&e1));
+    }
+    CPT_CUDA(cudaMemsetAsync(s->ray_counter, 0, sizeof(unsigned long long), stream));
+    if (stats) CPT_CUDA(cudaEventRecord(e0, stream));
+    cpt_status st = launch_render_megakernel(view_of(s), a, stream, s->ctx->render_block_x, s->ctx->render_block_y);
+    if (stats) CPT_CUDA(cudaEventRecord(e1, stream));
+    if (st == CPT_OK && host) {
+        size_t off = (size_t)r0 * W, cnt = (size_t)(r1 - r0) * W;
+        CPT_CUDA(cudaMemcpyAsync(out->rgb + 3 * off, rgb + 3 * off, cnt * 12, cudaMemcpyDeviceToHost, stream));
+        if (out->rgba8) CPT_CUDA(cudaMemcpyAsync(out->rgba8 + 4 * off, rgba8 + 4 * off, cnt * 4, cudaMemcpyDeviceToHost, stream));
+        if (out->gbuffer) CPT_CUDA(cudaMemcpyAsync(out->gbuffer + 8 * off, gbuf + 8 * off, cnt * 32, cudaMemcpyDeviceToHost, stream));
+    }
+    if (host) {
+        cudaFreeAsync(rgb, stream);
+        if (out->rgba8) cudaFreeAsync(rgba8, stream);
+        if (out->gbuffer) cudaFreeAsync(gbuf, stream);
+    }
+    if (st != CPT_OK) return st;
+    if (stats) {
+        unsigned long long rays = 0;
+        CPT_CUDA(cudaMemcpyAsync(&rays, s->ray_counter, sizeof rays, cudaMemcpyDeviceToHost, stream));
+        CPT_CUDA(cudaEventSynchronize(e1));
+        float ms = 0;
+        CPT_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        CPT_CUDA(cudaStreamSynchronize(stream));
+        stats->rays = rays;
+        stats->paths = (uint64_t)(r1 - r0) * W * p->spp;
+        stats->ms = ms;
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+    }
+    if (host || stats) return check_device_error(s, stream);
+    return CPT_OK;
+}

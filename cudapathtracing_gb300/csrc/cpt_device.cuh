@@ -1,0 +1,108 @@
+// cpt_device.cuh — device-side types and FP32 maths shared by the LBVH, trace and render
+// kernels.  Float restatements of the reference's double3 helpers (rtmath.cuh:17-112).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define CPT_INF_F 999999.0f                 // INF (rtmath.cuh:8)
+#define CPT_PI_F 3.14159265358979323846f     // PI (rtmath.cuh:9)
+#define CPT_STACK 64                          // Karras trees over 64-bit keys are at most 65 levels deep
+
+// Primitive kinds stored in leaf records (w of the second float4).
+enum { CPT_KIND_TRI = 0, CPT_KIND_SPHERE = 1, CPT_KIND_LIGHT = 2 };
+
+// ------------------------------------------------------------------ float3 maths
+__host__ __device__ __forceinline__ float3 f3(float x, float y, float z) { return make_float3(x, y, z); }
+__host__ __device__ __forceinline__ float3 operator+(float3 a, float3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__host__ __device__ __forceinline__ float3 operator-(float3 a, float3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__host__ __device__ __forceinline__ float3 operator-(float3 a) { return f3(-a.x, -a.y, -a.z); }
+__host__ __device__ __forceinline__ float3 operator*(float3 a, float3 b) { return f3(a.x * b.x, a.y * b.y, a.z * b.z); }
+__host__ __device__ __forceinline__ float3 operator*(float t, float3 v) { return f3(v.x * t, v.y * t, v.z * t); }
+__host__ __device__ __forceinline__ float3 operator*(float3 v, float t) { return f3(v.x * t, v.y * t, v.z * t); }
+__host__ __device__ __forceinline__ float3 operator/(float3 v, float t) { return f3(v.x / t, v.y / t, v.z / t); }
+__host__ __device__ __forceinline__ float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__host__ __device__ __forceinline__ float len2(float3 v) { return v.x * v.x + v.y * v.y + v.z * v.z; }
+__host__ __device__ __forceinline__ float3 cross3(float3 a, float3 b)
+{
+    return f3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ float3 unit3(float3 v) { return v / sqrtf(len2(v)); }
+
+// ------------------------------------------------------------------ device scene types
+struct DevMaterial {   // Material (Material.cuh:5-22) in FP32
+    float3 color;
+    float ax, ay;
+    int type;
+    float eta;
+    float sigma_t, albedo;
+    float pad[3];
+};
+
+struct DevLight {      // Light (Hittable.cuh:346-366): centre, unit normal, edge frame
+    float3 center;
+    float w;
+    float3 normal;
+    float h;
+    float3 eu;
+    int visible;
+    float3 ev;
+    int pad0;
+    float3 color;
+    int pad1;
+};
+
+struct DevCamera {     // Camera (Camera.cu:5-40), derived in double on the host
+    float3 look_from;
+    float3 pixel_center;
+    float3 delta_h;
+    float3 delta_v;
+    float3 background;
+    int width, height;
+};
+
+// Read-only view of a built scene passed to trace/render kernels by value.
+struct SceneView {
+    int n_prims, n_lights, n_spheres, n_tris, n_internal;
+    const float4* __restrict__ nodes;      // BVH2: 4 float4 per internal node (Aila-Laine layout)
+    const float4* __restrict__ leaf_rec;   // 3 float4 per sorted leaf
+    const uint32_t* __restrict__ tri_mat;  // per triangle
+    const float* __restrict__ tri_n;       // optional smooth normals, 9 per triangle
+    const float4* __restrict__ spheres;    // centre xyz, radius
+    const uint32_t* __restrict__ sphere_mat;
+    const DevLight* __restrict__ lights;
+    const DevMaterial* __restrict__ mats;
+    DevCamera cam;
+};
+
+// ------------------------------------------------------------------ PCG32
+#ifdef __CUDACC__
+// PCG32 (O'Neill 2014, pcg32_srandom_r / pcg32_random_r); uniforms are (x + 1) * 2^-32 in
+// (0, 1], rounded once to FP32, the stand-in for curand_uniform_double (Render.cu:43).
+struct Pcg32 {
+    uint64_t state, inc;
+    __device__ __forceinline__ uint32_t next()
+    {
+        uint64_t old = state;
+        state = old * 6364136223846793005ULL + inc;
+        uint32_t xs = (uint32_t)(((old >> 18u) ^ old) >> 27u);
+        uint32_t rot = (uint32_t)(old >> 59u);
+        return __funnelshift_r(xs, xs, rot);
+    }
+    __device__ __forceinline__ void init(uint64_t seed, uint64_t stream)
+    {
+        state = 0u;
+        inc = (stream << 1u) | 1u;
+        next();
+        state += seed;
+        next();
+    }
+    __device__ __forceinline__ float uniform() { return __ull2float_rn((uint64_t)next() + 1ull) * 2.3283064365386963e-10f; }
+    // 1 - uniform(), computed from the integer so it is not lost to cancellation near 1.
+    __device__ __forceinline__ float one_minus_uniform_from(uint32_t x) { return __uint2float_rn(~x) * 2.3283064365386963e-10f; }
+};
+#endif
+
+// ------------------------------------------------------------------ error word
+// Device-side error flags set by kernels that hit a limit (stack, iteration budget).
+enum { CPT_DEVERR_STACK = 1, CPT_DEVERR_ITER = 2 };

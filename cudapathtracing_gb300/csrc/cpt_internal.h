@@ -1,0 +1,90 @@
+// cpt_internal.h — host-side internals of libcpt.so shared between translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "cpt.h"
+#include "cpt_device.cuh"
+
+#define CPT_EXPORT extern "C" __attribute__((visibility("default")))
+
+namespace cpt {
+
+// Thread-local text of the last failure (cpt_last_error_string).
+void set_error(const std::string& msg);
+cpt_status fail(cpt_status st, const std::string& msg);
+cpt_status cuda_fail(cudaError_t e, const char* what);
+
+#define CPT_CUDA(call)                                             \
+    do {                                                           \
+        cudaError_t _e = (call);                                   \
+        if (_e != cudaSuccess) return ::cpt::cuda_fail(_e, #call); \
+    } while (0)
+
+inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// Count of kernels this library has launched since it was loaded (cpt_launch_count).
+void add_launches(uint64_t k);
+
+// ---- LBVH build on caller-provided device buffers (lbvh.cu)
+struct LbvhBuffers {
+    uint64_t* keys;       // N, optional
+    uint32_t* order;      // N
+    int2* child;          // N-1: (child A, child B), leaf k encoded as ~k
+    int2* range;          // N-1: (first, last), optional
+    float4* node_box;     // 2*(N-1): min (w = 0), max
+    float4* leaf_box;     // 2*N, sorted leaf order
+};
+
+struct LbvhTimings {
+    float ms_prep, ms_sort, ms_emit, ms_refit;
+};
+
+size_t lbvh_scratch_bytes(uint32_t n);
+
+// Builds keys/order/topology/boxes.  Primitive i < n_extra takes its centroid (double) and
+// box from the extra arrays; primitive n_extra + t is triangle t of tri_f32 or tri_f64.
+cpt_status lbvh_build(uint32_t n_extra, const double* extra_centroid, const float4* extra_box, uint32_t n_tri,
+                      const float* tri_f32, const double* tri_f64, const double smin[3], const double smax[3],
+                      const LbvhBuffers& out, void* scratch, size_t scratch_bytes, cudaStream_t stream,
+                      LbvhTimings* timings);
+
+// Range-union refit only (topology and ranges kept, boxes recomputed from new leaf boxes).
+cpt_status lbvh_refit(uint32_t n, const LbvhBuffers& out, void* scratch, size_t scratch_bytes, cudaStream_t stream);
+
+// Leaf boxes in sorted order for a refit: prim boxes recomputed from the vertices.
+cpt_status lbvh_leaf_boxes(uint32_t n_extra, const float4* extra_box, uint32_t n_tri, const float* tri_f32,
+                           const double* tri_f64, const uint32_t* order, float4* leaf_box, uint32_t n,
+                           cudaStream_t stream);
+
+// ---- traversal layout (lbvh.cu)
+// BVH2 nodes (4 float4 per internal node) and leaf records (3 float4 per leaf).
+cpt_status build_trace_layout(uint32_t n, uint32_t n_lights, uint32_t n_spheres, const int2* child,
+                              const float4* node_box, const float4* leaf_box, const uint32_t* order,
+                              const float* tri_f32, const double* tri_f64, const float4* spheres, float4* nodes,
+                              float4* leaf_rec, cudaStream_t stream);
+
+// ---- trace / render launchers (trace.cu, render.cu)
+cpt_status launch_trace(const SceneView& view, const cpt_ray* rays, uint64_t n, cpt_hit* hits, int* d_err,
+                        cudaStream_t stream);
+
+struct RenderArgs {
+    int spp, estimator, max_depth, rr_depth;
+    float rr_prob;
+    uint64_t seed;
+    int row_begin, row_end;
+    int flags;
+    float* rgb;
+    uint8_t* rgba8;
+    float* gbuf;
+    unsigned long long* ray_counter;
+    int* err;
+};
+
+cpt_status launch_render_megakernel(const SceneView& view, const RenderArgs& args, cudaStream_t stream, int block_x,
+                                    int block_y);
+
+}  // namespace cpt

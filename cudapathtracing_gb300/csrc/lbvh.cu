@@ -1,0 +1,711 @@
+// lbvh.cu — LBVH construction on the GPU (Device::buildBVH, Device.cuh:169-195).
+//
+//   k_prep        centroid (FP64) + Morton code + leaf box per primitive
+//                 (generateMortonCodes Device.cuh:134-142, morton3D BVH.cuh:23-41,
+//                  Hittable ctors Hittable.cuh:456-462)
+//   radix sort    stable LSD over the 30-bit codes, 8-bit digits, per-tile ranking with
+//                 __match_any_sync (replaces thrust::sort_by_key Device.cuh:187-189: keys are
+//                 code<<32|index, so a stable sort of codes with ascending indices is the
+//                 same permutation)
+//   k_emit        Karras 2012 range/split per internal node (generateHierarchy BVH.cuh:174-241)
+//   refit         atomic-free: an internal node covers the contiguous sorted leaves
+//                 [first, last], so its box is a range union, answered from 32-ary block
+//                 unions of the leaf boxes (replaces the serial constructAABB BVH.cuh:243-280;
+//                 min/max is exact, so the boxes equal the pairwise unions)
+//
+// All boxes are FP32 rounded outwards from the reference's FP64 boxes.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+
+#include "cpt_internal.h"
+
+namespace cpt {
+
+namespace {
+
+constexpr int RS_THREADS = 256;
+constexpr int RS_WARPS = RS_THREADS / 32;
+constexpr int RS_ITEMS = 16;
+constexpr int RS_TILE = RS_THREADS * RS_ITEMS;   // 4096 keys per tile
+constexpr int RS_BINS = 256;
+constexpr int RS_PASSES = 4;                     // bits 0-7, 8-15, 16-23, 24-29
+constexpr int MAX_LEVELS = 8;
+
+__device__ __forceinline__ uint32_t expand_bits(uint32_t v)   // BVH.cuh:12-19
+{
+    v = (v * 0x00010001u) & 0xFF0000FFu;
+    v = (v * 0x00000101u) & 0x0F00F00Fu;
+    v = (v * 0x00000011u) & 0xC30C30C3u;
+    v = (v * 0x00000005u) & 0x49249249u;
+    return v;
+}
+
+// morton3D (BVH.cuh:23-41) in double with explicitly rounded operations (no contraction).
+__device__ __forceinline__ uint32_t morton_axis(double c, double mn, double mx)
+{
+    double nrm = __ddiv_rn(__dsub_rn(c, mn), __dsub_rn(mx, mn));
+    double x = __dmul_rn(nrm, 1024.0);
+    x = x > 0.0 ? x : 0.0;        // mMax(x, 0.0): NaN -> 0
+    x = x < 1023.0 ? x : 1023.0;  // mMin(x, 1023.0)
+    return (uint32_t)x;
+}
+
+__device__ __forceinline__ double dmin(double a, double b) { return a < b ? a : b; }   // mMin
+__device__ __forceinline__ double dmax(double a, double b) { return a > b ? a : b; }   // mMax
+
+template <typename VT>
+__device__ __forceinline__ void load_tri(const VT* __restrict__ v, uint32_t t, double p[9])
+{
+#pragma unroll
+    for (int k = 0; k < 9; ++k) p[k] = (double)v[9ull * t + k];
+}
+
+// Triangle centroid and padded box (Hittable.cuh:459-461, AABB.cuh:30-40), boxes rounded
+// outwards to FP32.
+__device__ __forceinline__ void tri_center_box(const double p[9], double c[3], float4& bmin, float4& bmax)
+{
+    double mn[3], mx[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        c[a] = __ddiv_rn(__dadd_rn(__dadd_rn(p[a], p[3 + a]), p[6 + a]), 3.0);
+        mn[a] = __dsub_rn(dmin(dmin(p[a], p[3 + a]), p[6 + a]), 0.0001);
+        mx[a] = __dadd_rn(dmax(dmax(p[a], p[3 + a]), p[6 + a]), 0.0001);
+    }
+    bmin = make_float4(__double2float_rd(mn[0]), __double2float_rd(mn[1]), __double2float_rd(mn[2]), 0.f);
+    bmax = make_float4(__double2float_ru(mx[0]), __double2float_ru(mx[1]), __double2float_ru(mx[2]), 0.f);
+}
+
+template <typename VT>
+__global__ void k_prep(uint32_t n_extra, const double* __restrict__ extra_c, const float4* __restrict__ extra_box,
+                       uint32_t n_tri, const VT* __restrict__ tri_v, double3 smin, double3 smax,
+                       uint32_t* __restrict__ code, uint32_t* __restrict__ idx, float4* __restrict__ box)
+{
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t n = n_extra + n_tri;
+    if (i >= n) return;
+    double c[3];
+    float4 bmin, bmax;
+    if (i < n_extra) {
+        c[0] = extra_c[3ull * i];
+        c[1] = extra_c[3ull * i + 1];
+        c[2] = extra_c[3ull * i + 2];
+        bmin = extra_box[2ull * i];
+        bmax = extra_box[2ull * i + 1];
+    } else {
+        double p[9];
+        load_tri(tri_v, i - n_extra, p);
+        tri_center_box(p, c, bmin, bmax);
+    }
+    uint32_t xx = expand_bits(morton_axis(c[0], smin.x, smax.x));
+    uint32_t yy = expand_bits(morton_axis(c[1], smin.y, smax.y));
+    uint32_t zz = expand_bits(morton_axis(c[2], smin.z, smax.z));
+    code[i] = xx * 4 + yy * 2 + zz;
+    idx[i] = i;
+    box[2ull * i] = bmin;
+    box[2ull * i + 1] = bmax;
+}
+
+template <typename VT>
+__global__ void k_prim_boxes(uint32_t n_extra, const float4* __restrict__ extra_box, uint32_t n_tri,
+                             const VT* __restrict__ tri_v, const uint32_t* __restrict__ order,
+                             float4* __restrict__ leaf_box, uint32_t n)
+{
+    uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    uint32_t i = order[k];
+    float4 bmin, bmax;
+    if (i < n_extra) {
+        bmin = extra_box[2ull * i];
+        bmax = extra_box[2ull * i + 1];
+    } else {
+        double p[9], c[3];
+        load_tri(tri_v, i - n_extra, p);
+        tri_center_box(p, c, bmin, bmax);
+    }
+    leaf_box[2ull * k] = bmin;
+    leaf_box[2ull * k + 1] = bmax;
+}
+
+// ---------------------------------------------------------------- radix sort
+// Digit totals of all passes (they do not depend on the order): totals[pass][digit].
+__global__ void k_digit_totals(const uint32_t* __restrict__ code, uint32_t n, uint32_t* __restrict__ totals)
+{
+    __shared__ uint32_t h[RS_PASSES][RS_BINS];
+    for (int t = threadIdx.x; t < RS_PASSES * RS_BINS; t += blockDim.x) (&h[0][0])[t] = 0;
+    __syncthreads();
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint32_t c = code[i];
+#pragma unroll
+        for (int p = 0; p < RS_PASSES; ++p) atomicAdd(&h[p][(c >> (8 * p)) & 255u], 1u);
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < RS_PASSES * RS_BINS; t += blockDim.x) {
+        uint32_t v = (&h[0][0])[t];
+        if (v) atomicAdd(&totals[t], v);
+    }
+}
+
+__device__ __forceinline__ uint32_t lanemask_lt()
+{
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// Per-tile digit counts, digit-major: counts[d * num_tiles + tile].  Each warp aggregates
+// equal digits with __match_any_sync; the group leader adds to the warp's private row.
+__global__ void __launch_bounds__(RS_THREADS) k_radix_hist(const uint32_t* __restrict__ keys, uint32_t n, int shift,
+                                                           uint32_t* __restrict__ counts, uint32_t num_tiles)
+{
+    __shared__ uint32_t wh[RS_WARPS][RS_BINS];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int t = threadIdx.x; t < RS_WARPS * RS_BINS; t += RS_THREADS) (&wh[0][0])[t] = 0;
+    __syncthreads();
+    const uint32_t tile = blockIdx.x;
+    const uint32_t base = tile * RS_TILE + w * 32 * RS_ITEMS;
+#pragma unroll 4
+    for (int it = 0; it < RS_ITEMS; ++it) {
+        uint32_t e = base + it * 32 + lane;
+        uint32_t d = e < n ? (keys[e] >> shift) & 255u : 256u;
+        uint32_t peers = __match_any_sync(0xffffffffu, d);
+        if (d < 256u && lane == __ffs(peers) - 1) wh[w][d] += __popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    for (int d = threadIdx.x; d < RS_BINS; d += RS_THREADS) {
+        uint32_t s = 0;
+#pragma unroll
+        for (int k = 0; k < RS_WARPS; ++k) s += wh[k][d];
+        counts[(size_t)d * num_tiles + tile] = s;
+    }
+}
+
+// Exclusive scan of counts into global offsets.  Block d scans row d and adds the number
+// of keys with a smaller digit (from the pass's totals).
+__global__ void __launch_bounds__(256) k_radix_scan(uint32_t* __restrict__ counts, uint32_t num_tiles,
+                                                    const uint32_t* __restrict__ totals)
+{
+    __shared__ uint32_t s_part[8];
+    __shared__ uint32_t s_carry;
+    const int d = blockIdx.x;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint32_t b = (threadIdx.x < (unsigned)d) ? totals[threadIdx.x] : 0u;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) b += __shfl_xor_sync(0xffffffffu, b, o);
+    if (lane == 0) s_part[w] = b;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t s = 0;
+        for (int k = 0; k < 8; ++k) s += s_part[k];
+        s_carry = s;
+    }
+    __syncthreads();
+    uint32_t* row = counts + (size_t)d * num_tiles;
+    for (uint32_t start = 0; start < num_tiles; start += 256) {
+        uint32_t i = start + threadIdx.x;
+        uint32_t v = i < num_tiles ? row[i] : 0u;
+        uint32_t x = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        __syncthreads();
+        if (lane == 31) s_part[w] = x;
+        __syncthreads();
+        uint32_t wpre = 0;
+        for (int k = 0; k < w; ++k) wpre += s_part[k];
+        uint32_t carry = s_carry;
+        if (i < num_tiles) row[i] = carry + wpre + x - v;
+        __syncthreads();
+        if (threadIdx.x == 255) s_carry = carry + wpre + x;
+        __syncthreads();
+    }
+}
+
+// Stable scatter: rank each key within its tile (warp-ordered, lane-ordered), stage the tile
+// in shared memory in sorted order, then write runs to their global offsets.
+__global__ void __launch_bounds__(RS_THREADS) k_radix_scatter(const uint32_t* __restrict__ keys_in,
+                                                              const uint32_t* __restrict__ vals_in,
+                                                              uint32_t* __restrict__ keys_out,
+                                                              uint32_t* __restrict__ vals_out, uint32_t n, int shift,
+                                                              const uint32_t* __restrict__ offsets, uint32_t num_tiles)
+{
+    __shared__ uint32_t wh[RS_WARPS][RS_BINS];
+    __shared__ uint32_t s_start[RS_BINS];
+    __shared__ uint32_t s_gofs[RS_BINS];
+    __shared__ uint32_t s_keys[RS_TILE];
+    __shared__ uint32_t s_vals[RS_TILE];
+    __shared__ uint32_t s_wsum[RS_WARPS];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int t = threadIdx.x; t < RS_WARPS * RS_BINS; t += RS_THREADS) (&wh[0][0])[t] = 0;
+    __syncthreads();
+    const uint32_t tile = blockIdx.x;
+    const uint32_t base = tile * RS_TILE + w * 32 * RS_ITEMS;
+    const uint32_t lt = lanemask_lt();
+    uint32_t k[RS_ITEMS], v[RS_ITEMS], rank[RS_ITEMS];
+#pragma unroll
+    for (int it = 0; it < RS_ITEMS; ++it) {
+        uint32_t e = base + it * 32 + lane;
+        bool valid = e < n;
+        k[it] = valid ? keys_in[e] : 0u;
+        v[it] = valid ? vals_in[e] : 0u;
+        uint32_t d = valid ? (k[it] >> shift) & 255u : 256u;
+        uint32_t peers = __match_any_sync(0xffffffffu, d);
+        int leader = __ffs(peers) - 1;
+        uint32_t old = (lane == leader && valid) ? wh[w][d] : 0u;
+        old = __shfl_sync(0xffffffffu, old, leader);
+        if (lane == leader && valid) wh[w][d] = old + __popc(peers);
+        rank[it] = old + __popc(peers & lt);
+        __syncwarp();
+    }
+    __syncthreads();
+    // Per digit: exclusive prefix over warps (in place) and the tile's count.
+    uint32_t cnt;
+    {
+        const int d = threadIdx.x;
+        uint32_t run = 0;
+#pragma unroll
+        for (int q = 0; q < RS_WARPS; ++q) {
+            uint32_t c = wh[q][d];
+            wh[q][d] = run;
+            run += c;
+        }
+        cnt = run;
+        s_gofs[d] = offsets[(size_t)d * num_tiles + tile];
+    }
+    // Block exclusive scan of the 256 counts -> s_start.
+    uint32_t x = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_wsum[w] = x;
+    __syncthreads();
+    uint32_t wpre = 0;
+    for (int q = 0; q < w; ++q) wpre += s_wsum[q];
+    s_start[threadIdx.x] = wpre + x - cnt;
+    __syncthreads();
+#pragma unroll
+    for (int it = 0; it < RS_ITEMS; ++it) {
+        uint32_t e = base + it * 32 + lane;
+        if (e < n) {
+            uint32_t d = (k[it] >> shift) & 255u;
+            uint32_t pos = s_start[d] + wh[w][d] + rank[it];
+            s_keys[pos] = k[it];
+            s_vals[pos] = v[it];
+        }
+    }
+    __syncthreads();
+    uint32_t tile_n = min((uint32_t)RS_TILE, n - tile * RS_TILE);
+    for (uint32_t p = threadIdx.x; p < tile_n; p += RS_THREADS) {
+        uint32_t kk = s_keys[p];
+        uint32_t d = (kk >> shift) & 255u;
+        uint32_t g = s_gofs[d] + (p - s_start[d]);
+        keys_out[g] = kk;
+        vals_out[g] = s_vals[p];
+    }
+}
+
+// ---------------------------------------------------------------- Karras emission
+__device__ __forceinline__ uint64_t key_at(const uint32_t* __restrict__ code, const uint32_t* __restrict__ order, int j)
+{
+    return ((uint64_t)code[j] << 32) | (uint64_t)order[j];
+}
+
+__device__ __forceinline__ int delta_k(const uint32_t* code, const uint32_t* order, int n, uint64_t ki, int j)   // BVH.cuh:120-128
+{
+    if (j < 0 || j >= n) return -1;
+    uint64_t kj = key_at(code, order, j);
+    if (ki == kj) return 64;
+    return __clzll((long long)(ki ^ kj));
+}
+
+__global__ void k_emit(const uint32_t* __restrict__ code, const uint32_t* __restrict__ order, int n,
+                       int2* __restrict__ child, int2* __restrict__ range)
+{
+    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= n - 1) return;
+    // determineRange (BVH.cuh:130-172)
+    uint64_t ki = key_at(code, order, idx);
+    int dn = delta_k(code, order, n, ki, idx + 1);
+    int dp = delta_k(code, order, n, ki, idx - 1);
+    int d = (dn > dp) ? 1 : -1;
+    int dmin_ = delta_k(code, order, n, ki, idx - d);
+    int lmax = 2;
+    while (delta_k(code, order, n, ki, idx + lmax * d) > dmin_) lmax *= 2;
+    int l = 0;
+    for (int t = lmax / 2; t >= 1; t /= 2)
+        if (delta_k(code, order, n, ki, idx + (l + t) * d) > dmin_) l += t;
+    int j = idx + l * d;
+    int first = min(idx, j), last = max(idx, j);
+    // findSplit (BVH.cuh:81-118)
+    uint64_t fc = key_at(code, order, first), lc = key_at(code, order, last);
+    int split;
+    if (fc == lc) {
+        split = (first + last) >> 1;
+    } else {
+        int common = __clzll((long long)(fc ^ lc));
+        split = first;
+        int step = last - first;
+        do {
+            step = (step + 1) >> 1;
+            int ns = split + step;
+            if (ns < last) {
+                if (__clzll((long long)(fc ^ key_at(code, order, ns))) > common) split = ns;
+            }
+        } while (step > 1);
+    }
+    int a = (split == first) ? ~split : split;
+    int b = (split + 1 == last) ? ~(split + 1) : split + 1;
+    child[idx] = make_int2(a, b);
+    if (range) range[idx] = make_int2(first, last);
+}
+
+// Sorted leaf boxes and (optionally) the reference's 64-bit keys.
+__global__ void k_leaves(const uint32_t* __restrict__ code, const uint32_t* __restrict__ order, uint32_t n,
+                         const float4* __restrict__ box_unsorted, float4* __restrict__ leaf_box,
+                         uint64_t* __restrict__ keys)
+{
+    uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    uint32_t p = order[k];
+    leaf_box[2ull * k] = box_unsorted[2ull * p];
+    leaf_box[2ull * k + 1] = box_unsorted[2ull * p + 1];
+    if (keys) keys[k] = ((uint64_t)code[k] << 32) | p;
+}
+
+// ---------------------------------------------------------------- range-union refit
+__device__ __forceinline__ void box_union(float4& mn, float4& mx, float4 a, float4 b)
+{
+    mn.x = fminf(mn.x, a.x); mn.y = fminf(mn.y, a.y); mn.z = fminf(mn.z, a.z);
+    mx.x = fmaxf(mx.x, b.x); mx.y = fmaxf(mx.y, b.y); mx.z = fmaxf(mx.z, b.z);
+}
+
+// out[b] = union(in[32b .. 32b+31]); one warp per output box.
+__global__ void k_reduce32(const float4* __restrict__ in, uint32_t nin, float4* __restrict__ out, uint32_t nout)
+{
+    uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int lane = threadIdx.x & 31;
+    if (gw >= nout) return;
+    uint32_t e = gw * 32 + lane;
+    float4 mn = make_float4(INFINITY, INFINITY, INFINITY, 0.f), mx = make_float4(-INFINITY, -INFINITY, -INFINITY, 0.f);
+    if (e < nin) { mn = in[2ull * e]; mx = in[2ull * e + 1]; }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        mn.x = fminf(mn.x, __shfl_xor_sync(0xffffffffu, mn.x, o));
+        mn.y = fminf(mn.y, __shfl_xor_sync(0xffffffffu, mn.y, o));
+        mn.z = fminf(mn.z, __shfl_xor_sync(0xffffffffu, mn.z, o));
+        mx.x = fmaxf(mx.x, __shfl_xor_sync(0xffffffffu, mx.x, o));
+        mx.y = fmaxf(mx.y, __shfl_xor_sync(0xffffffffu, mx.y, o));
+        mx.z = fmaxf(mx.z, __shfl_xor_sync(0xffffffffu, mx.z, o));
+    }
+    if (lane == 0) { out[2ull * gw] = mn; out[2ull * gw + 1] = mx; }
+}
+
+struct Levels {
+    const float4* lv[MAX_LEVELS];
+    uint32_t n[MAX_LEVELS];
+    int count;
+};
+
+// Union of leaf boxes [lo, hi) (exclusive hi) from the block-union hierarchy: partial blocks
+// at each level, then move up one level with the aligned middle.
+__device__ __forceinline__ void range_union(const Levels& L, uint32_t lo, uint32_t hi, float4& mn, float4& mx)
+{
+    mn = make_float4(INFINITY, INFINITY, INFINITY, 0.f);
+    mx = make_float4(-INFINITY, -INFINITY, -INFINITY, 0.f);
+    for (int l = 0; l < L.count; ++l) {
+        const float4* a = L.lv[l];
+        uint32_t lo_up = (lo + 31u) & ~31u, hi_dn = hi & ~31u;
+        if (l == L.count - 1 || lo_up >= hi_dn) {
+            for (uint32_t x = lo; x < hi; ++x) box_union(mn, mx, a[2ull * x], a[2ull * x + 1]);
+            return;
+        }
+        for (uint32_t x = lo; x < lo_up; ++x) box_union(mn, mx, a[2ull * x], a[2ull * x + 1]);
+        for (uint32_t x = hi_dn; x < hi; ++x) box_union(mn, mx, a[2ull * x], a[2ull * x + 1]);
+        lo = lo_up >> 5;
+        hi = hi_dn >> 5;
+    }
+}
+
+__global__ void k_node_boxes(Levels L, const int2* __restrict__ range, uint32_t n_internal, float4* __restrict__ node_box)
+{
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_internal) return;
+    int2 r = range[i];
+    float4 mn, mx;
+    range_union(L, (uint32_t)r.x, (uint32_t)r.y + 1u, mn, mx);
+    node_box[2ull * i] = mn;
+    node_box[2ull * i + 1] = mx;
+}
+
+// ---------------------------------------------------------------- traversal layout
+// BVH2 node i: (A.lo.x, A.hi.x, A.lo.y, A.hi.y), (B.lo.x, B.hi.x, B.lo.y, B.hi.y),
+// (A.lo.z, A.hi.z, B.lo.z, B.hi.z), (childA, childB, 0, 0) — 64 bytes, four 16-byte loads.
+__global__ void k_bvh2_nodes(const int2* __restrict__ child, const float4* __restrict__ node_box,
+                             const float4* __restrict__ leaf_box, uint32_t n_internal, float4* __restrict__ nodes)
+{
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_internal) return;
+    int2 c = child[i];
+    const float4* ba = c.x < 0 ? leaf_box + 2ull * (uint32_t)(~c.x) : node_box + 2ull * (uint32_t)c.x;
+    const float4* bb = c.y < 0 ? leaf_box + 2ull * (uint32_t)(~c.y) : node_box + 2ull * (uint32_t)c.y;
+    float4 amn = ba[0], amx = ba[1], bmn = bb[0], bmx = bb[1];
+    nodes[4ull * i + 0] = make_float4(amn.x, amx.x, amn.y, amx.y);
+    nodes[4ull * i + 1] = make_float4(bmn.x, bmx.x, bmn.y, bmx.y);
+    nodes[4ull * i + 2] = make_float4(amn.z, amx.z, bmn.z, bmx.z);
+    nodes[4ull * i + 3] = make_float4(__int_as_float(c.x), __int_as_float(c.y), 0.f, 0.f);
+}
+
+// Leaf record k (48 bytes) for primitive order[k]:
+//   triangle: (p0, id), (p1 - p0, TRI), (p2 - p0, 0)   edges formed in double, rounded once
+//   sphere:   (centre, id), (radius, 0, 0, SPHERE), 0
+//   light:    (0, 0, 0, id), (light index, 0, 0, LIGHT), 0
+template <typename VT>
+__global__ void k_leaf_records(const uint32_t* __restrict__ order, uint32_t n, uint32_t n_lights, uint32_t n_spheres,
+                               const VT* __restrict__ tri_v, const float4* __restrict__ spheres,
+                               float4* __restrict__ rec)
+{
+    uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    uint32_t p = order[k];
+    float4 r0, r1, r2 = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (p < n_lights) {
+        r0 = make_float4(0.f, 0.f, 0.f, __int_as_float((int)p));
+        r1 = make_float4(__int_as_float((int)p), 0.f, 0.f, __int_as_float(CPT_KIND_LIGHT));
+    } else if (p < n_lights + n_spheres) {
+        float4 s = spheres[p - n_lights];
+        r0 = make_float4(s.x, s.y, s.z, __int_as_float((int)p));
+        r1 = make_float4(s.w, 0.f, 0.f, __int_as_float(CPT_KIND_SPHERE));
+    } else {
+        double q[9];
+        load_tri(tri_v, p - n_lights - n_spheres, q);
+        r0 = make_float4((float)q[0], (float)q[1], (float)q[2], __int_as_float((int)p));
+        r1 = make_float4((float)(q[3] - q[0]), (float)(q[4] - q[1]), (float)(q[5] - q[2]), __int_as_float(CPT_KIND_TRI));
+        r2 = make_float4((float)(q[6] - q[0]), (float)(q[7] - q[1]), (float)(q[8] - q[2]), 0.f);
+    }
+    rec[3ull * k] = r0;
+    rec[3ull * k + 1] = r1;
+    rec[3ull * k + 2] = r2;
+}
+
+inline unsigned blocks_for(uint64_t n, unsigned t) { return (unsigned)((n + t - 1) / t); }
+
+struct ScratchLayout {
+    size_t code0, code1, val1, counts, totals, box_unsorted, levels, total;
+    uint32_t num_tiles;
+    uint32_t level_n[MAX_LEVELS];
+    int level_count;
+};
+
+ScratchLayout layout_for(uint32_t n)
+{
+    ScratchLayout L;
+    std::memset(&L, 0, sizeof L);
+    size_t off = 0;
+    auto take = [&](size_t bytes) { size_t o = off; off = align_up(off + bytes, 256); return o; };
+    L.num_tiles = (n + RS_TILE - 1) / RS_TILE;
+    L.code0 = take((size_t)n * 4);
+    L.code1 = take((size_t)n * 4);
+    L.val1 = take((size_t)n * 4);
+    L.counts = take((size_t)RS_BINS * std::max(1u, L.num_tiles) * 4);
+    L.totals = take((size_t)RS_PASSES * RS_BINS * 4);
+    L.box_unsorted = take((size_t)n * 32);
+    // Block-union levels above the sorted leaf boxes: ceil(n/32), ceil(n/1024), ... down to 1.
+    uint32_t m = n;
+    L.level_count = 0;
+    size_t lv_bytes = 0;
+    while (m > 1 && L.level_count < MAX_LEVELS - 1) {
+        m = (m + 31) / 32;
+        L.level_n[L.level_count++] = m;
+        lv_bytes = align_up(lv_bytes + (size_t)m * 32, 256);
+    }
+    L.levels = take(lv_bytes);
+    L.total = off;
+    return L;
+}
+
+cpt_status refit_from_leaves(uint32_t n, const ScratchLayout& SL, char* base, const int2* range, float4* node_box,
+                             const float4* leaf_box, cudaStream_t stream)
+{
+    if (n < 2) return CPT_OK;
+    Levels L;
+    std::memset(&L, 0, sizeof L);
+    L.lv[0] = leaf_box;
+    L.n[0] = n;
+    L.count = 1;
+    float4* lvp = (float4*)(base + SL.levels);
+    const float4* prev = leaf_box;
+    uint32_t prev_n = n;
+    for (int l = 0; l < SL.level_count; ++l) {
+        uint32_t m = SL.level_n[l];
+        k_reduce32<<<blocks_for((uint64_t)m * 32, 256), 256, 0, stream>>>(prev, prev_n, lvp, m);
+        L.lv[L.count] = lvp;
+        L.n[L.count] = m;
+        L.count++;
+        prev = lvp;
+        prev_n = m;
+        lvp = (float4*)((char*)lvp + align_up((size_t)m * 32, 256));
+    }
+    k_node_boxes<<<blocks_for(n - 1, 256), 256, 0, stream>>>(L, range, n - 1, node_box);
+    add_launches(SL.level_count + 1);
+    CPT_CUDA(cudaGetLastError());
+    return CPT_OK;
+}
+
+}  // namespace
+
+size_t lbvh_scratch_bytes(uint32_t n) { return layout_for(std::max(n, 1u)).total; }
+
+cpt_status lbvh_build(uint32_t n_extra, const double* extra_centroid, const float4* extra_box, uint32_t n_tri,
+                      const float* tri_f32, const double* tri_f64, const double smin_in[3], const double smax_in[3],
+                      const LbvhBuffers& out, void* scratch, size_t scratch_bytes, cudaStream_t stream,
+                      LbvhTimings* timings)
+{
+    uint64_t n64 = (uint64_t)n_extra + n_tri;
+    if (n64 == 0) return CPT_OK;
+    if (n64 > 0x7fffffffull) return fail(CPT_ERR_INVALID_ARGUMENT, "lbvh_build: too many primitives");
+    uint32_t n = (uint32_t)n64;
+    if (n_tri && !tri_f32 && !tri_f64) return fail(CPT_ERR_INVALID_ARGUMENT, "lbvh_build: no triangle vertices");
+    if (n_extra && (!extra_centroid || !extra_box)) return fail(CPT_ERR_INVALID_ARGUMENT, "lbvh_build: extra prims");
+    if (!out.order || !out.leaf_box || (n > 1 && (!out.child || !out.node_box || !out.range)))
+        return fail(CPT_ERR_INVALID_ARGUMENT, "lbvh_build: missing output buffer");
+    ScratchLayout SL = layout_for(n);
+    if (!scratch || scratch_bytes < SL.total || ((uintptr_t)scratch & 255u))
+        return fail(CPT_ERR_INVALID_ARGUMENT, "lbvh_build: scratch too small or not 256-byte aligned");
+    char* base = (char*)scratch;
+    uint32_t* code0 = (uint32_t*)(base + SL.code0);
+    uint32_t* code1 = (uint32_t*)(base + SL.code1);
+    uint32_t* val0 = out.order;   // the final values land in order[] after an even number of passes
+    uint32_t* val1 = (uint32_t*)(base + SL.val1);
+    uint32_t* counts = (uint32_t*)(base + SL.counts);
+    uint32_t* totals = (uint32_t*)(base + SL.totals);
+    float4* box_unsorted = (float4*)(base + SL.box_unsorted);
+
+    // Device::buildBVH: expand the mesh bounds by 1, fall back to [-20,20]^3 (Device.cuh:174-181).
+    double3 smin = make_double3(smin_in[0] - 1.0, smin_in[1] - 1.0, smin_in[2] - 1.0);
+    double3 smax = make_double3(smax_in[0] + 1.0, smax_in[1] + 1.0, smax_in[2] + 1.0);
+    if (smin.x > smax.x) {
+        smin = make_double3(-20.0, -20.0, -20.0);
+        smax = make_double3(20.0, 20.0, 20.0);
+    }
+
+    cudaEvent_t ev[5];
+    if (timings)
+        for (auto& e : ev) CPT_CUDA(cudaEventCreate(&e));
+    if (timings) CPT_CUDA(cudaEventRecord(ev[0], stream));
+    if (tri_f64)
+        k_prep<double><<<blocks_for(n, 256), 256, 0, stream>>>(n_extra, extra_centroid, extra_box, n_tri, tri_f64, smin,
+                                                               smax, code0, val0, box_unsorted);
+    else
+        k_prep<float><<<blocks_for(n, 256), 256, 0, stream>>>(n_extra, extra_centroid, extra_box, n_tri, tri_f32, smin,
+                                                              smax, code0, val0, box_unsorted);
+    CPT_CUDA(cudaGetLastError());
+    add_launches(1);
+    if (timings) CPT_CUDA(cudaEventRecord(ev[1], stream));
+
+    // Radix sort: 4 passes of 8 bits; keys/values ping-pong code0/val0 <-> code1/val1 and end
+    // in code0/val0 (= out.order).
+    CPT_CUDA(cudaMemsetAsync(totals, 0, RS_PASSES * RS_BINS * 4, stream));
+    k_digit_totals<<<std::min(blocks_for(n, 256), 1024u), 256, 0, stream>>>(code0, n, totals);
+    uint32_t* kin = code0;
+    uint32_t* vin = val0;
+    uint32_t* kout = code1;
+    uint32_t* vout = val1;
+    for (int p = 0; p < RS_PASSES; ++p) {
+        k_radix_hist<<<SL.num_tiles, RS_THREADS, 0, stream>>>(kin, n, 8 * p, counts, SL.num_tiles);
+        k_radix_scan<<<RS_BINS, 256, 0, stream>>>(counts, SL.num_tiles, totals + p * RS_BINS);
+        k_radix_scatter<<<SL.num_tiles, RS_THREADS, 0, stream>>>(kin, vin, kout, vout, n, 8 * p, counts, SL.num_tiles);
+        std::swap(kin, kout);
+        std::swap(vin, vout);
+    }
+    CPT_CUDA(cudaGetLastError());
+    add_launches(1 + 3 * RS_PASSES);
+    if (timings) CPT_CUDA(cudaEventRecord(ev[2], stream));
+
+    // Emission + sorted leaf boxes.
+    if (n > 1) k_emit<<<blocks_for(n - 1, 256), 256, 0, stream>>>(kin, vin, (int)n, out.child, out.range);
+    k_leaves<<<blocks_for(n, 256), 256, 0, stream>>>(kin, vin, n, box_unsorted, out.leaf_box, out.keys);
+    CPT_CUDA(cudaGetLastError());
+    add_launches((n > 1 ? 1 : 0) + 1);
+    if (timings) CPT_CUDA(cudaEventRecord(ev[3], stream));
+
+    cpt_status st = refit_from_leaves(n, SL, base, out.range, out.node_box, out.leaf_box, stream);
+    if (st != CPT_OK) return st;
+    if (timings) {
+        CPT_CUDA(cudaEventRecord(ev[4], stream));
+        CPT_CUDA(cudaEventSynchronize(ev[4]));
+        CPT_CUDA(cudaEventElapsedTime(&timings->ms_prep, ev[0], ev[1]));
+        CPT_CUDA(cudaEventElapsedTime(&timings->ms_sort, ev[1], ev[2]));
+        CPT_CUDA(cudaEventElapsedTime(&timings->ms_emit, ev[2], ev[3]));
+        CPT_CUDA(cudaEventElapsedTime(&timings->ms_refit, ev[3], ev[4]));
+        for (auto& e : ev) cudaEventDestroy(e);
+    }
+    return CPT_OK;
+}
+
+cpt_status lbvh_leaf_boxes(uint32_t n_extra, const float4* extra_box, uint32_t n_tri, const float* tri_f32,
+                           const double* tri_f64, const uint32_t* order, float4* leaf_box, uint32_t n,
+                           cudaStream_t stream)
+{
+    if (n == 0) return CPT_OK;
+    if (tri_f64)
+        k_prim_boxes<double><<<blocks_for(n, 256), 256, 0, stream>>>(n_extra, extra_box, n_tri, tri_f64, order, leaf_box, n);
+    else
+        k_prim_boxes<float><<<blocks_for(n, 256), 256, 0, stream>>>(n_extra, extra_box, n_tri, tri_f32, order, leaf_box, n);
+    CPT_CUDA(cudaGetLastError());
+    add_launches(1);
+    return CPT_OK;
+}
+
+cpt_status lbvh_refit(uint32_t n, const LbvhBuffers& out, void* scratch, size_t scratch_bytes, cudaStream_t stream)
+{
+    ScratchLayout SL = layout_for(std::max(n, 1u));
+    if (!scratch || scratch_bytes < SL.total) return fail(CPT_ERR_INVALID_ARGUMENT, "lbvh_refit: scratch too small");
+    return refit_from_leaves(n, SL, (char*)scratch, out.range, out.node_box, out.leaf_box, stream);
+}
+
+cpt_status build_trace_layout(uint32_t n, uint32_t n_lights, uint32_t n_spheres, const int2* child,
+                              const float4* node_box, const float4* leaf_box, const uint32_t* order,
+                              const float* tri_f32, const double* tri_f64, const float4* spheres, float4* nodes,
+                              float4* leaf_rec, cudaStream_t stream)
+{
+    if (n == 0) return CPT_OK;
+    if (n > 1) k_bvh2_nodes<<<blocks_for(n - 1, 256), 256, 0, stream>>>(child, node_box, leaf_box, n - 1, nodes);
+    if (tri_f64)
+        k_leaf_records<double><<<blocks_for(n, 256), 256, 0, stream>>>(order, n, n_lights, n_spheres, tri_f64, spheres,
+                                                                       leaf_rec);
+    else
+        k_leaf_records<float><<<blocks_for(n, 256), 256, 0, stream>>>(order, n, n_lights, n_spheres, tri_f32, spheres,
+                                                                      leaf_rec);
+    CPT_CUDA(cudaGetLastError());
+    add_launches((n > 1 ? 1 : 0) + 1);
+    return CPT_OK;
+}
+
+}  // namespace cpt
+
+// ---------------------------------------------------------------- C ABI (low level)
+CPT_EXPORT size_t cpt_lbvh_scratch_bytes(uint32_t num_prims) { return cpt::lbvh_scratch_bytes(num_prims); }
+
+CPT_EXPORT cpt_status cpt_lbvh_build_device(uint32_t num_extra, const double* extra_centroids, const float* extra_boxes,
+                                            uint32_t num_tri, const float* tri_vertices, const double scene_min[3],
+                                            const double scene_max[3], uint64_t* out_keys, uint32_t* out_order,
+                                            int32_t* out_children, int32_t* out_node_range, float* out_node_boxes,
+                                            float* out_leaf_boxes, void* scratch, size_t scratch_bytes, void* stream)
+{
+    if (!scene_min || !scene_max) return cpt::fail(CPT_ERR_INVALID_ARGUMENT, "cpt_lbvh_build_device: bounds");
+    cpt::LbvhBuffers b;
+    b.keys = out_keys;
+    b.order = out_order;
+    b.child = (int2*)out_children;
+    b.range = (int2*)out_node_range;
+    b.node_box = (float4*)out_node_boxes;
+    b.leaf_box = (float4*)out_leaf_boxes;
+    return cpt::lbvh_build(num_extra, extra_centroids, (const float4*)extra_boxes, num_tri, tri_vertices, nullptr,
+                           scene_min, scene_max, b, scratch, scratch_bytes, (cudaStream_t)stream, nullptr);
+}

@@ -1,0 +1,115 @@
+"""Generates the golden fixtures in tests/golden/ from the reference's OWN code.
+
+The reference's path (BVH.cuh, Hittable.cuh, Material.cuh, Camera.*, Render.cu,
+IniParser.cpp) is compiled as host C++ by oracle/Makefile into oracle/_ref/libcpt_ref.so
+(only possible where the reference is mounted).  This script runs it on small seeded
+inputs and stores its outputs; the tests then check the restated oracle and the CUDA
+library against these vectors on any machine.
+
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+import oracle as O  # noqa: E402
+
+from cudapathtracing_gb300 import abi, procedural as P  # noqa: E402
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SCENES = os.path.join(HERE, "scenes")
+
+
+def degenerate_scene(n: int = 64) -> abi.SceneDesc:
+    """n triangles sharing one centroid cell: keys differ only in the index word."""
+    d = abi.SceneDesc()
+    d.add_material((0.5, 0.5, 0.5))
+    g = P.PCG32Streams(7, np.arange(n, dtype=np.uint64))
+    tri = np.zeros((n, 9))
+    for k in range(9):
+        tri[:, k] = 0.25 + 1e-4 * g.uniform()
+    d.tri_vertices = tri.astype(np.float32)
+    d.tri_material = np.zeros(n, np.uint32)
+    d.camera = abi.Camera(16, 1.0, (0, 0, 3), (0, 0, 0), 40.0, (0, 0, 0))
+    return d
+
+
+def mixed_scene(seed: int = 11) -> abi.SceneDesc:
+    """Random triangles, spheres and lights (all three primitive kinds in one tree)."""
+    d = abi.SceneDesc()
+    for m in range(3):
+        d.add_material((0.3 + 0.2 * m, 0.6, 0.8 - 0.2 * m), 0.2 + 0.2 * m, 0.3, abi.M_OPAQUE)
+    g = P.PCG32Streams(seed, np.arange(300, dtype=np.uint64))
+    c = np.stack([g.uniform() * 6 - 3 for _ in range(3)], 1)
+    e = np.stack([g.uniform() * 0.6 - 0.3 for _ in range(6)], 1)
+    tri = np.concatenate([c, c + e[:, :3], c + e[:, 3:]], 1)
+    d.tri_vertices = tri.astype(np.float32)
+    d.tri_material = (np.arange(300) % 3).astype(np.uint32)
+    for k in range(4):
+        d.spheres.append(dict(center=(k - 1.5, 0.5 * k, -1.0), radius=0.3 + 0.1 * k, material=k % 3))
+    d.lights.append(dict(center=(0.0, 4.0, 0.0), normal=(0.0, -1.0, 0.2), width=1.5, height=0.7,
+                         color=(8.0, 8.0, 8.0), visible=1))
+    d.lights.append(dict(center=(2.0, 1.0, 3.0), normal=(-1.0, 0.0, -1.0), width=0.5, height=0.5,
+                         color=(4.0, 2.0, 1.0), visible=1))
+    pts = tri.reshape(-1, 3)
+    d.bounds_min = tuple(pts.min(0))
+    d.bounds_max = tuple(pts.max(0))
+    d.camera = abi.Camera(32, 1.0, (0.0, 1.0, 9.0), (0.0, 0.0, 0.0), 50.0, (0.2, 0.2, 0.25))
+    return d
+
+
+def lbvh_fixture(name: str, ref: O.RefScene) -> None:
+    L = ref.lbvh()
+    np.savez_compressed(os.path.join(HERE, f"lbvh_{name}.npz"), **{k: L[k] for k in
+                                                                   ("keys", "order", "child_a", "child_b",
+                                                                    "node_boxes", "leaf_boxes")})
+
+
+def main() -> None:
+    if O.ref_lib() is None:
+        O.build(ref=True)
+    if O.ref_lib() is None:
+        raise SystemExit("oracle/_ref is not built: the reference is not mounted here")
+
+    # LBVH keys, order, topology and FP64 boxes
+    cornell = P.cornell_box(width=48)
+    lbvh_fixture("cornell", O.RefScene(cornell))
+    lbvh_fixture("degenerate", O.RefScene(degenerate_scene()))
+    mixed = mixed_scene()
+    lbvh_fixture("mixed", O.RefScene(mixed))
+    ico = P.icosphere_scene(level=3)
+    ref_ico = O.RefScene(ico)
+    lbvh_fixture("ico3", ref_ico)
+    for ini in ("volume_glass", "glossy"):
+        lbvh_fixture(ini, O.RefScene(ini_path=os.path.join(SCENES, ini + ".ini")))
+
+    # closest hits (traverseIterative)
+    rays = P.uniform_rays(4096, seed=1)
+    ids, t = ref_ico.trace(P.rays_as_f64(rays))
+    np.savez_compressed(os.path.join(HERE, "hits_ico3.npz"), ids=ids, t=t)
+    rays_m = P.uniform_rays(4096, seed=3, box=3.0)
+    ids, t = O.RefScene(mixed).trace(P.rays_as_f64(rays_m))
+    np.savez_compressed(os.path.join(HERE, "hits_mixed.npz"), ids=ids, t=t)
+
+    # renders (STATIC mode, PCG32 seed 0)
+    for name, ref, spp in (("cornell", O.RefScene(cornell), 4), ("mixed", O.RefScene(mixed), 4),
+                           ("volume_glass", O.RefScene(ini_path=os.path.join(SCENES, "volume_glass.ini")), 4),
+                           ("glossy", O.RefScene(ini_path=os.path.join(SCENES, "glossy.ini")), 4)):
+        r = ref.render(spp, seed=0)
+        np.savez_compressed(os.path.join(HERE, f"render_{name}.npz"), rgb=r["rgb"], rgba8=r["rgba8"], spp=spp)
+
+    # the reference's INI parser, flattened
+    for ini in ("volume_glass", "glossy", "parser_edge"):
+        np.save(os.path.join(HERE, f"ini_{ini}.npy"), O.ref_ini_dump(os.path.join(SCENES, ini + ".ini")))
+    print("golden fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main()
