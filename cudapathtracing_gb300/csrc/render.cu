@@ -75,7 +75,11 @@ __device__ PixelResult pixel_reference(const SceneView& s, int i, int j, const R
                 float t = -logf(rng.one_minus_uniform_from(rng.next())) / sig;
                 float3 pos = sf.pos + t * d;
                 o = pos;
-                while (t < dmax) {
+                for (int vguard = 0; t < dmax; ++vguard) {
+                    if (vguard >= ITER_LIMIT) {
+                        atomicOr(a.err, CPT_DEVERR_ITER);
+                        break;
+                    }
                     if (rng.uniform() > 0.8f) break;
                     thr = thr * (expf(-t * sig) / 0.8f);
                     float z = 1.0f - 2.0f * rng.uniform();
