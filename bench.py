@@ -189,6 +189,8 @@ def main():
     ap.add_argument("--workload", default="spheres_1080p", choices=sorted(WORKLOADS))
     ap.add_argument("--integrator", default="megakernel", choices=["megakernel", "wavefront"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--spp", type=int, default=0, help="override the workload's spp (profiling captures)")
+    ap.add_argument("--e2e-steps", type=int, default=2, help="steps of the end-to-end leg (0: skip)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference_arm(args)
@@ -203,7 +205,9 @@ def main():
     from cudapathtracing_gb300 import build as cbuild
     if not os.path.exists(_lib.LIB_PATH):
         cbuild.build()
-    wl = WORKLOADS[args.workload]
+    wl = dict(WORKLOADS[args.workload])
+    if args.spp > 0:
+        wl["spp"] = args.spp
     integ = abi.INTEGRATOR_WAVEFRONT if args.integrator == "wavefront" else abi.INTEGRATOR_MEGAKERNEL
     desc = make_scene(args.workload)
     W, H = desc.camera.width, desc.camera.height
@@ -260,7 +264,7 @@ def main():
     desc_e2e.tri_vertices = tri_pinned.numpy()
     host_rgb = torch.zeros((H, W, 3), dtype=torch.float32).pin_memory().numpy()
     host_rgba = torch.zeros((H, W, 4), dtype=torch.uint8).pin_memory().numpy()
-    e2e_steps = max(1, min(args.steps, 2))
+    e2e_steps = args.e2e_steps
     e2e_rays = 0
     barrier()
     t0 = time.perf_counter()
@@ -271,8 +275,8 @@ def main():
         e2e_rays += r2["rays"]
         s2.close()
     barrier()
-    e2e_t = time.perf_counter() - t0
-    h2d = desc.tri_vertices.nbytes + desc.tri_material.nbytes + 9 * 0
+    e2e_t = max(time.perf_counter() - t0, 1e-9)
+    h2d = desc.tri_vertices.nbytes + desc.tri_material.nbytes
     d2h = host_rgb.nbytes + host_rgba.nbytes
 
     if rank != 0:

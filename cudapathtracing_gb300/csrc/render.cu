@@ -228,8 +228,8 @@ __device__ PixelResult pixel_config(const SceneView& s, int i, int j, const Rend
                 for (int k = 0; k < s.n_lights; ++k) {
                     const DevLight& L = s.lights[k];
                     float area = L.w * L.h;
-                    float ub = rng.uniform();
                     float ua = rng.uniform();
+                    float ub = rng.uniform();
                     float3 lp = L.center + ((ua - 0.5f) * L.w) * L.eu + ((ub - 0.5f) * L.h) * L.ev;
                     float3 dir = unit3(lp - sf.pos);
                     Hit lh2;
