@@ -272,6 +272,22 @@ cpt_status cpt_lbvh_build_device(uint32_t num_extra, const double* extra_centroi
                                  int32_t* out_children, int32_t* out_node_range, float* out_node_boxes,
                                  float* out_leaf_boxes, void* scratch, size_t scratch_bytes, void* stream);
 
+/* No counterpart in the reference.  The same build as cpt_lbvh_build_device for callers that
+ * cannot allocate device memory — e.g. a host that has divided all of its HBM among its own
+ * pools at start-up, or code in a frame loop or callback where a cudaMalloc (and the device
+ * synchronisation it implies) is not allowed.  The caller passes inputs and outputs only; the
+ * scratch is a 3 MiB array compiled into this library, which every GPU that loads it keeps
+ * until the process exits.  At most CPT_LBVH_STATIC_MAX_PRIMS primitives; more is rejected with
+ * CPT_ERR_INVALID_ARGUMENT.  The call allocates nothing.  Its first call on a device looks up the
+ * array's device address (do that first call before any stream capture).  All calls share the
+ * one array: calls whose work overlaps on the GPU (other streams, other host threads) race. */
+#define CPT_LBVH_STATIC_MAX_PRIMS 65536u
+cpt_status cpt_lbvh_build_device_static(uint32_t num_extra, const double* extra_centroids, const float* extra_boxes,
+                                        uint32_t num_tri, const float* tri_vertices, const double scene_min[3],
+                                        const double scene_max[3], uint64_t* out_keys, uint32_t* out_order,
+                                        int32_t* out_children, int32_t* out_node_range, float* out_node_boxes,
+                                        float* out_leaf_boxes, void* stream);
+
 /* ---- trace ---------------------------------------------------------------------- */
 /* Closest hit for n rays (traverseIterative, BVH.cuh:282-332, and Hittable::hit,
  * Hittable.cuh:487-503).  rays/hits are device pointers when on_device != 0, else host
