@@ -39,6 +39,7 @@ def lib():
             "cpt_context_create": (S, [C.c_int, C.POINTER(P)]),
             "cpt_context_destroy": (S, [P]),
             "cpt_context_set_render_block": (S, [P, C.c_int, C.c_int]),
+            "cpt_context_set_wavefront": (S, [P, C.c_int, C.c_int, C.c_int, C.c_int]),
             "cpt_ini_load": (S, [C.c_char_p, C.POINTER(P)]),
             "cpt_ini_describe": (S, [P, C.POINTER(abi.cpt_scene_desc)]),
             "cpt_ini_free": (S, [P]),

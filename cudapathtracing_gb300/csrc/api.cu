@@ -46,7 +46,13 @@ struct cpt_context {
     int device;
     int sm_count;
     int render_block_x, render_block_y;
+    WavefrontTuning wf;        // grids are filled on first use
+    bool wf_grids_ready;
 };
+
+namespace cpt {
+cpt_status wavefront_grids(int sm_count, int block_trace, int block_shade, int* grid_trace, int* grid_shade);
+}
 
 struct cpt_scene {
     cpt_context* ctx;
@@ -391,13 +397,36 @@ CPT_EXPORT cpt_status cpt_context_create(int device, cpt_context** out)
     CPT_CUDA(cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device));
     c->render_block_x = 16;
     c->render_block_y = 8;
+    std::memset(&c->wf, 0, sizeof c->wf);
+    c->wf.slots = 1 << 20;
+    c->wf.block_trace = 128;
+    c->wf.block_shade = 128;
+    c->wf.use_graph = true;
+    c->wf_grids_ready = false;
+    CPT_CUDA(cudaStreamCreateWithFlags(&c->wf.capture_stream, cudaStreamNonBlocking));
     *out = c;
     return CPT_OK;
 }
 
 CPT_EXPORT cpt_status cpt_context_destroy(cpt_context* ctx)
 {
+    if (ctx && ctx->wf.capture_stream) cudaStreamDestroy(ctx->wf.capture_stream);
     delete ctx;
+    return CPT_OK;
+}
+
+// Internal tuning knob (the autotuner's setter): wavefront size, block sizes, graph replay.
+CPT_EXPORT cpt_status cpt_context_set_wavefront(cpt_context* ctx, int slots, int block_trace, int block_shade,
+                                                int use_graph)
+{
+    auto ok_block = [](int b) { return b >= 32 && b <= 1024 && b % 32 == 0; };
+    if (!ctx || slots < 1024 || !ok_block(block_trace) || !ok_block(block_shade))
+        return fail(CPT_ERR_INVALID_ARGUMENT, "wavefront: slots >= 1024, blocks multiples of 32 in [32, 1024]");
+    ctx->wf.slots = slots;
+    ctx->wf.block_trace = block_trace;
+    ctx->wf.block_shade = block_shade;
+    ctx->wf.use_graph = use_graph != 0;
+    ctx->wf_grids_ready = false;
     return CPT_OK;
 }
 
@@ -622,6 +651,8 @@ CPT_EXPORT cpt_status cpt_render(cpt_scene* s, const cpt_render_params* p, const
         return fail(CPT_ERR_INVALID_ARGUMENT, "cpt_render: unknown estimator");
     if (p->integrator != CPT_INTEGRATOR_MEGAKERNEL && p->integrator != CPT_INTEGRATOR_WAVEFRONT)
         return fail(CPT_ERR_INVALID_ARGUMENT, "cpt_render: unknown integrator");
+    if (p->integrator == CPT_INTEGRATOR_WAVEFRONT && p->estimator != CPT_ESTIMATOR_CONFIG)
+        return fail(CPT_ERR_UNSUPPORTED, "cpt_render: the wavefront integrator runs the config estimator");
     if (p->estimator == CPT_ESTIMATOR_CONFIG && !(p->rr_prob > 0.f && p->rr_prob <= 1.f))
         return fail(CPT_ERR_INVALID_ARGUMENT, "cpt_render: rr_prob must be in (0, 1]");
     int W = s->cam.width, H = s->cam.height;
@@ -664,7 +695,18 @@ CPT_EXPORT cpt_status cpt_render(cpt_scene* s, const cpt_render_params* p, const
     }
     CPT_CUDA(cudaMemsetAsync(s->ray_counter, 0, sizeof(unsigned long long), stream));
     if (stats) CPT_CUDA(cudaEventRecord(e0, stream));
-    cpt_status st = launch_render_megakernel(view_of(s), a, stream, s->ctx->render_block_x, s->ctx->render_block_y);
+    cpt_status st = CPT_OK;
+    if (p->integrator == CPT_INTEGRATOR_WAVEFRONT) {
+        cpt_context* c = s->ctx;
+        if (!c->wf_grids_ready) {
+            st = wavefront_grids(c->sm_count, c->wf.block_trace, c->wf.block_shade, &c->wf.grid_trace,
+                                 &c->wf.grid_shade);
+            c->wf_grids_ready = st == CPT_OK;
+        }
+        if (st == CPT_OK) st = launch_render_wavefront(view_of(s), a, stream, c->wf);
+    } else {
+        st = launch_render_megakernel(view_of(s), a, stream, s->ctx->render_block_x, s->ctx->render_block_y);
+    }
     if (stats) CPT_CUDA(cudaEventRecord(e1, stream));
     if (st == CPT_OK && host) {
         size_t off = (size_t)r0 * W, cnt = (size_t)(r1 - r0) * W;

@@ -87,4 +87,16 @@ struct RenderArgs {
 cpt_status launch_render_megakernel(const SceneView& view, const RenderArgs& args, cudaStream_t stream, int block_x,
                                     int block_y);
 
+// Wavefront integrator launch shape (the autotuner's knobs) and graph-capture resources.
+struct WavefrontTuning {
+    int slots;                   // path slots (the wavefront size)
+    int grid_trace, block_trace; // persistent grids
+    int grid_shade, block_shade;
+    bool use_graph;
+    cudaStream_t capture_stream; // non-default stream used only to capture the iteration graph
+};
+
+cpt_status launch_render_wavefront(const SceneView& view, const RenderArgs& args, cudaStream_t stream,
+                                   const WavefrontTuning& tune);
+
 }  // namespace cpt

@@ -232,12 +232,13 @@ __device__ PixelResult pixel_config(const SceneView& s, int i, int j, const Rend
                     float ub = rng.uniform();
                     float3 lp = L.center + ((ua - 0.5f) * L.w) * L.eu + ((ub - 0.5f) * L.h) * L.ev;
                     float3 dir = unit3(lp - sf.pos);
+                    float cs_ = dot3(dir, sf.normal), cl_ = dot3(-dir, L.normal);
+                    if (!(cs_ > 0.f && cl_ > 0.f)) continue;   // cannot contribute: no shadow ray
                     Hit lh2;
                     trace_closest(s, sf.pos, dir, 0.001f, CPT_INF_F, lh2, a.err);
                     out.rays++;
                     int obst = prim_of(s, lh2);
-                    float cs_ = dot3(dir, sf.normal), cl_ = dot3(-dir, L.normal);
-                    if (cs_ > 0.f && cl_ > 0.f && obst == k) {
+                    if (obst == k) {
                         float3 fr = bsdf_eval(sf, d, dir);
                         float g = cs_ * cl_ / len2(lp - sf.pos) * area;
                         rad = rad + thr * (L.color * fr * g);

@@ -1,0 +1,569 @@
+// wavefront.cu — the wavefront integrator (config estimator).
+//
+// Paths live in M slots (structure of arrays).  Each slot owns one pixel at a time and runs that
+// pixel's samples in sequence with the pixel's own PCG32 stream, drawing the same numbers in the
+// same order as the megakernel (render.cu, pixel_config), so both integrators compute the same
+// estimator.  One iteration is four persistent kernels over compacted queues:
+//
+//   k_wf_trace    closest hit of every queued extension ray            (queue Q_i)
+//   k_wf_shadow   closest hit of every queued next-event shadow ray     (queue S_i)
+//   k_wf_resolve  slots whose last sample ended with shadow rays in flight: add the visible
+//                 light contributions, write the pixel, take the next pixel  (queue R_i)
+//   k_wf_shade    one path vertex per slot: add last iteration's visible light contributions,
+//                 then medium / miss / emission / NEE (appends to S_{i+1}) / Russian roulette /
+//                 BSDF sampling (appends to Q_{i+1}); a finished sample starts the next one
+//
+// Queues are appended with warp-aggregated atomics; counters for iteration i+1 are cleared by
+// k_wf_trace of iteration i.  The host replays a CUDA graph of CPT_WF_CHUNK iterations and reads
+// the queue sizes after each replay to stop.
+#include <cooperative_groups.h>
+#include <cooperative_groups/reduce.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+
+#include "cpt_internal.h"
+#include "cpt_shade.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace cpt {
+
+namespace {
+
+constexpr int ITER_LIMIT = 1 << 16;   // loop trips per sample, as in the megakernel
+constexpr int CHUNK = 8;              // iterations per graph replay (even: parities repeat)
+
+enum : uint32_t {
+    F_CE = 1u << 0,        // count emission at the next surface
+    F_INM = 1u << 1,       // inside a medium
+    F_NEE_PREV = 1u << 2,  // pending shadow results belong to the finished sample (radp)
+    F_GBUF = 1u << 3,      // G-buffer written for this pixel
+};
+
+struct Wf {
+    int M, L, spp, first_pix, end_pix, W;
+    int* pixel;
+    int* spp_done;
+    uint32_t* flags;
+    int* depth;
+    int* guard;
+    int* nee;               // bit k: a shadow ray towards light k is in flight
+    uint64_t* rng;
+    float4* o;
+    float4* d;
+    float4* thr;
+    float4* rad;
+    float4* radp;
+    float4* pix;
+    float2* med;
+    float4* hit;
+    int* q;                 // 2 * M
+    int* rq;                // 2 * M
+    int* sq;                // 2 * M * L
+    float4* so;             // M * L
+    float4* sd;
+    float4* sc;
+    int* svis;
+    int* cnt;               // [0,1] Q sizes, [2,3] R sizes, [4,5] S sizes, [6] next pixel
+    unsigned long long* rays;
+    int* err;
+};
+
+__device__ __forceinline__ void append(int* base, int* counter, int v)
+{
+    cg::coalesced_group g = cg::coalesced_threads();
+    int b = 0;
+    if (g.thread_rank() == 0) b = atomicAdd(counter, (int)g.size());
+    b = g.shfl(b, 0);
+    base[b + g.thread_rank()] = v;
+}
+
+__device__ __forceinline__ void count_rays(unsigned long long* counter, uint32_t n)
+{
+    cg::coalesced_group g = cg::coalesced_threads();
+    uint32_t tot = cg::reduce(g, n, cg::plus<uint32_t>());
+    if (g.thread_rank() == 0 && tot) atomicAdd(counter, (unsigned long long)tot);
+}
+
+__device__ __forceinline__ float3 xyz(float4 v) { return f3(v.x, v.y, v.z); }
+__device__ __forceinline__ float4 w0(float3 v) { return make_float4(v.x, v.y, v.z, 0.f); }
+
+__device__ __forceinline__ float3 camera_dir(const DevCamera& c, int i, int j, float rx, float ry)   // Camera.cuh:37-43
+{
+    float3 p = c.pixel_center + (rx - 0.5f + (float)i) * c.delta_h + (ry - 0.5f + (float)j) * c.delta_v;
+    return p - c.look_from;
+}
+
+__device__ __forceinline__ uint8_t to_u8(float x)
+{
+    float c = sqrtf(x);
+    c = c > 1.0f ? 1.0f : (c < 0.0f ? 0.0f : c);
+    return (uint8_t)(254.99f * c);
+}
+
+// New sample for slot s of pixel `pixel`: camera ray (two draws), fresh path state.
+__device__ __forceinline__ void start_sample(const SceneView& s, const Wf& w, int slot, int pixel, Pcg32& rng,
+                                             uint32_t& fl)
+{
+    int W = s.cam.width;
+    int i = pixel % W, j = pixel / W;
+    float rx = rng.uniform();
+    float ry = rng.uniform();
+    w.o[slot] = w0(s.cam.look_from);
+    w.d[slot] = w0(camera_dir(s.cam, i, j, rx, ry));
+    w.thr[slot] = make_float4(1.f, 1.f, 1.f, 0.f);
+    w.rad[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
+    w.depth[slot] = 0;
+    w.guard[slot] = 0;
+    fl = (fl & ~F_INM) | F_CE;
+}
+
+__device__ __forceinline__ void write_pixel(const SceneView& s, const Wf& w, const RenderArgs& a, int slot, int pixel,
+                                            uint32_t fl)
+{
+    float3 p = xyz(w.pix[slot]) / (float)a.spp;
+    size_t off = (size_t)pixel;
+    if (a.flags & CPT_RENDER_ACCUMULATE) {
+        a.rgb[3 * off] += p.x;
+        a.rgb[3 * off + 1] += p.y;
+        a.rgb[3 * off + 2] += p.z;
+    } else {
+        a.rgb[3 * off] = p.x;
+        a.rgb[3 * off + 1] = p.y;
+        a.rgb[3 * off + 2] = p.z;
+    }
+    if (a.rgba8) reinterpret_cast<uchar4*>(a.rgba8)[off] = make_uchar4(to_u8(p.x), to_u8(p.y), to_u8(p.z), 255);
+    if (a.gbuf && !(fl & F_GBUF)) {
+        float4* g = reinterpret_cast<float4*>(a.gbuf) + 2 * off;
+        g[0] = make_float4(0.f, 0.f, 0.f, CPT_INF_F);
+        g[1] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+}
+
+// Takes the next unrendered pixel for the slot (or leaves it idle) and queues its first ray.
+__device__ __forceinline__ void next_pixel(const SceneView& s, const Wf& w, const RenderArgs& a, int slot, int nq)
+{
+    int p = atomicAdd(&w.cnt[6], 1);
+    if (p >= w.end_pix) {
+        w.pixel[slot] = -1;
+        return;
+    }
+    Pcg32 rng;
+    rng.init(a.seed, (uint64_t)p);
+    uint32_t fl = 0;
+    w.pixel[slot] = p;
+    w.spp_done[slot] = 0;
+    w.pix[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
+    w.nee[slot] = 0;
+    start_sample(s, w, slot, p, rng, fl);
+    w.flags[slot] = fl;
+    w.rng[slot] = rng.state;
+    append(w.q + (size_t)nq * w.M, &w.cnt[nq], slot);
+}
+
+__global__ void k_wf_init(SceneView s, Wf w, RenderArgs a)
+{
+    int slot = blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= w.M) return;
+    int p = w.first_pix + slot;
+    if (slot == 0) {
+        w.cnt[0] = w.M;
+        w.cnt[1] = w.cnt[2] = w.cnt[3] = w.cnt[4] = w.cnt[5] = 0;
+        w.cnt[6] = w.first_pix + w.M;
+    }
+    Pcg32 rng;
+    rng.init(a.seed, (uint64_t)p);
+    uint32_t fl = 0;
+    w.pixel[slot] = p;
+    w.spp_done[slot] = 0;
+    w.pix[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
+    w.nee[slot] = 0;
+    start_sample(s, w, slot, p, rng, fl);
+    w.flags[slot] = fl;
+    w.rng[slot] = rng.state;
+    w.q[slot] = slot;   // Q_0 holds every slot in order; its size is set by the host
+}
+
+__global__ void __launch_bounds__(256) k_wf_trace(SceneView s, Wf w, int par)
+{
+    const int n = w.cnt[par];
+    const int nq = par ^ 1;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        w.cnt[nq] = 0;
+        w.cnt[2 + nq] = 0;
+        w.cnt[4 + nq] = 0;
+    }
+    const int* q = w.q + (size_t)par * w.M;
+    uint32_t rays = 0;
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
+        int slot = q[idx];
+        float4 o = w.o[slot], d = w.d[slot];
+        Hit h;
+        bool hit = trace_closest(s, xyz(o), xyz(d), 0.001f, CPT_INF_F, h, w.err);
+        w.hit[slot] = make_float4(h.t, __int_as_float(hit ? h.leaf : -1), h.u, h.v);
+        rays++;
+    }
+    count_rays(w.rays, rays);
+}
+
+__global__ void __launch_bounds__(256) k_wf_shadow(SceneView s, Wf w, int par)
+{
+    const int n = w.cnt[4 + par];
+    const int* sq = w.sq + (size_t)par * w.M * w.L;
+    uint32_t rays = 0;
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
+        int e = sq[idx];
+        int k = e % w.L;
+        Hit h;
+        bool hit = trace_closest(s, xyz(w.so[e]), xyz(w.sd[e]), 0.001f, CPT_INF_F, h, w.err);
+        int obst = hit ? __float_as_int(ldg4(s.leaf_rec + 3 * (size_t)h.leaf).w) : -1;
+        w.svis[e] = obst == k ? 1 : 0;
+        rays++;
+    }
+    count_rays(w.rays, rays);
+}
+
+// Adds the visible contributions of the shadow rays in flight, in light order.
+__device__ __forceinline__ float3 add_visible(const Wf& w, int slot, int mask, float3 acc)
+{
+    for (int k = 0; k < w.L; ++k) {
+        if (!((mask >> k) & 1)) continue;
+        int e = slot * w.L + k;
+        if (w.svis[e]) acc = acc + xyz(w.sc[e]);
+    }
+    return acc;
+}
+
+__global__ void __launch_bounds__(128) k_wf_resolve(SceneView s, Wf w, RenderArgs a, int par)
+{
+    const int n = w.cnt[2 + par];
+    const int nq = par ^ 1;
+    const int* rq = w.rq + (size_t)par * w.M;
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
+        int slot = rq[idx];
+        float3 acc = add_visible(w, slot, w.nee[slot], xyz(w.radp[slot]));
+        w.pix[slot] = w0(xyz(w.pix[slot]) + acc);
+        w.nee[slot] = 0;
+        write_pixel(s, w, a, slot, w.pixel[slot], w.flags[slot]);
+        next_pixel(s, w, a, slot, nq);
+    }
+}
+
+__global__ void __launch_bounds__(128) k_wf_shade(SceneView s, Wf w, RenderArgs a, int par)
+{
+    const int n = w.cnt[par];
+    const int nq = par ^ 1;
+    const int* q = w.q + (size_t)par * w.M;
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
+        const int slot = q[idx];
+        const int pixel = w.pixel[slot];
+        uint32_t fl = w.flags[slot];
+        Pcg32 rng;
+        rng.state = w.rng[slot];
+        rng.inc = ((uint64_t)pixel << 1u) | 1u;
+        float3 rad = xyz(w.rad[slot]);
+        // 1. shadow rays from the previous vertex
+        int pend = w.nee[slot];
+        if (pend) {
+            if (fl & F_NEE_PREV) {
+                float3 accp = add_visible(w, slot, pend, xyz(w.radp[slot]));
+                w.pix[slot] = w0(xyz(w.pix[slot]) + accp);
+            } else {
+                rad = add_visible(w, slot, pend, rad);
+            }
+            fl &= ~F_NEE_PREV;
+        }
+        // 2. the vertex (pixel_config's loop body)
+        float3 o = xyz(w.o[slot]), d = xyz(w.d[slot]);
+        float3 thr = xyz(w.thr[slot]);
+        int depth = w.depth[slot];
+        int guard = w.guard[slot] + 1;
+        float4 hv = w.hit[slot];
+        Hit h;
+        h.t = hv.x;
+        h.leaf = __float_as_int(hv.y);
+        h.u = hv.z;
+        h.v = hv.w;
+        const bool hit = h.leaf >= 0;
+        int nee = 0;
+        bool cont = false;   // path continues with (o, d)
+        if (guard >= ITER_LIMIT) {
+            atomicOr(w.err, CPT_DEVERR_ITER);
+        } else {
+            bool done_vertex = false;
+            if (fl & F_INM) {
+                float2 m = w.med[slot];
+                float t_hit = hit ? h.t : CPT_INF_F;
+                float t = -logf(rng.uniform()) / m.x;
+                if (t < t_hit) {
+                    float3 pos = o + t * d;
+                    thr = thr * m.y;
+                    depth++;
+                    done_vertex = true;
+                    bool alive = !(a.max_depth > 0 && depth >= a.max_depth);
+                    float P = 1.0f;
+                    if (alive && depth >= a.rr_depth) {
+                        P = a.rr_prob;
+                        if (rng.uniform() > P) alive = false;
+                    }
+                    if (alive) {
+                        thr = thr * (1.0f / P);
+                        float z = 1.0f - 2.0f * rng.uniform();
+                        float r = sqrtf(fmaxf(0.f, 1.0f - z * z));
+                        float phi = 2.0f * CPT_PI_F * rng.uniform();
+                        float sn, cs;
+                        sincosf(phi, &sn, &cs);
+                        o = pos;
+                        d = f3(r * cs, r * sn, z);
+                        fl |= F_CE;
+                        cont = true;
+                    }
+                }
+            }
+            if (!done_vertex) {
+                if (!hit) {
+                    rad = rad + thr * s.cam.background;
+                } else {
+                    Surf sf;
+                    make_surface(s, o, d, h, false, sf);
+                    if (sf.type == M_VOLUME) {
+                        fl = sf.front ? (fl | F_INM) : (fl & ~F_INM);
+                        w.med[slot] = make_float2(sf.sigma_t, sf.albedo);
+                        o = sf.pos;
+                        cont = true;
+                    } else if (sf.type == M_LIGHT) {
+                        if (fl & F_CE) rad = rad + thr * sf.color;
+                    } else {
+                        if (depth == 0 && !(fl & F_GBUF)) {
+                            fl |= F_GBUF;
+                            if (a.gbuf) {
+                                float4* g = reinterpret_cast<float4*>(a.gbuf) + 2 * (size_t)pixel;
+                                g[0] = make_float4(sf.normal.x, sf.normal.y, sf.normal.z,
+                                                   sqrtf(len2(s.cam.look_from - sf.pos)));
+                                g[1] = make_float4(sf.color.x, sf.color.y, sf.color.z, 0.f);
+                            }
+                        }
+                        bool diffuse_like = (sf.type == M_OPAQUE || sf.type == M_LAMBERT);
+                        if (diffuse_like) {
+                            for (int k = 0; k < s.n_lights; ++k) {
+                                const DevLight& L = s.lights[k];
+                                float area = L.w * L.h;
+                                float ua = rng.uniform();
+                                float ub = rng.uniform();
+                                float3 lp = L.center + ((ua - 0.5f) * L.w) * L.eu + ((ub - 0.5f) * L.h) * L.ev;
+                                float3 dir = unit3(lp - sf.pos);
+                                float cs_ = dot3(dir, sf.normal), cl_ = dot3(-dir, L.normal);
+                                if (!(cs_ > 0.f && cl_ > 0.f)) continue;
+                                float3 fr = bsdf_eval(sf, d, dir);
+                                float g = cs_ * cl_ / len2(lp - sf.pos) * area;
+                                int e = slot * w.L + k;
+                                w.so[e] = w0(sf.pos);
+                                w.sd[e] = w0(dir);
+                                w.sc[e] = w0(thr * (L.color * fr * g));
+                                nee |= 1 << k;
+                            }
+                        }
+                        if (diffuse_like && s.n_lights > 0) fl &= ~F_CE;
+                        else fl |= F_CE;
+                        depth++;
+                        bool alive = !(a.max_depth > 0 && depth >= a.max_depth);
+                        float P = 1.0f;
+                        if (alive && depth >= a.rr_depth) {
+                            P = a.rr_prob;
+                            if (rng.uniform() > P) alive = false;
+                        }
+                        if (alive) {
+                            float r1 = rng.uniform(), r2 = rng.uniform(), r3 = rng.uniform();
+                            float3 dir;
+                            float pdf;
+                            bsdf_sample(sf, d, dir, pdf, r1, r2, r3);
+                            if (pdf > 0.f) {
+                                float3 fr = bsdf_eval(sf, d, dir);
+                                thr = thr * (fr * fabsf(dot3(dir, sf.normal)) / pdf / P);
+                                o = sf.pos;
+                                d = dir;
+                                cont = true;
+                            }
+                        }
+                    }
+                }
+            }
+        }
+        w.nee[slot] = nee;
+        bool to_resolve = false, to_trace = false;
+        if (cont) {
+            w.o[slot] = w0(o);
+            w.d[slot] = w0(d);
+            w.thr[slot] = w0(thr);
+            w.rad[slot] = w0(rad);
+            w.depth[slot] = depth;
+            w.guard[slot] = guard;
+            to_trace = true;
+        } else {
+            // the sample ended
+            int done = w.spp_done[slot] + 1;
+            w.spp_done[slot] = done;
+            if (nee) {
+                w.radp[slot] = w0(rad);
+                fl |= F_NEE_PREV;
+            } else {
+                w.pix[slot] = w0(xyz(w.pix[slot]) + rad);
+            }
+            if (done < a.spp) {
+                start_sample(s, w, slot, pixel, rng, fl);
+                to_trace = true;
+            } else if (nee) {
+                to_resolve = true;
+            } else {
+                write_pixel(s, w, a, slot, pixel, fl);
+            }
+        }
+        w.flags[slot] = fl;
+        w.rng[slot] = rng.state;
+        if (nee)
+            for (int k = 0; k < w.L; ++k)
+                if ((nee >> k) & 1) append(w.sq + (size_t)nq * w.M * w.L, &w.cnt[4 + nq], slot * w.L + k);
+        if (to_trace) append(w.q + (size_t)nq * w.M, &w.cnt[nq], slot);
+        if (to_resolve) append(w.rq + (size_t)nq * w.M, &w.cnt[2 + nq], slot);
+        if (!cont && !to_trace && !to_resolve) next_pixel(s, w, a, slot, nq);
+    }
+}
+
+template <typename T>
+cpt_status carve(char*& p, size_t& left, T** out, size_t count)
+{
+    size_t bytes = align_up(count * sizeof(T), 256);
+    if (bytes > left) return fail(CPT_ERR_INVALID_ARGUMENT, "wavefront buffer too small");
+    *out = (T*)p;
+    p += bytes;
+    left -= bytes;
+    return CPT_OK;
+}
+
+size_t wf_bytes(int M, int L)
+{
+    size_t m = (size_t)M, ml = (size_t)M * std::max(L, 1);
+    auto a = [](size_t b) { return align_up(b, 256); };
+    return a(m * 4) * 6 + a(m * 8) + a(m * 16) * 8 + a(m * 8) + a(2 * m * 4) * 2 + a(2 * ml * 4) + a(ml * 16) * 3 +
+           a(ml * 4) + a(64);
+}
+
+}  // namespace
+
+cpt_status launch_render_wavefront(const SceneView& view, const RenderArgs& args, cudaStream_t stream,
+                                   const WavefrontTuning& tune)
+{
+    int W = view.cam.width;
+    int first = args.row_begin * W, end = args.row_end * W;
+    int npix = end - first;
+    if (npix <= 0) return CPT_OK;
+    int L = std::max(view.n_lights, 1);
+    if (view.n_lights > 30) return fail(CPT_ERR_UNSUPPORTED, "wavefront integrator: at most 30 lights");
+    int M = std::min(npix, std::max(tune.slots, 1024));
+    Wf w;
+    std::memset(&w, 0, sizeof w);
+    w.M = M;
+    w.L = L;
+    w.spp = args.spp;
+    w.first_pix = first;
+    w.end_pix = end;
+    w.W = W;
+    w.rays = args.ray_counter;
+    w.err = args.err;
+    size_t bytes = wf_bytes(M, L);
+    char* base = nullptr;
+    CPT_CUDA(cudaMallocAsync((void**)&base, bytes, stream));
+    char* p = base;
+    size_t left = bytes;
+    size_t ml = (size_t)M * L;
+    cpt_status st = CPT_OK;
+#define CARVE(f, n)                                   \
+    if (st == CPT_OK) st = carve(p, left, &w.f, (n));
+    CARVE(pixel, M) CARVE(spp_done, M) CARVE(flags, M) CARVE(depth, M) CARVE(guard, M) CARVE(nee, M)
+    CARVE(rng, M) CARVE(o, M) CARVE(d, M) CARVE(thr, M) CARVE(rad, M) CARVE(radp, M) CARVE(pix, M) CARVE(hit, M)
+    CARVE(so, ml) CARVE(med, M) CARVE(q, 2 * (size_t)M) CARVE(rq, 2 * (size_t)M) CARVE(sq, 2 * ml) CARVE(sd, ml)
+    CARVE(sc, ml) CARVE(svis, ml) CARVE(cnt, 16)
+#undef CARVE
+    if (st != CPT_OK) {
+        cudaFreeAsync(base, stream);
+        return st;
+    }
+    // Q_0 = all M slots
+    k_wf_init<<<(M + 255) / 256, 256, 0, stream>>>(view, w, args);
+    add_launches(1);
+    const int gt = tune.grid_trace, gs = tune.grid_shade;
+    const int bt = tune.block_trace, bs = tune.block_shade;
+    cudaGraphExec_t exec = nullptr;
+    cudaGraph_t graph = nullptr;
+    bool use_graph = tune.use_graph;
+    if (use_graph) {
+        // Capture CHUNK iterations (4 launches each) once; replay until the queues drain.
+        cudaStream_t cs = tune.capture_stream;
+        CPT_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+        for (int it = 0; it < CHUNK; ++it) {
+            int par = it & 1;
+            k_wf_trace<<<gt, bt, 0, cs>>>(view, w, par);
+            k_wf_shadow<<<gt, bt, 0, cs>>>(view, w, par);
+            k_wf_resolve<<<gs, bs, 0, cs>>>(view, w, args, par);
+            k_wf_shade<<<gs, bs, 0, cs>>>(view, w, args, par);
+        }
+        cudaError_t ce = cudaStreamEndCapture(cs, &graph);
+        if (ce != cudaSuccess) {
+            cudaFreeAsync(base, stream);
+            return cuda_fail(ce, "cudaStreamEndCapture");
+        }
+        ce = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ce != cudaSuccess) {
+            cudaFreeAsync(base, stream);
+            return cuda_fail(ce, "cudaGraphInstantiate");
+        }
+    }
+    int host_cnt[6];
+    const int max_chunks = 1 << 20;
+    bool drained = false;
+    for (int chunk = 0; chunk < max_chunks; ++chunk) {
+        if (use_graph) {
+            CPT_CUDA(cudaGraphLaunch(exec, stream));
+        } else {
+            for (int it = 0; it < CHUNK; ++it) {
+                int par = it & 1;
+                k_wf_trace<<<gt, bt, 0, stream>>>(view, w, par);
+                k_wf_shadow<<<gt, bt, 0, stream>>>(view, w, par);
+                k_wf_resolve<<<gs, bs, 0, stream>>>(view, w, args, par);
+                k_wf_shade<<<gs, bs, 0, stream>>>(view, w, args, par);
+            }
+        }
+        add_launches(4 * CHUNK);
+        CPT_CUDA(cudaMemcpyAsync(host_cnt, w.cnt, sizeof host_cnt, cudaMemcpyDeviceToHost, stream));
+        CPT_CUDA(cudaStreamSynchronize(stream));
+        if (host_cnt[0] == 0 && host_cnt[2] == 0 && host_cnt[4] == 0) {
+            drained = true;
+            break;
+        }
+    }
+    if (exec) cudaGraphExecDestroy(exec);
+    cudaFreeAsync(base, stream);
+    CPT_CUDA(cudaGetLastError());
+    if (!drained) return fail(CPT_ERR_TIMEOUT, "wavefront integrator did not drain");
+    return CPT_OK;
+}
+
+}  // namespace cpt
+
+namespace cpt {
+
+// Persistent grid sizes: resident blocks per SM (occupancy) x SMs, for the given block sizes.
+cpt_status wavefront_grids(int sm_count, int block_trace, int block_shade, int* grid_trace, int* grid_shade)
+{
+    int bt = 0, bs = 0;
+    CPT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bt, k_wf_trace, block_trace, 0));
+    CPT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bs, k_wf_shade, block_shade, 0));
+    *grid_trace = std::max(1, bt) * sm_count;
+    *grid_shade = std::max(1, bs) * sm_count;
+    return CPT_OK;
+}
+
+}  // namespace cpt

@@ -1010,12 +1010,13 @@ static PixelOut renderPixelConfig(const Scene& s, int i, int j, const cpt_render
                     double ub = st.uniform();
                     V3 lp = L.sc + (ua - 0.5) * L.lw * L.eu + (ub - 0.5) * L.lh * L.ev;
                     V3 dir = unit(lp - rec.hitPos);
+                    double cs = dot(dir, rec.normal), cl = dot(-dir, L.ln);
+                    if (!(cs > 0.0 && cl > 0.0)) continue;   // cannot contribute: no shadow ray
                     Ray sr = {rec.hitPos, dir};
                     HitRecord lrec;
                     int obst = traverse(s, sr, lrec);
                     rays++;
-                    double cs = dot(dir, rec.normal), cl = dot(-dir, L.ln);
-                    if (cs > 0.0 && cl > 0.0 && obst == k) {
+                    if (obst == k) {
                         V3 fr = bsdfEval(m, rec.hitColor, ray, rec.normal, dir, rec.hitWm, rec.frontFace);
                         double g = cs * cl / len2(lp - rec.hitPos) * area;
                         rad = rad + thr * (lrec.hitColor * fr * g);

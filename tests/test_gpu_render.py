@@ -62,20 +62,68 @@ def test_reference_estimator_cornell_512_vs_oracle(ctx, oracle_mod):
     assert abs(r["rays"] - o["rays"]) / o["rays"] < 0.01
 
 
-@pytest.mark.parametrize("name", ["cornell", "volume_glass", "glossy", "spheres"])
-def test_config_estimator_vs_oracle(ctx, oracle_mod, name):
+def config_scene(name):
     if name == "spheres":
-        d = P.spheres_scene(num_spheres=12, level=3, width=96)
-    elif name == "cornell":
-        d = P.cornell_box(width=96)
-    else:
-        d = scenes.ini_desc(name)
+        return P.spheres_scene(num_spheres=12, level=3, width=96)
+    if name == "cornell":
+        return P.cornell_box(width=96)
+    return scenes.ini_desc(name)
+
+
+def config_params(name, spp=8):
+    return dict(spp=spp, estimator=abi.ESTIMATOR_CONFIG, max_depth=8 if name == "cornell" else 16,
+                rr_depth=3, rr_prob=0.8, seed=5)
+
+
+@pytest.mark.parametrize("integrator", [abi.INTEGRATOR_MEGAKERNEL, abi.INTEGRATOR_WAVEFRONT])
+@pytest.mark.parametrize("name", ["cornell", "volume_glass", "glossy", "spheres"])
+def test_config_estimator_vs_oracle(ctx, oracle_mod, name, integrator):
+    d = config_scene(name)
     s = api.Scene(ctx, d).init()
-    prm = dict(spp=8, estimator=abi.ESTIMATOR_CONFIG, max_depth=8 if name == "cornell" else 16,
-               rr_depth=3, rr_prob=0.8, seed=5)
-    r = s.render(**prm)
+    prm = config_params(name)
+    r = s.render(integrator=integrator, **prm)
     o = oracle_mod.OracleScene(d).render(abi.render_params(**prm))
     compare(r["rgb"], o["rgb"])
+    assert abs(r["rays"] - o["rays"]) / o["rays"] < 0.01
+
+
+@pytest.mark.parametrize("slots,graph", [(1 << 20, 1), (1024, 1), (1536, 0)])
+@pytest.mark.parametrize("name", ["cornell", "volume_glass", "spheres"])
+def test_wavefront_matches_megakernel(ctx, name, slots, graph):
+    """Same estimator, same PCG32 streams and draw order: the two integrators trace the same
+    paths.  With fewer slots than pixels the slots take new pixels as they finish."""
+    d = config_scene(name)
+    s = api.Scene(ctx, d).init()
+    prm = config_params(name, spp=6)
+    mk = s.render(integrator=abi.INTEGRATOR_MEGAKERNEL, **prm)
+    ctx.set_wavefront(slots, 128, 128, graph)
+    try:
+        wf = s.render(integrator=abi.INTEGRATOR_WAVEFRONT, **prm)
+    finally:
+        ctx.set_wavefront(1 << 20, 128, 128, 1)
+    exact = (wf["rgb"] == mk["rgb"]).all(-1).mean()
+    print(f"wavefront == megakernel on {exact:.5f} of pixels; rays {wf['rays']} vs {mk['rays']}")
+    compare(wf["rgb"], mk["rgb"].astype(np.float64), match_frac=0.999, mean_tol=1e-3)
+    assert abs(wf["rays"] - mk["rays"]) <= 1e-3 * mk["rays"]
+
+
+def test_wavefront_gbuffer_and_rows(ctx):
+    import torch
+    d = P.cornell_box(width=40)
+    s = api.Scene(ctx, d).init()
+    prm = dict(spp=3, estimator=abi.ESTIMATOR_CONFIG, max_depth=6, rr_depth=2, rr_prob=0.75, seed=9)
+    gm = torch.zeros((40, 40, 8), device="cuda")
+    gw = torch.zeros((40, 40, 8), device="cuda")
+    rm = torch.zeros((40, 40, 3), device="cuda")
+    rw = torch.zeros((40, 40, 3), device="cuda")
+    s.render(integrator=abi.INTEGRATOR_MEGAKERNEL, rgb=rm, gbuffer=gm, **prm)
+    s.render(integrator=abi.INTEGRATOR_WAVEFRONT, rgb=rw, gbuffer=gw, rows=(0, 17), **prm)
+    s.render(integrator=abi.INTEGRATOR_WAVEFRONT, rgb=rw, gbuffer=gw, rows=(17, 40), **prm)
+    torch.cuda.synchronize()
+    assert torch.allclose(gm, gw, atol=1e-5)
+    assert torch.allclose(rm, rw, rtol=2e-3, atol=2e-3)
+    with pytest.raises(Exception):
+        s.render(integrator=abi.INTEGRATOR_WAVEFRONT, spp=1, estimator=abi.ESTIMATOR_REFERENCE)
 
 
 def test_accumulate_and_row_ranges(ctx):
