@@ -191,6 +191,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--spp", type=int, default=0, help="override the workload's spp (profiling captures)")
     ap.add_argument("--e2e-steps", type=int, default=2, help="steps of the end-to-end leg (0: skip)")
+    ap.add_argument("--bvh-width", type=int, default=8, choices=[2, 8], help="traversal layout")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference_arm(args)
@@ -212,6 +213,7 @@ def main():
     desc = make_scene(args.workload)
     W, H = desc.camera.width, desc.camera.height
     ctx = api.Context(local)
+    ctx.set_bvh_width(args.bvh_width)
     stream = torch.cuda.current_stream()
     scene = api.Scene(ctx, desc)
     scene.buildBVH(stream.cuda_stream)
@@ -313,7 +315,7 @@ def main():
         "warmup": args.warmup, "ms_per_step": round(elapsed / args.steps * 1e3, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": args.workload, "width": W, "height": H, "spp": wl["spp"],
-                   "triangles": desc.num_triangles, "integrator": args.integrator,
+                   "triangles": desc.num_triangles, "integrator": args.integrator, "bvh_width": args.bvh_width,
                    "estimator": "config" if wl["estimator"] == 1 else "reference",
                    "max_depth": wl["max_depth"], "rr_depth": wl["rr_depth"], "rr_prob": wl["rr_prob"],
                    "step": "LBVH build + full render", "l2": "inputs larger than L2 (BVH + leaf records)",

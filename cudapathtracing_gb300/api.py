@@ -42,6 +42,9 @@ class Context:
     def set_render_block(self, bx: int, by: int) -> None:
         check(lib().cpt_context_set_render_block(self.h, bx, by), "cpt_context_set_render_block")
 
+    def set_bvh_width(self, width: int) -> None:
+        check(lib().cpt_context_set_bvh_width(self.h, width), "cpt_context_set_bvh_width")
+
     def set_wavefront(self, slots: int, block_trace: int = 128, block_shade: int = 128, use_graph: int = 1) -> None:
         check(lib().cpt_context_set_wavefront(self.h, slots, block_trace, block_shade, use_graph),
               "cpt_context_set_wavefront")

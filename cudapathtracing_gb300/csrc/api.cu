@@ -48,10 +48,16 @@ struct cpt_context {
     int render_block_x, render_block_y;
     WavefrontTuning wf;        // grids are filled on first use
     bool wf_grids_ready;
+    int bvh_width;             // traversal layout built by cpt_lbvh_build: 8 (compressed wide) or 2
 };
 
 namespace cpt {
 cpt_status wavefront_grids(int sm_count, int block_trace, int block_shade, int* grid_trace, int* grid_shade);
+size_t wide_scratch_bytes(uint32_t n);
+cpt_status build_wide(uint32_t n, uint32_t n_lights, uint32_t n_spheres, const int2* child, const float4* node_box,
+                      const float4* leaf_box, const uint32_t* order, const float* tri_f32, const double* tri_f64,
+                      const float4* spheres, float4* wide, float4* leaf_rec, void* scratch, size_t scratch_bytes,
+                      cudaStream_t stream, uint32_t* num_wide);
 }
 
 struct cpt_scene {
@@ -83,7 +89,9 @@ struct cpt_scene {
     void* scratch;
     size_t scratch_bytes;
     // traversal layout
-    float4* nodes;
+    int width;          // layout of the last build: 2 or 8
+    float4* nodes;      // BVH2 nodes (width 2)
+    float4* wide;       // compressed 8-wide nodes (width 8)
     float4* leaf_rec;
     // misc
     unsigned long long* ray_counter;
@@ -113,7 +121,7 @@ void free_scene(cpt_scene* s)
     dfree(s->tri_f32); dfree(s->tri_f64); dfree(s->tri_n); dfree(s->tri_mat); dfree(s->spheres);
     dfree(s->sphere_mat); dfree(s->lights); dfree(s->mats); dfree(s->extra_c); dfree(s->extra_box);
     dfree(s->keys); dfree(s->order); dfree(s->child); dfree(s->range); dfree(s->node_box); dfree(s->leaf_box);
-    dfree(s->scratch); dfree(s->nodes); dfree(s->leaf_rec); dfree(s->ray_counter); dfree(s->err);
+    dfree(s->scratch); dfree(s->nodes); dfree(s->wide); dfree(s->leaf_rec); dfree(s->ray_counter); dfree(s->err);
 }
 
 // ---- reference double maths for the host-side derived quantities
@@ -316,7 +324,6 @@ cpt_status create_scene(cpt_context* ctx, const cpt_scene_desc* d, cpt_scene** o
     CPT_TRY(dalloc(&s->range, ni));
     CPT_TRY(dalloc(&s->node_box, 2 * (size_t)ni));
     CPT_TRY(dalloc(&s->leaf_box, 2 * (size_t)n));
-    CPT_TRY(dalloc(&s->nodes, 4 * (size_t)ni));
     CPT_TRY(dalloc(&s->leaf_rec, 3 * (size_t)n));
     s->scratch_bytes = lbvh_scratch_bytes(n);
     CPT_TRY(dalloc((char**)&s->scratch, s->scratch_bytes));
@@ -338,6 +345,7 @@ SceneView view_of(const cpt_scene* s)
     v.n_tris = (int)s->n_tris;
     v.n_internal = s->n > 1 ? (int)s->n - 1 : 0;
     v.nodes = s->nodes;
+    v.wide = s->width == 8 ? s->wide : nullptr;
     v.leaf_rec = s->leaf_rec;
     v.tri_mat = s->tri_mat;
     v.tri_n = s->tri_n;
@@ -347,6 +355,34 @@ SceneView view_of(const cpt_scene* s)
     v.mats = s->mats;
     v.cam = s->cam;
     return v;
+}
+
+// Traversal layout for the context's BVH width: the compressed 8-wide BVH (collapse in wide.cu,
+// using the LBVH scratch for its task queues) or the BVH2 node array; leaf records in the
+// matching order.  Buffers are allocated on first use.
+cpt_status make_layout(cpt_scene* s, cudaStream_t stream, uint32_t* num_wide)
+{
+    uint32_t n = s->n;
+    uint32_t ni = n > 1 ? n - 1 : 0;
+    int width = s->ctx->bvh_width;
+    if (width == 8 && n > 1) {
+        if (!s->wide) {
+            cpt_status st = dalloc(&s->wide, 5 * (size_t)ni);
+            if (st != CPT_OK) return st;
+        }
+        if (wide_scratch_bytes(n) > s->scratch_bytes) return fail(CPT_ERR_INVALID_ARGUMENT, "wide scratch too small");
+        s->width = 8;
+        return build_wide(n, s->n_lights, s->n_spheres, s->child, s->node_box, s->leaf_box, s->order, s->tri_f32,
+                          s->tri_f64, s->spheres, s->wide, s->leaf_rec, s->scratch, s->scratch_bytes, stream, num_wide);
+    }
+    if (!s->nodes && ni) {
+        cpt_status st = dalloc(&s->nodes, 4 * (size_t)ni);
+        if (st != CPT_OK) return st;
+    }
+    s->width = 2;
+    if (num_wide) *num_wide = 0;
+    return build_trace_layout(n, s->n_lights, s->n_spheres, s->child, s->node_box, s->leaf_box, s->order, s->tri_f32,
+                              s->tri_f64, s->spheres, s->nodes, s->leaf_rec, stream);
 }
 
 LbvhBuffers buffers_of(cpt_scene* s)
@@ -403,6 +439,7 @@ CPT_EXPORT cpt_status cpt_context_create(int device, cpt_context** out)
     c->wf.block_shade = 128;
     c->wf.use_graph = true;
     c->wf_grids_ready = false;
+    c->bvh_width = 8;
     CPT_CUDA(cudaStreamCreateWithFlags(&c->wf.capture_stream, cudaStreamNonBlocking));
     *out = c;
     return CPT_OK;
@@ -427,6 +464,13 @@ CPT_EXPORT cpt_status cpt_context_set_wavefront(cpt_context* ctx, int slots, int
     ctx->wf.block_shade = block_shade;
     ctx->wf.use_graph = use_graph != 0;
     ctx->wf_grids_ready = false;
+    return CPT_OK;
+}
+
+CPT_EXPORT cpt_status cpt_context_set_bvh_width(cpt_context* ctx, int width)
+{
+    if (!ctx || (width != 2 && width != 8)) return fail(CPT_ERR_INVALID_ARGUMENT, "BVH width must be 2 or 8");
+    ctx->bvh_width = width;
     return CPT_OK;
 }
 
@@ -523,8 +567,8 @@ CPT_EXPORT cpt_status cpt_lbvh_build(cpt_scene* s, void* stream_, cpt_bvh_stats*
                                buffers_of(s), s->scratch, s->scratch_bytes, stream, stats ? &tm : nullptr);
     if (st != CPT_OK) return st;
     if (stats) CPT_CUDA(cudaEventRecord(e0, stream));
-    st = build_trace_layout(s->n, s->n_lights, s->n_spheres, s->child, s->node_box, s->leaf_box, s->order, s->tri_f32,
-                            s->tri_f64, s->spheres, s->nodes, s->leaf_rec, stream);
+    uint32_t num_wide = 0;
+    st = make_layout(s, stream, &num_wide);
     if (st != CPT_OK) return st;
     s->built = true;
     if (stats) {
@@ -532,6 +576,7 @@ CPT_EXPORT cpt_status cpt_lbvh_build(cpt_scene* s, void* stream_, cpt_bvh_stats*
         CPT_CUDA(cudaEventSynchronize(e1));
         std::memset(stats, 0, sizeof *stats);
         stats->num_prims = s->n;
+        stats->num_wide_nodes = num_wide;
         stats->ms_prep = tm.ms_prep;
         stats->ms_sort = tm.ms_sort;
         stats->ms_emit = tm.ms_emit;
@@ -560,8 +605,7 @@ CPT_EXPORT cpt_status cpt_lbvh_refit(cpt_scene* s, void* stream_, cpt_bvh_stats*
     if (st != CPT_OK) return st;
     st = lbvh_refit(s->n, buffers_of(s), s->scratch, s->scratch_bytes, stream);
     if (st != CPT_OK) return st;
-    st = build_trace_layout(s->n, s->n_lights, s->n_spheres, s->child, s->node_box, s->leaf_box, s->order, s->tri_f32,
-                            s->tri_f64, s->spheres, s->nodes, s->leaf_rec, stream);
+    st = make_layout(s, stream, nullptr);
     if (st != CPT_OK) return st;
     if (stats) {
         CPT_CUDA(cudaEventRecord(e1, stream));

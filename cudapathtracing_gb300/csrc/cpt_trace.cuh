@@ -82,12 +82,118 @@ __device__ __forceinline__ bool hit_leaf(const SceneView& s, int k, float3 o, fl
     return hit_light(s.lights[__float_as_int(r1.x)], o, d, 0.001f, tmax, t);
 }
 
+__device__ __forceinline__ void cas(float& ka, uint32_t& va, float& kb, uint32_t& vb)
+{
+    if (kb < ka) {
+        float tk = ka; ka = kb; kb = tk;
+        uint32_t tv = va; va = vb; vb = tv;
+    }
+}
+
+// Closest hit through the compressed 8-wide BVH (layout in wide.cu).  Each visit decodes the 8
+// quantised child boxes, tests leaf children at once (as the reference tests leaves when it
+// reaches them), sorts the hit internal children by entry distance with a 19-comparator Batcher
+// network held in registers, continues with the nearest and pushes the others far-to-near with
+// their entry distance; popped entries farther than the closest hit are skipped.
+__device__ __forceinline__ bool trace_closest_wide(const SceneView& s, float3 o, float3 d, float tmin, float tmax,
+                                                   Hit& hit, int* err)
+{
+    const float3 idir = f3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
+    float best = tmax;
+    uint64_t stack[CPT_WSTACK];
+    int sp = 0;
+    uint32_t node = 0;
+    for (;;) {
+        const float4* np = s.wide + 5 * (size_t)node;
+        const float4 h0 = ldg4(np), h1 = ldg4(np + 1), q0 = ldg4(np + 2), q1 = ldg4(np + 3), q2 = ldg4(np + 4);
+        const uint32_t e = __float_as_uint(h0.w);
+        const float ax = __uint_as_float((e & 0xFFu) << 23) * idir.x;
+        const float ay = __uint_as_float(((e >> 8) & 0xFFu) << 23) * idir.y;
+        const float az = __uint_as_float(((e >> 16) & 0xFFu) << 23) * idir.z;
+        const float bx = (h0.x - o.x) * idir.x, by = (h0.y - o.y) * idir.y, bz = (h0.z - o.z) * idir.z;
+        const uint32_t cb = __float_as_uint(h1.x), lb = __float_as_uint(h1.y);
+        float key[8];
+        uint32_t val[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            const int w = i >> 2, sh = (i & 3) * 8;
+            const uint32_t m = ((w ? __float_as_uint(h1.w) : __float_as_uint(h1.z)) >> sh) & 0xFFu;
+            key[i] = INFINITY;
+            val[i] = 0;
+            if (m == 0xFFu) continue;
+            const float lx = (float)(((w ? __float_as_uint(q0.y) : __float_as_uint(q0.x)) >> sh) & 0xFFu);
+            const float hx = (float)(((w ? __float_as_uint(q0.w) : __float_as_uint(q0.z)) >> sh) & 0xFFu);
+            const float ly = (float)(((w ? __float_as_uint(q1.y) : __float_as_uint(q1.x)) >> sh) & 0xFFu);
+            const float hy = (float)(((w ? __float_as_uint(q1.w) : __float_as_uint(q1.z)) >> sh) & 0xFFu);
+            const float lz = (float)(((w ? __float_as_uint(q2.y) : __float_as_uint(q2.x)) >> sh) & 0xFFu);
+            const float hz = (float)(((w ? __float_as_uint(q2.w) : __float_as_uint(q2.z)) >> sh) & 0xFFu);
+            const float x0 = fmaf(lx, ax, bx), x1 = fmaf(hx, ax, bx);
+            const float y0 = fmaf(ly, ay, by), y1 = fmaf(hy, ay, by);
+            const float z0 = fmaf(lz, az, bz), z1 = fmaf(hz, az, bz);
+            const float tn = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fmaxf(fminf(z0, z1), tmin));
+            const float tf = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fminf(fmaxf(z0, z1), best));
+            if (tn <= tf) {
+                if (m & 0x80u) {
+                    key[i] = tn;
+                    val[i] = cb + (m & 0x7Fu);
+                } else {
+                    const int leaf = (int)(lb + m);
+                    float t, u, v;
+                    if (hit_leaf(s, leaf, o, d, best, t, u, v)) {
+                        best = t; hit.t = t; hit.u = u; hit.v = v; hit.leaf = leaf;
+                    }
+                }
+            }
+        }
+        cas(key[0], val[0], key[1], val[1]); cas(key[2], val[2], key[3], val[3]);
+        cas(key[4], val[4], key[5], val[5]); cas(key[6], val[6], key[7], val[7]);
+        cas(key[0], val[0], key[2], val[2]); cas(key[1], val[1], key[3], val[3]);
+        cas(key[4], val[4], key[6], val[6]); cas(key[5], val[5], key[7], val[7]);
+        cas(key[1], val[1], key[2], val[2]); cas(key[5], val[5], key[6], val[6]);
+        cas(key[0], val[0], key[4], val[4]); cas(key[1], val[1], key[5], val[5]);
+        cas(key[2], val[2], key[6], val[6]); cas(key[3], val[3], key[7], val[7]);
+        cas(key[2], val[2], key[4], val[4]); cas(key[3], val[3], key[5], val[5]);
+        cas(key[1], val[1], key[2], val[2]); cas(key[3], val[3], key[4], val[4]);
+        cas(key[5], val[5], key[6], val[6]);
+        bool have_next = false;
+#pragma unroll
+        for (int i = 7; i >= 1; --i) {
+            if (key[i] < INFINITY && key[i] <= best) {
+                if (sp >= CPT_WSTACK) {
+                    if (err) atomicOr(err, CPT_DEVERR_STACK);
+                    return hit.leaf >= 0;
+                }
+                stack[sp++] = ((uint64_t)__float_as_uint(key[i]) << 32) | val[i];
+            }
+        }
+        if (key[0] < INFINITY && key[0] <= best) {
+            node = val[0];
+            have_next = true;
+        }
+        while (!have_next && sp > 0) {
+            uint64_t top = stack[--sp];
+            if (__uint_as_float((uint32_t)(top >> 32)) <= best) {
+                node = (uint32_t)top;
+                have_next = true;
+            }
+        }
+        if (!have_next) break;
+    }
+    return hit.leaf >= 0;
+}
+
 // Closest hit over [tmin (boxes), tmax].  Returns false on a miss.  *err gets
 // CPT_DEVERR_STACK if the fixed stack would overflow (cannot happen for Karras trees over
-// 64-bit keys, whose depth is at most 65).
+// 64-bit keys, whose depth is at most 65).  Uses the 8-wide BVH when the scene has one.
 __device__ __forceinline__ bool trace_closest(const SceneView& s, float3 o, float3 d, float tmin, float tmax, Hit& hit,
                                               int* err)
 {
+    if (s.wide && s.n_internal > 0) {
+        hit.leaf = -1;
+        hit.t = tmax;
+        hit.u = hit.v = 0.f;
+        return trace_closest_wide(s, o, d, tmin, tmax, hit, err);
+    }
     hit.leaf = -1;
     hit.t = tmax;
     hit.u = hit.v = 0.f;

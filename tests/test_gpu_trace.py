@@ -55,10 +55,18 @@ def check_t(gpu, ref_ids, ref_t):
     assert rel.max(initial=0) < 2e-5
 
 
+@pytest.fixture(params=[8, 2], ids=["bvh8", "bvh2"])
+def width(request, ctx):
+    ctx.set_bvh_width(request.param)
+    yield request.param
+    ctx.set_bvh_width(8)
+
+
 @pytest.mark.parametrize("name,seed,box", [("ico3", 1, 2.0), ("mixed", 3, 3.0)])
-def test_hits_match_reference_golden(ctx, oracle_mod, name, seed, box):
+def test_hits_match_reference_golden(ctx, oracle_mod, width, name, seed, box):
     d = scenes.by_name(name)
     s = api.Scene(ctx, d).init()
+    assert s.stats.num_wide_nodes > 0 if width == 8 else s.stats.num_wide_nodes == 0
     rays = P.uniform_rays(4096, seed=seed, box=box)
     gpu = s.trace(rays)
     G = golden(f"hits_{name}.npz")
@@ -68,7 +76,7 @@ def test_hits_match_reference_golden(ctx, oracle_mod, name, seed, box):
     check_t(gpu, G["ids"], G["t"])
 
 
-def test_hits_full_icosphere_vs_oracle(ctx, oracle_mod):
+def test_hits_full_icosphere_vs_oracle(ctx, oracle_mod, width):
     """The 1,310,720-triangle microbench scene with 10M rays traced on the GPU; a 131,072-ray
     sample (spread over the whole set) is checked against the oracle."""
     import torch
