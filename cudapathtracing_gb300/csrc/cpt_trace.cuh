@@ -114,6 +114,7 @@ __device__ __forceinline__ bool trace_closest_wide(const SceneView& s, float3 o,
         const uint32_t cb = __float_as_uint(h1.x), lb = __float_as_uint(h1.y);
         float key[8];
         uint32_t val[8];
+        uint32_t leafmask = 0;
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
             const int w = i >> 2, sh = (i & 3) * 8;
@@ -137,12 +138,19 @@ __device__ __forceinline__ bool trace_closest_wide(const SceneView& s, float3 o,
                     key[i] = tn;
                     val[i] = cb + (m & 0x7Fu);
                 } else {
-                    const int leaf = (int)(lb + m);
-                    float t, u, v;
-                    if (hit_leaf(s, leaf, o, d, best, t, u, v)) {
-                        best = t; hit.t = t; hit.u = u; hit.v = v; hit.leaf = leaf;
-                    }
+                    leafmask |= 1u << i;
                 }
+            }
+        }
+        // Leaf children in slot order, one copy of the primitive tests.
+        while (leafmask) {
+            const int i = __ffs(leafmask) - 1;
+            leafmask &= leafmask - 1;
+            const uint32_t m = ((i >> 2 ? __float_as_uint(h1.w) : __float_as_uint(h1.z)) >> ((i & 3) * 8)) & 0xFFu;
+            const int leaf = (int)(lb + m);
+            float t, u, v;
+            if (hit_leaf(s, leaf, o, d, best, t, u, v)) {
+                best = t; hit.t = t; hit.u = u; hit.v = v; hit.leaf = leaf;
             }
         }
         cas(key[0], val[0], key[1], val[1]); cas(key[2], val[2], key[3], val[3]);
@@ -182,30 +190,11 @@ __device__ __forceinline__ bool trace_closest_wide(const SceneView& s, float3 o,
     return hit.leaf >= 0;
 }
 
-// Closest hit over [tmin (boxes), tmax].  Returns false on a miss.  *err gets
-// CPT_DEVERR_STACK if the fixed stack would overflow (cannot happen for Karras trees over
-// 64-bit keys, whose depth is at most 65).  Uses the 8-wide BVH when the scene has one.
-__device__ __forceinline__ bool trace_closest(const SceneView& s, float3 o, float3 d, float tmin, float tmax, Hit& hit,
-                                              int* err)
+// Binary-node traversal (Aila–Laine node layout): near child first, far child pushed.  The
+// stack cannot overflow for Karras trees over 64-bit keys (at most 65 levels).
+__device__ __forceinline__ bool trace_closest_bvh2(const SceneView& s, float3 o, float3 d, float tmin, float tmax,
+                                                   Hit& hit, int* err)
 {
-    if (s.wide && s.n_internal > 0) {
-        hit.leaf = -1;
-        hit.t = tmax;
-        hit.u = hit.v = 0.f;
-        return trace_closest_wide(s, o, d, tmin, tmax, hit, err);
-    }
-    hit.leaf = -1;
-    hit.t = tmax;
-    hit.u = hit.v = 0.f;
-    if (s.n_prims <= 0) return false;
-    if (s.n_internal == 0) {
-        float t, u, v;
-        if (hit_leaf(s, 0, o, d, tmax, t, u, v)) {
-            hit.t = t; hit.u = u; hit.v = v; hit.leaf = 0;
-            return true;
-        }
-        return false;
-    }
     const float3 idir = f3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
     const float3 ood = f3(o.x * idir.x, o.y * idir.y, o.z * idir.z);
     int stack[CPT_STACK];
@@ -255,6 +244,30 @@ __device__ __forceinline__ bool trace_closest(const SceneView& s, float3 o, floa
         }
     }
     return hit.leaf >= 0;
+}
+
+// Closest hit over [tmin (boxes), tmax]; false on a miss.  WIDE selects the traversal layout at
+// compile time (each kernel is instantiated for the layout the scene was built with), so a
+// kernel carries the registers and code of one traversal only.  *err gets CPT_DEVERR_STACK if a
+// fixed stack would overflow.
+template <bool WIDE>
+__device__ __forceinline__ bool trace_closest(const SceneView& s, float3 o, float3 d, float tmin, float tmax, Hit& hit,
+                                              int* err)
+{
+    hit.leaf = -1;
+    hit.t = tmax;
+    hit.u = hit.v = 0.f;
+    if (s.n_prims <= 0) return false;
+    if (s.n_internal == 0) {
+        float t, u, v;
+        if (hit_leaf(s, 0, o, d, tmax, t, u, v)) {
+            hit.t = t; hit.u = u; hit.v = v; hit.leaf = 0;
+            return true;
+        }
+        return false;
+    }
+    if (WIDE) return trace_closest_wide(s, o, d, tmin, tmax, hit, err);
+    return trace_closest_bvh2(s, o, d, tmin, tmax, hit, err);
 }
 
 }  // namespace cpt

@@ -36,6 +36,7 @@ __device__ __forceinline__ int prim_of(const SceneView& s, const Hit& h)
     return h.leaf >= 0 ? __float_as_int(ldg4(s.leaf_rec + 3 * (size_t)h.leaf).w) : -1;
 }
 
+template <bool WIDE>
 __device__ PixelResult pixel_reference(const SceneView& s, int i, int j, const RenderArgs& a)
 {
     PixelResult out;
@@ -60,7 +61,7 @@ __device__ PixelResult pixel_reference(const SceneView& s, int i, int j, const R
                 break;
             }
             Hit h;
-            bool hit = trace_closest(s, o, d, 0.001f, CPT_INF_F, h, a.err);
+            bool hit = trace_closest<WIDE>(s,o, d, 0.001f, CPT_INF_F, h, a.err);
             out.rays++;
             Surf sf;
             if (hit) make_surface(s, o, d, h, true, sf);
@@ -68,7 +69,7 @@ __device__ PixelResult pixel_reference(const SceneView& s, int i, int j, const R
                 const float sig = 25.0f;
                 o = sf.pos;
                 Hit vh;
-                bool vhit = trace_closest(s, o, d, 0.001f, CPT_INF_F, vh, a.err);
+                bool vhit = trace_closest<WIDE>(s,o, d, 0.001f, CPT_INF_F, vh, a.err);
                 out.rays++;
                 if (!vhit) continue;
                 float dmax = vh.t;
@@ -91,7 +92,7 @@ __device__ PixelResult pixel_reference(const SceneView& s, int i, int j, const R
                     o = pos;
                     d = nd;
                     pos = sf.pos + t * nd;
-                    vhit = trace_closest(s, o, d, 0.001f, CPT_INF_F, vh, a.err);
+                    vhit = trace_closest<WIDE>(s,o, d, 0.001f, CPT_INF_F, vh, a.err);
                     out.rays++;
                     if (vhit) dmax = vh.t;
                     t = -logf(rng.one_minus_uniform_from(rng.next())) / sig;
@@ -120,7 +121,7 @@ __device__ PixelResult pixel_reference(const SceneView& s, int i, int j, const R
                 float3 lp = L.center + ((ua - 0.5f) * lw) * L.eu + ((ub - 0.5f) * lh) * L.ev;
                 float3 dir = unit3(lp - sf.pos);
                 Hit lh2;
-                trace_closest(s, sf.pos, dir, 0.001f, CPT_INF_F, lh2, a.err);
+                trace_closest<WIDE>(s,sf.pos, dir, 0.001f, CPT_INF_F, lh2, a.err);
                 out.rays++;
                 int obst = prim_of(s, lh2);
                 if (dot3(dir, sf.normal) > 0.f && dot3(-dir, L.normal) > 0.f && obst == k) {
@@ -148,6 +149,7 @@ __device__ PixelResult pixel_reference(const SceneView& s, int i, int j, const R
     return out;
 }
 
+template <bool WIDE>
 __device__ PixelResult pixel_config(const SceneView& s, int i, int j, const RenderArgs& a)
 {
     PixelResult out;
@@ -174,7 +176,7 @@ __device__ PixelResult pixel_config(const SceneView& s, int i, int j, const Rend
                 break;
             }
             Hit h;
-            bool hit = trace_closest(s, o, d, 0.001f, CPT_INF_F, h, a.err);
+            bool hit = trace_closest<WIDE>(s,o, d, 0.001f, CPT_INF_F, h, a.err);
             out.rays++;
             if (in_medium) {
                 float t_hit = hit ? h.t : CPT_INF_F;
@@ -235,7 +237,7 @@ __device__ PixelResult pixel_config(const SceneView& s, int i, int j, const Rend
                     float cs_ = dot3(dir, sf.normal), cl_ = dot3(-dir, L.normal);
                     if (!(cs_ > 0.f && cl_ > 0.f)) continue;   // cannot contribute: no shadow ray
                     Hit lh2;
-                    trace_closest(s, sf.pos, dir, 0.001f, CPT_INF_F, lh2, a.err);
+                    trace_closest<WIDE>(s,sf.pos, dir, 0.001f, CPT_INF_F, lh2, a.err);
                     out.rays++;
                     int obst = prim_of(s, lh2);
                     if (obst == k) {
@@ -276,7 +278,7 @@ __device__ __forceinline__ uint8_t to_u8(float x)   // Render.cu:256-258
     return (uint8_t)(254.99f * c);
 }
 
-template <int EST>
+template <int EST, bool WIDE>
 __global__ void k_render(SceneView s, RenderArgs a)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -284,7 +286,7 @@ __global__ void k_render(SceneView s, RenderArgs a)
     bool active = i < s.cam.width && j < a.row_end;
     uint32_t rays = 0;
     if (active) {
-        PixelResult r = EST == 0 ? pixel_reference(s, i, j, a) : pixel_config(s, i, j, a);
+        PixelResult r = EST == 0 ? pixel_reference<WIDE>(s, i, j, a) : pixel_config<WIDE>(s, i, j, a);
         size_t off = (size_t)j * s.cam.width + i;
         if (a.flags & CPT_RENDER_ACCUMULATE) {
             a.rgb[3 * off] += r.rgb.x;
@@ -321,10 +323,14 @@ cpt_status launch_render_megakernel(const SceneView& view, const RenderArgs& arg
     if (rows <= 0) return CPT_OK;
     dim3 block(bx, by);
     dim3 grid((view.cam.width + bx - 1) / bx, (rows + by - 1) / by);
-    if (args.estimator == CPT_ESTIMATOR_REFERENCE)
-        k_render<0><<<grid, block, 0, stream>>>(view, args);
-    else
-        k_render<1><<<grid, block, 0, stream>>>(view, args);
+    const bool wide = view.wide != nullptr;
+    if (args.estimator == CPT_ESTIMATOR_REFERENCE) {
+        if (wide) k_render<0, true><<<grid, block, 0, stream>>>(view, args);
+        else k_render<0, false><<<grid, block, 0, stream>>>(view, args);
+    } else {
+        if (wide) k_render<1, true><<<grid, block, 0, stream>>>(view, args);
+        else k_render<1, false><<<grid, block, 0, stream>>>(view, args);
+    }
     CPT_CUDA(cudaGetLastError());
     add_launches(1);
     return CPT_OK;

@@ -9,13 +9,14 @@ namespace cpt {
 
 namespace {
 
+template <bool WIDE>
 __global__ void k_trace(SceneView s, const float4* __restrict__ rays, uint64_t n, float4* __restrict__ hits, int* err)
 {
     uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float4 a = __ldg(rays + 2 * i), b = __ldg(rays + 2 * i + 1);
     Hit h;
-    bool hit = trace_closest(s, f3(a.x, a.y, a.z), f3(b.x, b.y, b.z), a.w, b.w, h, err);
+    bool hit = trace_closest<WIDE>(s, f3(a.x, a.y, a.z), f3(b.x, b.y, b.z), a.w, b.w, h, err);
     int prim = hit ? __float_as_int(ldg4(s.leaf_rec + 3 * (size_t)h.leaf).w) : -1;
     hits[i] = make_float4(hit ? h.t : -1.0f, __int_as_float(prim), h.u, h.v);
 }
@@ -31,7 +32,10 @@ cpt_status launch_trace(const SceneView& view, const cpt_ray* rays, uint64_t n, 
     const unsigned T = 128;
     uint64_t blocks = (n + T - 1) / T;
     if (blocks > 0x7fffffffull) return fail(CPT_ERR_INVALID_ARGUMENT, "cpt_trace_closest: too many rays");
-    k_trace<<<(unsigned)blocks, T, 0, stream>>>(view, (const float4*)rays, n, (float4*)hits, d_err);
+    if (view.wide)
+        k_trace<true><<<(unsigned)blocks, T, 0, stream>>>(view, (const float4*)rays, n, (float4*)hits, d_err);
+    else
+        k_trace<false><<<(unsigned)blocks, T, 0, stream>>>(view, (const float4*)rays, n, (float4*)hits, d_err);
     CPT_CUDA(cudaGetLastError());
     add_launches(1);
     return CPT_OK;

@@ -186,6 +186,7 @@ __global__ void k_wf_init(SceneView s, Wf w, RenderArgs a)
     w.q[slot] = slot;   // Q_0 holds every slot in order; its size is set by the host
 }
 
+template <bool WIDE>
 __global__ void __launch_bounds__(256) k_wf_trace(SceneView s, Wf w, int par)
 {
     const int n = w.cnt[par];
@@ -201,13 +202,14 @@ __global__ void __launch_bounds__(256) k_wf_trace(SceneView s, Wf w, int par)
         int slot = q[idx];
         float4 o = w.o[slot], d = w.d[slot];
         Hit h;
-        bool hit = trace_closest(s, xyz(o), xyz(d), 0.001f, CPT_INF_F, h, w.err);
+        bool hit = trace_closest<WIDE>(s,xyz(o), xyz(d), 0.001f, CPT_INF_F, h, w.err);
         w.hit[slot] = make_float4(h.t, __int_as_float(hit ? h.leaf : -1), h.u, h.v);
         rays++;
     }
     count_rays(w.rays, rays);
 }
 
+template <bool WIDE>
 __global__ void __launch_bounds__(256) k_wf_shadow(SceneView s, Wf w, int par)
 {
     const int n = w.cnt[4 + par];
@@ -217,7 +219,7 @@ __global__ void __launch_bounds__(256) k_wf_shadow(SceneView s, Wf w, int par)
         int e = sq[idx];
         int k = e % w.L;
         Hit h;
-        bool hit = trace_closest(s, xyz(w.so[e]), xyz(w.sd[e]), 0.001f, CPT_INF_F, h, w.err);
+        bool hit = trace_closest<WIDE>(s,xyz(w.so[e]), xyz(w.sd[e]), 0.001f, CPT_INF_F, h, w.err);
         int obst = hit ? __float_as_int(ldg4(s.leaf_rec + 3 * (size_t)h.leaf).w) : -1;
         w.svis[e] = obst == k ? 1 : 0;
         rays++;
@@ -431,6 +433,25 @@ __global__ void __launch_bounds__(128) k_wf_shade(SceneView s, Wf w, RenderArgs 
     }
 }
 
+// CHUNK iterations: trace, shadow, resolve, shade, with the traversal of the scene's layout.
+void enqueue_chunk(const SceneView& view, const Wf& w, const RenderArgs& args, int gt, int bt, int gs, int bs,
+                   cudaStream_t st)
+{
+    const bool wide = view.wide != nullptr;
+    for (int it = 0; it < CHUNK; ++it) {
+        int par = it & 1;
+        if (wide) {
+            k_wf_trace<true><<<gt, bt, 0, st>>>(view, w, par);
+            k_wf_shadow<true><<<gt, bt, 0, st>>>(view, w, par);
+        } else {
+            k_wf_trace<false><<<gt, bt, 0, st>>>(view, w, par);
+            k_wf_shadow<false><<<gt, bt, 0, st>>>(view, w, par);
+        }
+        k_wf_resolve<<<gs, bs, 0, st>>>(view, w, args, par);
+        k_wf_shade<<<gs, bs, 0, st>>>(view, w, args, par);
+    }
+}
+
 template <typename T>
 cpt_status carve(char*& p, size_t& left, T** out, size_t count)
 {
@@ -502,13 +523,7 @@ cpt_status launch_render_wavefront(const SceneView& view, const RenderArgs& args
         // Capture CHUNK iterations (4 launches each) once; replay until the queues drain.
         cudaStream_t cs = tune.capture_stream;
         CPT_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
-        for (int it = 0; it < CHUNK; ++it) {
-            int par = it & 1;
-            k_wf_trace<<<gt, bt, 0, cs>>>(view, w, par);
-            k_wf_shadow<<<gt, bt, 0, cs>>>(view, w, par);
-            k_wf_resolve<<<gs, bs, 0, cs>>>(view, w, args, par);
-            k_wf_shade<<<gs, bs, 0, cs>>>(view, w, args, par);
-        }
+        enqueue_chunk(view, w, args, gt, bt, gs, bs, cs);
         cudaError_t ce = cudaStreamEndCapture(cs, &graph);
         if (ce != cudaSuccess) {
             cudaFreeAsync(base, stream);
@@ -528,13 +543,7 @@ cpt_status launch_render_wavefront(const SceneView& view, const RenderArgs& args
         if (use_graph) {
             CPT_CUDA(cudaGraphLaunch(exec, stream));
         } else {
-            for (int it = 0; it < CHUNK; ++it) {
-                int par = it & 1;
-                k_wf_trace<<<gt, bt, 0, stream>>>(view, w, par);
-                k_wf_shadow<<<gt, bt, 0, stream>>>(view, w, par);
-                k_wf_resolve<<<gs, bs, 0, stream>>>(view, w, args, par);
-                k_wf_shade<<<gs, bs, 0, stream>>>(view, w, args, par);
-            }
+            enqueue_chunk(view, w, args, gt, bt, gs, bs, stream);
         }
         add_launches(4 * CHUNK);
         CPT_CUDA(cudaMemcpyAsync(host_cnt, w.cnt, sizeof host_cnt, cudaMemcpyDeviceToHost, stream));
@@ -559,7 +568,10 @@ namespace cpt {
 cpt_status wavefront_grids(int sm_count, int block_trace, int block_shade, int* grid_trace, int* grid_shade)
 {
     int bt = 0, bs = 0;
-    CPT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bt, k_wf_trace, block_trace, 0));
+    int bt2 = 0;
+    CPT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bt, k_wf_trace<true>, block_trace, 0));
+    CPT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bt2, k_wf_trace<false>, block_trace, 0));
+    bt = std::min(bt, bt2);
     CPT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bs, k_wf_shade, block_shade, 0));
     *grid_trace = std::max(1, bt) * sm_count;
     *grid_shade = std::max(1, bs) * sm_count;
