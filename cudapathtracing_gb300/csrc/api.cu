@@ -367,7 +367,7 @@ cpt_status make_layout(cpt_scene* s, cudaStream_t stream, uint32_t* num_wide)
     int width = s->ctx->bvh_width;
     if (width == 8 && n > 1) {
         if (!s->wide) {
-            cpt_status st = dalloc(&s->wide, 5 * (size_t)ni);
+            cpt_status st = dalloc(&s->wide, 8 * (size_t)ni);
             if (st != CPT_OK) return st;
         }
         if (wide_scratch_bytes(n) > s->scratch_bytes) return fail(CPT_ERR_INVALID_ARGUMENT, "wide scratch too small");

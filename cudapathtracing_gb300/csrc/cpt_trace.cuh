@@ -82,108 +82,96 @@ __device__ __forceinline__ bool hit_leaf(const SceneView& s, int k, float3 o, fl
     return hit_light(s.lights[__float_as_int(r1.x)], o, d, 0.001f, tmax, t);
 }
 
-__device__ __forceinline__ void cas(float& ka, uint32_t& va, float& kb, uint32_t& vb)
+__device__ __forceinline__ uint32_t word_of(const float4& f, int w)
 {
-    if (kb < ka) {
-        float tk = ka; ka = kb; kb = tk;
-        uint32_t tv = va; va = vb; vb = tv;
-    }
+    return __float_as_uint(w == 0 ? f.x : (w == 1 ? f.y : (w == 2 ? f.z : f.w)));
 }
 
-// Closest hit through the compressed 8-wide BVH (layout in wide.cu).  Each visit decodes the 8
-// quantised child boxes, tests leaf children at once (as the reference tests leaves when it
-// reaches them), sorts the hit internal children by entry distance with a 19-comparator Batcher
-// network held in registers, continues with the nearest and pushes the others far-to-near with
-// their entry distance; popped entries farther than the closest hit are skipped.
+// Closest hit through the compressed 8-wide BVH (layout in wide.cu).  A visit decodes the 8
+// 16-bit quantised child boxes and tests them; hit children are recorded in a byte mask at bit
+// positions slot ^ (7 ^ octant), which orders them roughly front to back for this ray (the slots
+// were assigned by direction at build time).  Leaf children are tested at once, nearest bit
+// first (the reference tests leaves as it reaches them); the traversal continues with the first
+// internal child and keeps the rest as one node-group entry (first child index, internal-slot
+// mask, remaining hit bits) on the stack, as in compressed wide BVH traversal (Ylitie et al.
+// 2017).  Boxes are tested against the closest hit so far, so far subtrees are culled.
 __device__ __forceinline__ bool trace_closest_wide(const SceneView& s, float3 o, float3 d, float tmin, float tmax,
                                                    Hit& hit, int* err)
 {
     const float3 idir = f3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
+    const uint32_t first = 7u ^ ((d.x < 0.f ? 1u : 0u) | (d.y < 0.f ? 2u : 0u) | (d.z < 0.f ? 4u : 0u));
     float best = tmax;
     uint64_t stack[CPT_WSTACK];
     int sp = 0;
     uint32_t node = 0;
     for (;;) {
-        const float4* np = s.wide + 5 * (size_t)node;
-        const float4 h0 = ldg4(np), h1 = ldg4(np + 1), q0 = ldg4(np + 2), q1 = ldg4(np + 3), q2 = ldg4(np + 4);
-        const uint32_t e = __float_as_uint(h0.w);
+        const float4* np = s.wide + 8 * (size_t)node;
+        const float4 f0 = ldg4(np), f1 = ldg4(np + 1);
+        const float4 f2 = ldg4(np + 2), f3v = ldg4(np + 3), f4 = ldg4(np + 4), f5 = ldg4(np + 5), f6 = ldg4(np + 6),
+                     f7 = ldg4(np + 7);
+        const uint32_t e = __float_as_uint(f0.w);
+        const uint32_t imask = e >> 24;
         const float ax = __uint_as_float((e & 0xFFu) << 23) * idir.x;
         const float ay = __uint_as_float(((e >> 8) & 0xFFu) << 23) * idir.y;
         const float az = __uint_as_float(((e >> 16) & 0xFFu) << 23) * idir.z;
-        const float bx = (h0.x - o.x) * idir.x, by = (h0.y - o.y) * idir.y, bz = (h0.z - o.z) * idir.z;
-        const uint32_t cb = __float_as_uint(h1.x), lb = __float_as_uint(h1.y);
-        float key[8];
-        uint32_t val[8];
-        uint32_t leafmask = 0;
+        const float bx = (f0.x - o.x) * idir.x, by = (f0.y - o.y) * idir.y, bz = (f0.z - o.z) * idir.z;
+        const uint32_t cb = __float_as_uint(f1.x), lb = __float_as_uint(f1.y);
+        const uint32_t meta0 = __float_as_uint(f1.z), meta1 = __float_as_uint(f1.w);
+        uint32_t ihits = 0, lhits = 0;
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
-            const int w = i >> 2, sh = (i & 3) * 8;
-            const uint32_t m = ((w ? __float_as_uint(h1.w) : __float_as_uint(h1.z)) >> sh) & 0xFFu;
-            key[i] = INFINITY;
-            val[i] = 0;
+            const uint32_t m = ((i < 4 ? meta0 : meta1) >> ((i & 3) * 8)) & 0xFFu;
             if (m == 0xFFu) continue;
-            const float lx = (float)(((w ? __float_as_uint(q0.y) : __float_as_uint(q0.x)) >> sh) & 0xFFu);
-            const float hx = (float)(((w ? __float_as_uint(q0.w) : __float_as_uint(q0.z)) >> sh) & 0xFFu);
-            const float ly = (float)(((w ? __float_as_uint(q1.y) : __float_as_uint(q1.x)) >> sh) & 0xFFu);
-            const float hy = (float)(((w ? __float_as_uint(q1.w) : __float_as_uint(q1.z)) >> sh) & 0xFFu);
-            const float lz = (float)(((w ? __float_as_uint(q2.y) : __float_as_uint(q2.x)) >> sh) & 0xFFu);
-            const float hz = (float)(((w ? __float_as_uint(q2.w) : __float_as_uint(q2.z)) >> sh) & 0xFFu);
+            const int qw = i >> 1, qs = (i & 1) * 16;
+            const float lx = (float)((word_of(f2, qw) >> qs) & 0xFFFFu);
+            const float hx = (float)((word_of(f3v, qw) >> qs) & 0xFFFFu);
+            const float ly = (float)((word_of(f4, qw) >> qs) & 0xFFFFu);
+            const float hy = (float)((word_of(f5, qw) >> qs) & 0xFFFFu);
+            const float lz = (float)((word_of(f6, qw) >> qs) & 0xFFFFu);
+            const float hz = (float)((word_of(f7, qw) >> qs) & 0xFFFFu);
             const float x0 = fmaf(lx, ax, bx), x1 = fmaf(hx, ax, bx);
             const float y0 = fmaf(ly, ay, by), y1 = fmaf(hy, ay, by);
             const float z0 = fmaf(lz, az, bz), z1 = fmaf(hz, az, bz);
             const float tn = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fmaxf(fminf(z0, z1), tmin));
             const float tf = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fminf(fmaxf(z0, z1), best));
             if (tn <= tf) {
-                if (m & 0x80u) {
-                    key[i] = tn;
-                    val[i] = cb + (m & 0x7Fu);
-                } else {
-                    leafmask |= 1u << i;
-                }
+                const uint32_t bit = 1u << ((uint32_t)i ^ first);
+                if (m & 0x80u) ihits |= bit;
+                else lhits |= bit;
             }
         }
-        // Leaf children in slot order, one copy of the primitive tests.
-        while (leafmask) {
-            const int i = __ffs(leafmask) - 1;
-            leafmask &= leafmask - 1;
-            const uint32_t m = ((i >> 2 ? __float_as_uint(h1.w) : __float_as_uint(h1.z)) >> ((i & 3) * 8)) & 0xFFu;
+        while (lhits) {
+            const uint32_t slot = (uint32_t)(__ffs(lhits) - 1) ^ first;
+            lhits &= lhits - 1;
+            const uint32_t m = ((slot < 4 ? meta0 : meta1) >> ((slot & 3) * 8)) & 0x7Fu;
             const int leaf = (int)(lb + m);
             float t, u, v;
             if (hit_leaf(s, leaf, o, d, best, t, u, v)) {
                 best = t; hit.t = t; hit.u = u; hit.v = v; hit.leaf = leaf;
             }
         }
-        cas(key[0], val[0], key[1], val[1]); cas(key[2], val[2], key[3], val[3]);
-        cas(key[4], val[4], key[5], val[5]); cas(key[6], val[6], key[7], val[7]);
-        cas(key[0], val[0], key[2], val[2]); cas(key[1], val[1], key[3], val[3]);
-        cas(key[4], val[4], key[6], val[6]); cas(key[5], val[5], key[7], val[7]);
-        cas(key[1], val[1], key[2], val[2]); cas(key[5], val[5], key[6], val[6]);
-        cas(key[0], val[0], key[4], val[4]); cas(key[1], val[1], key[5], val[5]);
-        cas(key[2], val[2], key[6], val[6]); cas(key[3], val[3], key[7], val[7]);
-        cas(key[2], val[2], key[4], val[4]); cas(key[3], val[3], key[5], val[5]);
-        cas(key[1], val[1], key[2], val[2]); cas(key[3], val[3], key[4], val[4]);
-        cas(key[5], val[5], key[6], val[6]);
+        uint32_t g_cb = cb, g_imask = imask, g_hits = ihits;
         bool have_next = false;
-#pragma unroll
-        for (int i = 7; i >= 1; --i) {
-            if (key[i] < INFINITY && key[i] <= best) {
-                if (sp >= CPT_WSTACK) {
-                    if (err) atomicOr(err, CPT_DEVERR_STACK);
-                    return hit.leaf >= 0;
+        for (;;) {
+            if (g_hits) {
+                const uint32_t slot = (uint32_t)(__ffs(g_hits) - 1) ^ first;
+                g_hits &= g_hits - 1;
+                node = g_cb + __popc(g_imask & ((1u << slot) - 1u));
+                if (g_hits) {
+                    if (sp >= CPT_WSTACK) {
+                        if (err) atomicOr(err, CPT_DEVERR_STACK);
+                        return hit.leaf >= 0;
+                    }
+                    stack[sp++] = (uint64_t)g_cb | ((uint64_t)g_imask << 32) | ((uint64_t)g_hits << 40);
                 }
-                stack[sp++] = ((uint64_t)__float_as_uint(key[i]) << 32) | val[i];
-            }
-        }
-        if (key[0] < INFINITY && key[0] <= best) {
-            node = val[0];
-            have_next = true;
-        }
-        while (!have_next && sp > 0) {
-            uint64_t top = stack[--sp];
-            if (__uint_as_float((uint32_t)(top >> 32)) <= best) {
-                node = (uint32_t)top;
                 have_next = true;
+                break;
             }
+            if (sp == 0) break;
+            const uint64_t g = stack[--sp];
+            g_cb = (uint32_t)g;
+            g_imask = (uint32_t)(g >> 32) & 0xFFu;
+            g_hits = (uint32_t)(g >> 40) & 0xFFu;
         }
         if (!have_next) break;
     }

@@ -2,19 +2,22 @@
 //
 // Each wide node stands for one binary node b: starting from b's two children, the child with
 // the largest surface area that is an internal binary node is replaced by its two children until
-// there are 8 children or only leaves remain.  Node layout (80 bytes, five 16-byte loads):
+// there are 8 children or only leaves remain.  Children are then placed in slots by direction:
+// slot s (bits: negative x, y, z) holds the child whose centroid offset from the node's centre
+// points most along (+-1, +-1, +-1)_s (greedy assignment), so that a ray of octant o meets the
+// children roughly in the order of slots s ^ (7 ^ o) — the ordering scheme of compressed wide
+// BVHs (Ylitie, Karras, Laine 2017), which needs no sort during traversal.
 //
-//   float4 h0   origin p.xyz (the node's box minimum), w = exponent bytes ex | ey << 8 | ez << 16
-//   uint4  h1   x = first internal child's wide index, y = first leaf slot, z/w = meta bytes
-//               for slots 0..7: 0xFF empty, 0x80 | r internal child r, r leaf child r
-//   uint4  q0   x: lo bytes for slots 0..7 (x) then hi bytes (x)
-//   uint4  q1   y: lo, hi
-//   uint4  q2   z: lo, hi
+// Node layout (128 bytes, eight 16-byte loads):
+//   float4 f0   origin p.xyz (node box minimum); w = ex | ey << 8 | ez << 16 | imask << 24
+//               (biased grid exponents, bit s of imask: slot s is an internal child)
+//   uint4  f1   x = first internal child's wide index, y = first leaf slot,
+//               z/w = meta bytes of slots 0..7: 0xFF empty, 0x80 | r internal child r, r leaf r
+//   f2..f7      16-bit quantised child boxes, 8 slots each: lo.x, hi.x, lo.y, hi.y, lo.z, hi.z
 //
-// Child boxes are quantised to 8 bits per plane on a power-of-two grid anchored at p, rounded
-// outwards (lo down, hi up), so every child box contains its exact FP32 box.  Leaf children of a
-// wide node occupy consecutive leaf slots; leaf records are rewritten in that slot order, so the
-// traversal reads the records of one node's leaves from one place.
+// Child boxes sit on a power-of-two grid anchored at p with 65535 steps across the node, rounded
+// outwards, so every quantised box contains the child's FP32 box.  Internal children and leaf
+// children are numbered in slot order; leaf records are rewritten in leaf-slot order.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -38,13 +41,13 @@ __device__ __forceinline__ void ref_box(int ref, const float4* node_box, const f
     mx = b[1];
 }
 
-// Exponent byte e (biased by 127) such that 255 * 2^(e-127) >= extent, for extent >= 0.
+// Biased exponent e such that 65535 * 2^(e-127) >= extent (extent >= 0).
 __device__ __forceinline__ uint32_t grid_exponent(float lo, float hi)
 {
     float ext = __fsub_ru(hi, lo);
-    float x = __fdiv_ru(ext, 255.0f);
+    float x = __fdiv_ru(ext, 65535.0f);
     int e = 0;
-    if (x > 0.0f) frexpf(x, &e);   // x = m * 2^e, m in [0.5, 1): 2^e > x
+    if (x > 0.0f) frexpf(x, &e);   // x = m * 2^e with m in [0.5, 1): 2^e > x
     e = max(-126, min(127, e));
     return (uint32_t)(e + 127);
 }
@@ -52,14 +55,16 @@ __device__ __forceinline__ uint32_t grid_exponent(float lo, float hi)
 __device__ __forceinline__ uint32_t q_lo(float v, float p, float inv_scale)
 {
     float t = floorf(__fmul_rd(__fsub_rd(v, p), inv_scale));
-    return (uint32_t)fminf(fmaxf(t, 0.0f), 255.0f);
+    return (uint32_t)fminf(fmaxf(t, 0.0f), 65535.0f);
 }
 
 __device__ __forceinline__ uint32_t q_hi(float v, float p, float inv_scale)
 {
     float t = ceilf(__fmul_ru(__fsub_ru(v, p), inv_scale));
-    return (uint32_t)fminf(fmaxf(t, 0.0f), 255.0f);
+    return (uint32_t)fminf(fmaxf(t, 0.0f), 65535.0f);
 }
+
+__device__ __forceinline__ float inv_grid(uint32_t e) { return __int_as_float((int)((254u - e) << 23)); }
 
 __global__ void k_collapse_level(const int2* __restrict__ child, const float4* __restrict__ node_box,
                                  const float4* __restrict__ leaf_box, const int2* __restrict__ tasks_in,
@@ -93,53 +98,88 @@ __global__ void k_collapse_level(const int2* __restrict__ child, const float4* _
             refs[best] = cc.x;
             refs[nr++] = cc.y;
         }
+        float4 nmn, nmx;
+        ref_box(b, node_box, leaf_box, nmn, nmx);
+        const float cx = 0.5f * (nmn.x + nmx.x), cy = 0.5f * (nmn.y + nmx.y), cz = 0.5f * (nmn.z + nmx.z);
+        // greedy slot assignment by direction
+        int slot_of[8];
+        float dx[8], dy[8], dz[8];
+        for (int k = 0; k < nr; ++k) {
+            float4 mn, mx;
+            ref_box(refs[k], node_box, leaf_box, mn, mx);
+            dx[k] = 0.5f * (mn.x + mx.x) - cx;
+            dy[k] = 0.5f * (mn.y + mx.y) - cy;
+            dz[k] = 0.5f * (mn.z + mx.z) - cz;
+            slot_of[k] = -1;
+        }
+        uint32_t used = 0;
+        for (int round = 0; round < nr; ++round) {
+            float best = INFINITY;
+            int bk = -1, bs = -1;
+            for (int k = 0; k < nr; ++k) {
+                if (slot_of[k] >= 0) continue;
+                for (int s = 0; s < 8; ++s) {
+                    if ((used >> s) & 1u) continue;
+                    float cost = -((s & 1 ? -dx[k] : dx[k]) + (s & 2 ? -dy[k] : dy[k]) + (s & 4 ? -dz[k] : dz[k]));
+                    if (cost < best) {
+                        best = cost;
+                        bk = k;
+                        bs = s;
+                    }
+                }
+            }
+            slot_of[bk] = bs;
+            used |= 1u << bs;
+        }
+        int at_slot[8];
+        for (int s = 0; s < 8; ++s) at_slot[s] = 0x7fffffff;   // empty
+        for (int k = 0; k < nr; ++k) at_slot[slot_of[k]] = refs[k];
         int n_int = 0, n_leaf = 0;
         for (int k = 0; k < nr; ++k) (refs[k] >= 0 ? n_int : n_leaf)++;
         int cb = n_int ? atomicAdd(&counters[0], n_int) : 0;
         int lb = n_leaf ? atomicAdd(&counters[1], n_leaf) : 0;
-        float4 nmn, nmx;
-        ref_box(b, node_box, leaf_box, nmn, nmx);
         uint32_t ex = grid_exponent(nmn.x, nmx.x), ey = grid_exponent(nmn.y, nmx.y), ez = grid_exponent(nmn.z, nmx.z);
-        float isx = __int_as_float((int)((254u - ex) << 23));   // 2^-(e-127)
-        float isy = __int_as_float((int)((254u - ey) << 23));
-        float isz = __int_as_float((int)((254u - ez) << 23));
+        float isx = inv_grid(ex), isy = inv_grid(ey), isz = inv_grid(ez);
         uint32_t meta[2] = {0xFFFFFFFFu, 0xFFFFFFFFu};
-        uint32_t qlx[2] = {0, 0}, qhx[2] = {0, 0}, qly[2] = {0, 0}, qhy[2] = {0, 0}, qlz[2] = {0, 0}, qhz[2] = {0, 0};
+        uint32_t q[6][4];
+        for (int a = 0; a < 6; ++a)
+            for (int w = 0; w < 4; ++w) q[a][w] = 0;
+        uint32_t imask = 0;
         int ri = 0, rl = 0;
-        int2* out = tasks_out;
-        for (int k = 0; k < nr; ++k) {
+        for (int s = 0; s < 8; ++s) {
+            int ref = at_slot[s];
+            if (ref == 0x7fffffff) continue;
             float4 mn, mx;
-            ref_box(refs[k], node_box, leaf_box, mn, mx);
+            ref_box(ref, node_box, leaf_box, mn, mx);
             uint32_t m;
-            if (refs[k] >= 0) {
+            if (ref >= 0) {
                 m = 0x80u | (uint32_t)ri;
+                imask |= 1u << s;
                 int slot = atomicAdd(n_out, 1);
-                out[slot] = make_int2(refs[k], cb + ri);
+                tasks_out[slot] = make_int2(ref, cb + ri);
                 ri++;
             } else {
                 m = (uint32_t)rl;
-                leaf_perm[lb + rl] = (uint32_t)(~refs[k]);
+                leaf_perm[lb + rl] = (uint32_t)(~ref);
                 rl++;
             }
-            int word = k >> 2, sh = (k & 3) * 8;
+            int word = s >> 2, sh = (s & 3) * 8;
             meta[word] = (meta[word] & ~(0xFFu << sh)) | (m << sh);
-            qlx[word] |= q_lo(mn.x, nmn.x, isx) << sh;
-            qhx[word] |= q_hi(mx.x, nmn.x, isx) << sh;
-            qly[word] |= q_lo(mn.y, nmn.y, isy) << sh;
-            qhy[word] |= q_hi(mx.y, nmn.y, isy) << sh;
-            qlz[word] |= q_lo(mn.z, nmn.z, isz) << sh;
-            qhz[word] |= q_hi(mx.z, nmn.z, isz) << sh;
+            int qw = s >> 1, qs = (s & 1) * 16;
+            q[0][qw] |= q_lo(mn.x, nmn.x, isx) << qs;
+            q[1][qw] |= q_hi(mx.x, nmn.x, isx) << qs;
+            q[2][qw] |= q_lo(mn.y, nmn.y, isy) << qs;
+            q[3][qw] |= q_hi(mx.y, nmn.y, isy) << qs;
+            q[4][qw] |= q_lo(mn.z, nmn.z, isz) << qs;
+            q[5][qw] |= q_hi(mx.z, nmn.z, isz) << qs;
         }
-        float4* dst = wide + 5 * (size_t)wi;
-        dst[0] = make_float4(nmn.x, nmn.y, nmn.z, __int_as_float((int)(ex | (ey << 8) | (ez << 16))));
+        float4* dst = wide + 8 * (size_t)wi;
+        dst[0] = make_float4(nmn.x, nmn.y, nmn.z, __int_as_float((int)(ex | (ey << 8) | (ez << 16) | (imask << 24))));
         dst[1] = make_float4(__int_as_float(cb), __int_as_float(lb), __int_as_float((int)meta[0]),
                              __int_as_float((int)meta[1]));
-        dst[2] = make_float4(__int_as_float((int)qlx[0]), __int_as_float((int)qlx[1]), __int_as_float((int)qhx[0]),
-                             __int_as_float((int)qhx[1]));
-        dst[3] = make_float4(__int_as_float((int)qly[0]), __int_as_float((int)qly[1]), __int_as_float((int)qhy[0]),
-                             __int_as_float((int)qhy[1]));
-        dst[4] = make_float4(__int_as_float((int)qlz[0]), __int_as_float((int)qlz[1]), __int_as_float((int)qhz[0]),
-                             __int_as_float((int)qhz[1]));
+        for (int a = 0; a < 6; ++a)
+            dst[2 + a] = make_float4(__int_as_float((int)q[a][0]), __int_as_float((int)q[a][1]),
+                                     __int_as_float((int)q[a][2]), __int_as_float((int)q[a][3]));
     }
 }
 
@@ -189,7 +229,7 @@ __global__ void k_wide_leaf_records(const uint32_t* __restrict__ leaf_perm, cons
 
 size_t wide_scratch_bytes(uint32_t n)
 {
-    // two task queues of up to n entries + two counters pairs
+    // two task queues of up to n entries, counters, the leaf permutation
     return align_up((size_t)n * 8, 256) * 2 + 256 + align_up((size_t)n * 4, 256);
 }
 
