@@ -9,6 +9,8 @@
 #define CPT_PI_F 3.14159265358979323846f     // PI (rtmath.cuh:9)
 #define CPT_STACK 64                          // Karras trees over 64-bit keys are at most 65 levels deep
 #define CPT_WSTACK 72                         // 8-wide traversal: at most one node group per level
+#define CPT_WIDE_F4 6                         // float4 per wide node (96 bytes)
+#define CPT_WIDE_EMPTY 0x7fffffff             // child reference of an unused wide-node slot
 
 // Primitive kinds stored in leaf records (w of the second float4).
 enum { CPT_KIND_TRI = 0, CPT_KIND_SPHERE = 1, CPT_KIND_LIGHT = 2 };
@@ -66,7 +68,7 @@ struct DevCamera {     // Camera (Camera.cu:5-40), derived in double on the host
 struct SceneView {
     int n_prims, n_lights, n_spheres, n_tris, n_internal;
     const float4* __restrict__ nodes;      // BVH2: 4 float4 per internal node (Aila-Laine layout)
-    const float4* __restrict__ wide;       // BVH8: 8 float4 per wide node, or NULL (use BVH2)
+    const float4* __restrict__ wide;       // BVH8: CPT_WIDE_F4 float4 per wide node, or NULL (use BVH2)
     const float4* __restrict__ leaf_rec;   // 3 float4 per leaf (sorted order, or wide slot order)
     const uint32_t* __restrict__ tri_mat;  // per triangle
     const float* __restrict__ tri_n;       // optional smooth normals, 9 per triangle

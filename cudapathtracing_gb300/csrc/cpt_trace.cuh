@@ -105,30 +105,23 @@ __device__ __forceinline__ bool trace_closest_wide(const SceneView& s, float3 o,
     int sp = 0;
     uint32_t node = 0;
     for (;;) {
-        const float4* np = s.wide + 8 * (size_t)node;
-        const float4 f0 = ldg4(np), f1 = ldg4(np + 1);
-        const float4 f2 = ldg4(np + 2), f3v = ldg4(np + 3), f4 = ldg4(np + 4), f5 = ldg4(np + 5), f6 = ldg4(np + 6),
-                     f7 = ldg4(np + 7);
+        const float4* np = s.wide + CPT_WIDE_F4 * (size_t)node;
+        const float4 f0 = ldg4(np), f1 = ldg4(np + 1), f2 = ldg4(np + 2);
+        const float4 qx = ldg4(np + 3), qy = ldg4(np + 4), qz = ldg4(np + 5);
         const uint32_t e = __float_as_uint(f0.w);
-        const uint32_t imask = e >> 24;
         const float ax = __uint_as_float((e & 0xFFu) << 23) * idir.x;
         const float ay = __uint_as_float(((e >> 8) & 0xFFu) << 23) * idir.y;
         const float az = __uint_as_float(((e >> 16) & 0xFFu) << 23) * idir.z;
         const float bx = (f0.x - o.x) * idir.x, by = (f0.y - o.y) * idir.y, bz = (f0.z - o.z) * idir.z;
-        const uint32_t cb = __float_as_uint(f1.x), lb = __float_as_uint(f1.y);
-        const uint32_t meta0 = __float_as_uint(f1.z), meta1 = __float_as_uint(f1.w);
         uint32_t ihits = 0, lhits = 0;
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
-            const uint32_t m = ((i < 4 ? meta0 : meta1) >> ((i & 3) * 8)) & 0xFFu;
-            if (m == 0xFFu) continue;
-            const int qw = i >> 1, qs = (i & 1) * 16;
-            const float lx = (float)((word_of(f2, qw) >> qs) & 0xFFFFu);
-            const float hx = (float)((word_of(f3v, qw) >> qs) & 0xFFFFu);
-            const float ly = (float)((word_of(f4, qw) >> qs) & 0xFFFFu);
-            const float hy = (float)((word_of(f5, qw) >> qs) & 0xFFFFu);
-            const float lz = (float)((word_of(f6, qw) >> qs) & 0xFFFFu);
-            const float hz = (float)((word_of(f7, qw) >> qs) & 0xFFFFu);
+            const int ref = (int)(i < 4 ? word_of(f1, i & 3) : word_of(f2, i & 3));
+            if (ref == CPT_WIDE_EMPTY) continue;
+            const int lo = i >> 2, sh = (i & 3) * 8;
+            const float lx = (float)((word_of(qx, lo) >> sh) & 0xFFu), hx = (float)((word_of(qx, 2 + lo) >> sh) & 0xFFu);
+            const float ly = (float)((word_of(qy, lo) >> sh) & 0xFFu), hy = (float)((word_of(qy, 2 + lo) >> sh) & 0xFFu);
+            const float lz = (float)((word_of(qz, lo) >> sh) & 0xFFu), hz = (float)((word_of(qz, 2 + lo) >> sh) & 0xFFu);
             const float x0 = fmaf(lx, ax, bx), x1 = fmaf(hx, ax, bx);
             const float y0 = fmaf(ly, ay, by), y1 = fmaf(hy, ay, by);
             const float z0 = fmaf(lz, az, bz), z1 = fmaf(hz, az, bz);
@@ -136,42 +129,44 @@ __device__ __forceinline__ bool trace_closest_wide(const SceneView& s, float3 o,
             const float tf = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fminf(fmaxf(z0, z1), best));
             if (tn <= tf) {
                 const uint32_t bit = 1u << ((uint32_t)i ^ first);
-                if (m & 0x80u) ihits |= bit;
+                if (ref >= 0) ihits |= bit;
                 else lhits |= bit;
             }
         }
         while (lhits) {
             const uint32_t slot = (uint32_t)(__ffs(lhits) - 1) ^ first;
             lhits &= lhits - 1;
-            const uint32_t m = ((slot < 4 ? meta0 : meta1) >> ((slot & 3) * 8)) & 0x7Fu;
-            const int leaf = (int)(lb + m);
+            const int leaf = ~(int)(slot < 4 ? word_of(f1, slot & 3) : word_of(f2, slot & 3));
             float t, u, v;
             if (hit_leaf(s, leaf, o, d, best, t, u, v)) {
                 best = t; hit.t = t; hit.u = u; hit.v = v; hit.leaf = leaf;
             }
         }
-        uint32_t g_cb = cb, g_imask = imask, g_hits = ihits;
+        // Continue with the first hit internal child; the others stay on the stack as one group
+        // (this node, remaining hit bits) and are read back from the node when popped.
         bool have_next = false;
-        for (;;) {
-            if (g_hits) {
-                const uint32_t slot = (uint32_t)(__ffs(g_hits) - 1) ^ first;
-                g_hits &= g_hits - 1;
-                node = g_cb + __popc(g_imask & ((1u << slot) - 1u));
-                if (g_hits) {
-                    if (sp >= CPT_WSTACK) {
-                        if (err) atomicOr(err, CPT_DEVERR_STACK);
-                        return hit.leaf >= 0;
-                    }
-                    stack[sp++] = (uint64_t)g_cb | ((uint64_t)g_imask << 32) | ((uint64_t)g_hits << 40);
+        if (ihits) {
+            const uint32_t slot = (uint32_t)(__ffs(ihits) - 1) ^ first;
+            const uint32_t rest = ihits & (ihits - 1);
+            const uint32_t cur = node;
+            node = slot < 4 ? word_of(f1, slot & 3) : word_of(f2, slot & 3);
+            if (rest) {
+                if (sp >= CPT_WSTACK) {
+                    if (err) atomicOr(err, CPT_DEVERR_STACK);
+                    return hit.leaf >= 0;
                 }
-                have_next = true;
-                break;
+                stack[sp++] = (uint64_t)cur | ((uint64_t)rest << 32);
             }
-            if (sp == 0) break;
+            have_next = true;
+        } else if (sp > 0) {
             const uint64_t g = stack[--sp];
-            g_cb = (uint32_t)g;
-            g_imask = (uint32_t)(g >> 32) & 0xFFu;
-            g_hits = (uint32_t)(g >> 40) & 0xFFu;
+            const uint32_t gnode = (uint32_t)g;
+            const uint32_t hits = (uint32_t)(g >> 32);
+            const uint32_t slot = (uint32_t)(__ffs(hits) - 1) ^ first;
+            const uint32_t rest = hits & (hits - 1);
+            if (rest) stack[sp++] = (uint64_t)gnode | ((uint64_t)rest << 32);
+            node = (uint32_t)__ldg(reinterpret_cast<const int*>(s.wide + CPT_WIDE_F4 * (size_t)gnode + 1) + slot);
+            have_next = true;
         }
         if (!have_next) break;
     }

@@ -675,7 +675,7 @@ cpt_status build_trace_layout(uint32_t n, uint32_t n_lights, uint32_t n_spheres,
                               float4* leaf_rec, cudaStream_t stream)
 {
     if (n == 0) return CPT_OK;
-    if (n > 1) k_bvh2_nodes<<<blocks_for(n - 1, 256), 256, 0, stream>>>(child, node_box, leaf_box, n - 1, nodes);
+    if (n > 1 && nodes) k_bvh2_nodes<<<blocks_for(n - 1, 256), 256, 0, stream>>>(child, node_box, leaf_box, n - 1, nodes);
     if (tri_f64)
         k_leaf_records<double><<<blocks_for(n, 256), 256, 0, stream>>>(order, n, n_lights, n_spheres, tri_f64, spheres,
                                                                        leaf_rec);
@@ -683,7 +683,7 @@ cpt_status build_trace_layout(uint32_t n, uint32_t n_lights, uint32_t n_spheres,
         k_leaf_records<float><<<blocks_for(n, 256), 256, 0, stream>>>(order, n, n_lights, n_spheres, tri_f32, spheres,
                                                                       leaf_rec);
     CPT_CUDA(cudaGetLastError());
-    add_launches((n > 1 ? 1 : 0) + 1);
+    add_launches((n > 1 && nodes ? 1 : 0) + 1);
     return CPT_OK;
 }
 
