@@ -82,6 +82,20 @@ __device__ __forceinline__ bool hit_leaf(const SceneView& s, int k, float3 o, fl
     return hit_light(s.lights[__float_as_int(r1.x)], o, d, 0.001f, tmax, t);
 }
 
+// Inverse direction for slab tests.  A zero component (an axis-parallel ray, e.g. a cosine
+// sample with r1 = 1 from a floor) would make 1/d infinite and turn slab distances into NaN,
+// which the min/max chain then drops: boxes are wrongly accepted or rejected.  Components
+// below 1e-20 in magnitude are replaced by +-1e-20 (the limit of a nearly parallel ray); the
+// primitive tests keep the exact direction.
+__device__ __forceinline__ float3 safe_inverse(float3 d)
+{
+    const float e = 1e-20f;
+    float x = fabsf(d.x) < e ? copysignf(e, d.x) : d.x;
+    float y = fabsf(d.y) < e ? copysignf(e, d.y) : d.y;
+    float z = fabsf(d.z) < e ? copysignf(e, d.z) : d.z;
+    return f3(1.0f / x, 1.0f / y, 1.0f / z);
+}
+
 __device__ __forceinline__ uint32_t word_of(const float4& f, int w)
 {
     return __float_as_uint(w == 0 ? f.x : (w == 1 ? f.y : (w == 2 ? f.z : f.w)));
@@ -98,7 +112,7 @@ __device__ __forceinline__ uint32_t word_of(const float4& f, int w)
 __device__ __forceinline__ bool trace_closest_wide(const SceneView& s, float3 o, float3 d, float tmin, float tmax,
                                                    Hit& hit, int* err)
 {
-    const float3 idir = f3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
+    const float3 idir = safe_inverse(d);
     const uint32_t first = 7u ^ ((d.x < 0.f ? 1u : 0u) | (d.y < 0.f ? 2u : 0u) | (d.z < 0.f ? 4u : 0u));
     float best = tmax;
     uint64_t stack[CPT_WSTACK];
@@ -178,7 +192,7 @@ __device__ __forceinline__ bool trace_closest_wide(const SceneView& s, float3 o,
 __device__ __forceinline__ bool trace_closest_bvh2(const SceneView& s, float3 o, float3 d, float tmin, float tmax,
                                                    Hit& hit, int* err)
 {
-    const float3 idir = f3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
+    const float3 idir = safe_inverse(d);
     const float3 ood = f3(o.x * idir.x, o.y * idir.y, o.z * idir.z);
     int stack[CPT_STACK];
     int sp = 0;
