@@ -195,7 +195,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--spp", type=int, default=0, help="override the workload's spp (profiling captures)")
     ap.add_argument("--e2e-steps", type=int, default=2, help="steps of the end-to-end leg (0: skip)")
-    ap.add_argument("--bvh-width", type=int, default=8, choices=[2, 8], help="traversal layout")
+    ap.add_argument("--bvh-width", type=int, default=2, choices=[2, 8], help="traversal layout")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference_arm(args)

@@ -326,9 +326,9 @@ cpt_status create_scene(cpt_context* ctx, const cpt_scene_desc* d, cpt_scene** o
     s->scratch_bytes = lbvh_scratch_bytes(n);
     CPT_TRY(dalloc((char**)&s->scratch, s->scratch_bytes));
     CPT_TRY(dalloc(&s->ray_counter, 1));
-    CPT_TRY(dalloc(&s->err, 1));
+    CPT_TRY(dalloc(&s->err, 2));   // [0] device error word, [1] work counter of batched traces
 #undef CPT_TRY
-    CPT_CUDA(cudaMemset(s->err, 0, sizeof(int)));
+    CPT_CUDA(cudaMemset(s->err, 0, 2 * sizeof(int)));
     *out = s;
     return CPT_OK;
 }
@@ -441,7 +441,7 @@ CPT_EXPORT cpt_status cpt_context_create(int device, cpt_context** out)
     c->wf.block_shade = 128;
     c->wf.use_graph = true;
     c->wf_grids_ready = false;
-    c->bvh_width = 8;
+    c->bvh_width = 2;   // the faster layout on GB300 in this build (see the measurement notes)
     CPT_CUDA(cudaStreamCreateWithFlags(&c->wf.capture_stream, cudaStreamNonBlocking));
     *out = c;
     return CPT_OK;

@@ -243,6 +243,126 @@ __device__ __forceinline__ bool trace_closest_bvh2(const SceneView& s, float3 o,
     return hit.leaf >= 0;
 }
 
+// ---------------------------------------------------------------- step-wise BVH2 traversal
+// One ray's traversal state, advanced one node per call, so that a warp can refill lanes whose
+// ray finished with new rays instead of waiting for its slowest lane (dynamic ray fetching,
+// Aila & Laine 2009).  The visit order and pruning are those of trace_closest_bvh2.
+struct Bvh2Walk {
+    float3 o, d, idir, ood;
+    float tmin, best;
+    int node, sp;
+    Hit hit;
+    int stack[CPT_STACK];
+
+    __device__ __forceinline__ void start(float3 o_, float3 d_, float tmin_, float tmax_)
+    {
+        o = o_;
+        d = d_;
+        idir = safe_inverse(d_);
+        ood = f3(o.x * idir.x, o.y * idir.y, o.z * idir.z);
+        tmin = tmin_;
+        best = tmax_;
+        node = 0;
+        sp = 0;
+        hit.leaf = -1;
+        hit.t = tmax_;
+        hit.u = hit.v = 0.f;
+    }
+
+    // Visits one node; returns true when the traversal has finished.
+    __device__ __forceinline__ bool step(const SceneView& s, int* err)
+    {
+        const float4* np = s.nodes + 4 * (size_t)node;
+        float4 n0 = ldg4(np), n1 = ldg4(np + 1), n2 = ldg4(np + 2), n3 = ldg4(np + 3);
+        float ax0 = fmaf(n0.x, idir.x, -ood.x), ax1 = fmaf(n0.y, idir.x, -ood.x);
+        float ay0 = fmaf(n0.z, idir.y, -ood.y), ay1 = fmaf(n0.w, idir.y, -ood.y);
+        float az0 = fmaf(n2.x, idir.z, -ood.z), az1 = fmaf(n2.y, idir.z, -ood.z);
+        float an = fmaxf(fmaxf(fminf(ax0, ax1), fminf(ay0, ay1)), fmaxf(fminf(az0, az1), tmin));
+        float af = fminf(fminf(fmaxf(ax0, ax1), fmaxf(ay0, ay1)), fminf(fmaxf(az0, az1), best));
+        float bx0 = fmaf(n1.x, idir.x, -ood.x), bx1 = fmaf(n1.y, idir.x, -ood.x);
+        float by0 = fmaf(n1.z, idir.y, -ood.y), by1 = fmaf(n1.w, idir.y, -ood.y);
+        float bz0 = fmaf(n2.z, idir.z, -ood.z), bz1 = fmaf(n2.w, idir.z, -ood.z);
+        float bn = fmaxf(fmaxf(fminf(bx0, bx1), fminf(by0, by1)), fmaxf(fminf(bz0, bz1), tmin));
+        float bf = fminf(fminf(fmaxf(bx0, bx1), fmaxf(by0, by1)), fminf(fmaxf(bz0, bz1), best));
+        int ca = __float_as_int(n3.x), cb = __float_as_int(n3.y);
+        bool ha = an <= af, hb = bn <= bf;
+        float t, u, v;
+        if (ha && ca < 0 && hit_leaf(s, ~ca, o, d, best, t, u, v)) {
+            best = t; hit.t = t; hit.u = u; hit.v = v; hit.leaf = ~ca;
+        }
+        if (hb && cb < 0 && hit_leaf(s, ~cb, o, d, best, t, u, v)) {
+            best = t; hit.t = t; hit.u = u; hit.v = v; hit.leaf = ~cb;
+        }
+        bool ta = ha && ca >= 0, tb = hb && cb >= 0;
+        if (ta && tb) {
+            bool anear = an <= bn;
+            if (sp >= CPT_STACK) {
+                if (err) atomicOr(err, CPT_DEVERR_STACK);
+                return true;
+            }
+            stack[sp++] = anear ? cb : ca;
+            node = anear ? ca : cb;
+        } else if (ta) {
+            node = ca;
+        } else if (tb) {
+            node = cb;
+        } else {
+            if (sp == 0) return true;
+            node = stack[--sp];
+        }
+        return false;
+    }
+};
+
+__device__ __forceinline__ uint32_t lane_mask_lt()
+{
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// Traces work items [0, n) through the BVH2 with dynamic fetching: every loop trip each busy lane
+// advances its ray by one node, and idle lanes take the next items from *fetch (one atomic per
+// warp).  load(i, o, d, tmin, tmax) supplies item i's ray, store(i, hit) takes its result.  All
+// 32 lanes of every warp must call this together.  Returns the number of rays traced by the lane.
+template <typename Load, typename Store>
+__device__ __forceinline__ uint32_t trace_items_bvh2(const SceneView& s, int n, int* fetch, int* err, Load load,
+                                                     Store store)
+{
+    const int lane = threadIdx.x & 31;
+    Bvh2Walk w;
+    int item = -1;
+    bool exhausted = false;
+    uint32_t rays = 0;
+    for (;;) {
+        const bool idle = item < 0;
+        const uint32_t m = __ballot_sync(0xffffffffu, idle);
+        if (m && !exhausted) {
+            int base = 0;
+            if (lane == 0) base = atomicAdd(fetch, __popc(m));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (base + __popc(m) >= n) exhausted = true;
+            if (idle) {
+                const int r = base + __popc(m & lane_mask_lt());
+                if (r < n) {
+                    float3 o, d;
+                    float tmn, tmx;
+                    load(r, o, d, tmn, tmx);
+                    w.start(o, d, tmn, tmx);
+                    item = r;
+                    rays++;
+                }
+            }
+        }
+        if (__all_sync(0xffffffffu, item < 0)) break;
+        if (item >= 0 && w.step(s, err)) {
+            store(item, w.hit);
+            item = -1;
+        }
+    }
+    return rays;
+}
+
 // Closest hit over [tmin (boxes), tmax]; false on a miss.  WIDE selects the traversal layout at
 // compile time (each kernel is instantiated for the layout the scene was built with), so a
 // kernel carries the registers and code of one traversal only.  *err gets CPT_DEVERR_STACK if a

@@ -21,6 +21,26 @@ __global__ void k_trace(SceneView s, const float4* __restrict__ rays, uint64_t n
     hits[i] = make_float4(hit ? h.t : -1.0f, __int_as_float(prim), h.u, h.v);
 }
 
+// Persistent BVH2 variant: warps fetch rays dynamically (trace_items_bvh2), so lanes whose ray
+// finished take new rays instead of idling until the warp's slowest ray is done.
+__global__ void __launch_bounds__(128) k_trace_dyn(SceneView s, const float4* __restrict__ rays, int n,
+                                                   float4* __restrict__ hits, int* err, int* fetch)
+{
+    trace_items_bvh2(
+        s, n, fetch, err,
+        [&](int i, float3& o, float3& d, float& tmn, float& tmx) {
+            float4 a = __ldg(rays + 2 * (size_t)i), b = __ldg(rays + 2 * (size_t)i + 1);
+            o = f3(a.x, a.y, a.z);
+            d = f3(b.x, b.y, b.z);
+            tmn = a.w;
+            tmx = b.w;
+        },
+        [&](int i, const Hit& h) {
+            int prim = h.leaf >= 0 ? __float_as_int(ldg4(s.leaf_rec + 3 * (size_t)h.leaf).w) : -1;
+            hits[i] = make_float4(h.leaf >= 0 ? h.t : -1.0f, __int_as_float(prim), h.u, h.v);
+        });
+}
+
 }  // namespace
 
 cpt_status launch_trace(const SceneView& view, const cpt_ray* rays, uint64_t n, cpt_hit* hits, int* d_err,
@@ -32,7 +52,16 @@ cpt_status launch_trace(const SceneView& view, const cpt_ray* rays, uint64_t n, 
     const unsigned T = 128;
     uint64_t blocks = (n + T - 1) / T;
     if (blocks > 0x7fffffffull) return fail(CPT_ERR_INVALID_ARGUMENT, "cpt_trace_closest: too many rays");
-    if (view.wide)
+    if (!view.wide && view.n_internal > 0 && n < 0x7fffffffull) {
+        int dev = 0, sms = 0, per_sm = 0;
+        CPT_CUDA(cudaGetDevice(&dev));
+        CPT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        CPT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_dyn, T, 0));
+        int* fetch = d_err + 1;   // the scene's work counter
+        CPT_CUDA(cudaMemsetAsync(fetch, 0, sizeof(int), stream));
+        k_trace_dyn<<<std::max(1, per_sm) * sms, T, 0, stream>>>(view, (const float4*)rays, (int)n, (float4*)hits,
+                                                                 d_err, fetch);
+    } else if (view.wide)
         k_trace<true><<<(unsigned)blocks, T, 0, stream>>>(view, (const float4*)rays, n, (float4*)hits, d_err);
     else
         k_trace<false><<<(unsigned)blocks, T, 0, stream>>>(view, (const float4*)rays, n, (float4*)hits, d_err);

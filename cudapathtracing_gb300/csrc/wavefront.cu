@@ -172,6 +172,7 @@ __global__ void k_wf_init(SceneView s, Wf w, RenderArgs a)
         w.cnt[0] = w.M;
         w.cnt[1] = w.cnt[2] = w.cnt[3] = w.cnt[4] = w.cnt[5] = 0;
         w.cnt[6] = w.first_pix + w.M;
+        w.cnt[8] = w.cnt[9] = w.cnt[10] = w.cnt[11] = 0;
     }
     Pcg32 rng;
     rng.init(a.seed, (uint64_t)p);
@@ -195,16 +196,33 @@ __global__ void __launch_bounds__(256) k_wf_trace(SceneView s, Wf w, int par)
         w.cnt[nq] = 0;
         w.cnt[2 + nq] = 0;
         w.cnt[4 + nq] = 0;
+        w.cnt[8 + 2 * nq] = 0;   // fetch counters of the next iteration's trace and shadow kernels
+        w.cnt[9 + 2 * nq] = 0;
     }
     const int* q = w.q + (size_t)par * w.M;
     uint32_t rays = 0;
-    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
-        int slot = q[idx];
-        float4 o = w.o[slot], d = w.d[slot];
-        Hit h;
-        bool hit = trace_closest<WIDE>(s,xyz(o), xyz(d), 0.001f, CPT_INF_F, h, w.err);
-        w.hit[slot] = make_float4(h.t, __int_as_float(hit ? h.leaf : -1), h.u, h.v);
-        rays++;
+    if (!WIDE && s.n_internal > 0) {
+        rays = trace_items_bvh2(
+            s, n, &w.cnt[8 + 2 * par], w.err,
+            [&](int i, float3& o, float3& d, float& tmn, float& tmx) {
+                int slot = q[i];
+                o = xyz(w.o[slot]);
+                d = xyz(w.d[slot]);
+                tmn = 0.001f;
+                tmx = CPT_INF_F;
+            },
+            [&](int i, const Hit& h) {
+                w.hit[q[i]] = make_float4(h.t, __int_as_float(h.leaf), h.u, h.v);
+            });
+    } else {
+        for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
+            int slot = q[idx];
+            float4 o = w.o[slot], d = w.d[slot];
+            Hit h;
+            bool hit = trace_closest<WIDE>(s, xyz(o), xyz(d), 0.001f, CPT_INF_F, h, w.err);
+            w.hit[slot] = make_float4(h.t, __int_as_float(hit ? h.leaf : -1), h.u, h.v);
+            rays++;
+        }
     }
     count_rays(w.rays, rays);
 }
@@ -215,14 +233,31 @@ __global__ void __launch_bounds__(256) k_wf_shadow(SceneView s, Wf w, int par)
     const int n = w.cnt[4 + par];
     const int* sq = w.sq + (size_t)par * w.M * w.L;
     uint32_t rays = 0;
-    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
-        int e = sq[idx];
-        int k = e % w.L;
-        Hit h;
-        bool hit = trace_closest<WIDE>(s,xyz(w.so[e]), xyz(w.sd[e]), 0.001f, CPT_INF_F, h, w.err);
-        int obst = hit ? __float_as_int(ldg4(s.leaf_rec + 3 * (size_t)h.leaf).w) : -1;
-        w.svis[e] = obst == k ? 1 : 0;
-        rays++;
+    if (!WIDE && s.n_internal > 0) {
+        rays = trace_items_bvh2(
+            s, n, &w.cnt[9 + 2 * par], w.err,
+            [&](int i, float3& o, float3& d, float& tmn, float& tmx) {
+                int e = sq[i];
+                o = xyz(w.so[e]);
+                d = xyz(w.sd[e]);
+                tmn = 0.001f;
+                tmx = CPT_INF_F;
+            },
+            [&](int i, const Hit& h) {
+                int e = sq[i];
+                int obst = h.leaf >= 0 ? __float_as_int(ldg4(s.leaf_rec + 3 * (size_t)h.leaf).w) : -1;
+                w.svis[e] = obst == e % w.L ? 1 : 0;
+            });
+    } else {
+        for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
+            int e = sq[idx];
+            int k = e % w.L;
+            Hit h;
+            bool hit = trace_closest<WIDE>(s, xyz(w.so[e]), xyz(w.sd[e]), 0.001f, CPT_INF_F, h, w.err);
+            int obst = hit ? __float_as_int(ldg4(s.leaf_rec + 3 * (size_t)h.leaf).w) : -1;
+            w.svis[e] = obst == k ? 1 : 0;
+            rays++;
+        }
     }
     count_rays(w.rays, rays);
 }

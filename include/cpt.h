@@ -214,8 +214,9 @@ cpt_status cpt_context_set_render_block(cpt_context* ctx, int block_x, int block
  * sizes of the trace and shade kernels (multiples of 32), and whether iterations are replayed
  * from a captured CUDA graph.  Defaults: 1,048,576 slots, 128, 128, graphs on. */
 cpt_status cpt_context_set_wavefront(cpt_context* ctx, int slots, int block_trace, int block_shade, int use_graph);
-/* Traversal layout built by later cpt_lbvh_build / cpt_lbvh_refit calls: 8 = the compressed
- * 8-wide BVH (80-byte nodes, 8-bit quantised child boxes; the default), 2 = binary nodes. */
+/* Traversal layout built by later cpt_lbvh_build / cpt_lbvh_refit calls: 2 = binary nodes with
+ * both child boxes per 64-byte node (the default), 8 = the compressed 8-wide BVH (96-byte nodes,
+ * 8-bit quantised child boxes, direction-ordered slots). */
 cpt_status cpt_context_set_bvh_width(cpt_context* ctx, int width);
 
 /* ---- scene files (host only, no GPU needed) ------------------------------------------ */

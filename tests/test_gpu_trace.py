@@ -59,7 +59,28 @@ def check_t(gpu, ref_ids, ref_t):
 def width(request, ctx):
     ctx.set_bvh_width(request.param)
     yield request.param
-    ctx.set_bvh_width(8)
+    ctx.set_bvh_width(2)
+
+
+def test_axis_parallel_rays(ctx, oracle_mod, width):
+    """Directions with exact zero components (e.g. a cosine sample with r1 = 1 on a floor)
+    must traverse correctly and quickly: infinite inverse components are clamped."""
+    d = scenes.by_name("mixed")
+    s = api.Scene(ctx, d).init()
+    g = P.PCG32Streams(5, np.arange(600, dtype=np.uint64))
+    org = np.stack([g.uniform() * 6 - 3 for _ in range(3)], 1)
+    rays = np.zeros(3600, abi.RAY_DTYPE)
+    for k, dirv in enumerate([(1, 0, 0), (-1, 0, 0), (0, 1, 0), (0, -1, 0), (0, 0, 1), (0, 0, -1)]):
+        rays["origin"][k * 600:(k + 1) * 600] = org
+        rays["direction"][k * 600:(k + 1) * 600] = dirv
+    rays["tmin"] = 0.001
+    rays["tmax"] = 999999.0
+    gpu = s.trace(rays)
+    o = oracle_mod.OracleScene(d)
+    ids, t, _, _ = o.trace(P.rays_as_f64(rays))
+    nbad, unexplained = classify(o, rays, gpu, ids, t)
+    assert not unexplained, (nbad, unexplained[:10])
+    assert (gpu["prim"] >= 0).mean() > 0.05
 
 
 @pytest.mark.parametrize("name,seed,box", [("ico3", 1, 2.0), ("mixed", 3, 3.0)])
