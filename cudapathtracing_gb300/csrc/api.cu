@@ -441,8 +441,11 @@ CPT_EXPORT cpt_status cpt_context_create(int device, cpt_context** out)
     c->wf.block_shade = 128;
     c->wf.use_graph = true;
     c->wf_grids_ready = false;
-    c->bvh_width = 2;   // the faster layout on GB300 in this build (see the measurement notes)
+    c->bvh_width = 2;   // the faster of the two layouts as measured on GB300
     CPT_CUDA(cudaStreamCreateWithFlags(&c->wf.capture_stream, cudaStreamNonBlocking));
+    CPT_CUDA(cudaStreamCreateWithFlags(&c->wf.side_stream, cudaStreamNonBlocking));
+    CPT_CUDA(cudaEventCreateWithFlags(&c->wf.fork, cudaEventDisableTiming));
+    CPT_CUDA(cudaEventCreateWithFlags(&c->wf.join, cudaEventDisableTiming));
     *out = c;
     return CPT_OK;
 }
@@ -450,6 +453,9 @@ CPT_EXPORT cpt_status cpt_context_create(int device, cpt_context** out)
 CPT_EXPORT cpt_status cpt_context_destroy(cpt_context* ctx)
 {
     if (ctx && ctx->wf.capture_stream) cudaStreamDestroy(ctx->wf.capture_stream);
+    if (ctx && ctx->wf.side_stream) cudaStreamDestroy(ctx->wf.side_stream);
+    if (ctx && ctx->wf.fork) cudaEventDestroy(ctx->wf.fork);
+    if (ctx && ctx->wf.join) cudaEventDestroy(ctx->wf.join);
     delete ctx;
     return CPT_OK;
 }
@@ -458,9 +464,10 @@ CPT_EXPORT cpt_status cpt_context_destroy(cpt_context* ctx)
 CPT_EXPORT cpt_status cpt_context_set_wavefront(cpt_context* ctx, int slots, int block_trace, int block_shade,
                                                 int use_graph)
 {
-    auto ok_block = [](int b) { return b >= 32 && b <= 1024 && b % 32 == 0; };
-    if (!ctx || slots < 1024 || !ok_block(block_trace) || !ok_block(block_shade))
-        return fail(CPT_ERR_INVALID_ARGUMENT, "wavefront: slots >= 1024, blocks multiples of 32 in [32, 1024]");
+    auto ok_block = [](int b, int hi) { return b >= 32 && b <= hi && b % 32 == 0; };
+    if (!ctx || slots < 1024 || !ok_block(block_trace, 512) || !ok_block(block_shade, 1024))
+        return fail(CPT_ERR_INVALID_ARGUMENT,
+                    "wavefront: slots >= 1024, blocks multiples of 32 (trace <= 512, shade <= 1024)");
     ctx->wf.slots = slots;
     ctx->wf.block_trace = block_trace;
     ctx->wf.block_shade = block_shade;
@@ -479,8 +486,8 @@ CPT_EXPORT cpt_status cpt_context_set_bvh_width(cpt_context* ctx, int width)
 // Internal tuning knob (the autotuner's setter): render block shape.
 CPT_EXPORT cpt_status cpt_context_set_render_block(cpt_context* ctx, int bx, int by)
 {
-    if (!ctx || bx <= 0 || by <= 0 || (bx * by) % 32 || bx * by > 1024)
-        return fail(CPT_ERR_INVALID_ARGUMENT, "render block must be a positive multiple of 32 threads, <= 1024");
+    if (!ctx || bx <= 0 || by <= 0 || (bx * by) % 32 || bx * by > 512)   // short stacks: <= 32 KB shared
+        return fail(CPT_ERR_INVALID_ARGUMENT, "render block must be a positive multiple of 32 threads, <= 512");
     ctx->render_block_x = bx;
     ctx->render_block_y = by;
     return CPT_OK;

@@ -80,6 +80,35 @@ struct SceneView {
 };
 
 // ------------------------------------------------------------------ PCG32
+// Config estimator: sample k of a pixel draws from the pixel's PCG32 stream started k * 2^32
+// draws ahead (no sample draws 2^32 numbers), so the samples of one pixel are independent and
+// an integrator may run them in any order or in parallel.  Sample radiance is summed in groups
+// of sample_group(spp) consecutive samples and the group sums are added in group order, which
+// fixes the FP32 summation order for every integrator.
+constexpr uint64_t CPT_PCG_MULT = 6364136223846793005ULL;
+
+// The LCG step x -> a x + c applied 2^n times is x -> A x + c P; jump_mult(n) = A and
+// jump_plus(n) = P (Brown 1994, "Random number generation with arbitrary strides").
+constexpr uint64_t pcg_jump_mult(int n)
+{
+    uint64_t m = CPT_PCG_MULT;
+    for (int i = 0; i < n; ++i) m *= m;
+    return m;
+}
+constexpr uint64_t pcg_jump_plus(int n)
+{
+    uint64_t m = CPT_PCG_MULT, p = 1;
+    for (int i = 0; i < n; ++i) {
+        p *= m + 1;
+        m *= m;
+    }
+    return p;
+}
+constexpr uint64_t CPT_PCG_JUMP32_MULT = pcg_jump_mult(32);
+constexpr uint64_t CPT_PCG_JUMP32_PLUS = pcg_jump_plus(32);
+
+__host__ __device__ __forceinline__ int sample_group(int spp) { return spp <= 256 ? 8 : (spp + 31) / 32; }
+
 #ifdef __CUDACC__
 // PCG32 (O'Neill 2014, pcg32_srandom_r / pcg32_random_r); uniforms are (x + 1) * 2^-32 in
 // (0, 1], rounded once to FP32, the stand-in for curand_uniform_double (Render.cu:43).
@@ -88,7 +117,7 @@ struct Pcg32 {
     __device__ __forceinline__ uint32_t next()
     {
         uint64_t old = state;
-        state = old * 6364136223846793005ULL + inc;
+        state = old * CPT_PCG_MULT + inc;
         uint32_t xs = (uint32_t)(((old >> 18u) ^ old) >> 27u);
         uint32_t rot = (uint32_t)(old >> 59u);
         return __funnelshift_r(xs, xs, rot);
@@ -101,9 +130,62 @@ struct Pcg32 {
         state += seed;
         next();
     }
+    // Moves the generator k * 2^32 draws ahead in O(log k) steps.
+    __device__ __forceinline__ void jump_samples(uint32_t k)
+    {
+        uint64_t cm = CPT_PCG_JUMP32_MULT, cp = CPT_PCG_JUMP32_PLUS * inc, am = 1, ap = 0;
+        while (k) {
+            if (k & 1u) {
+                am *= cm;
+                ap = ap * cm + cp;
+            }
+            cp *= cm + 1;
+            cm *= cm;
+            k >>= 1;
+        }
+        state = am * state + ap;
+    }
+    // Generator of sample k of the pixel with stream `stream` (config estimator).
+    __device__ __forceinline__ void init_sample(uint64_t seed, uint64_t stream, uint32_t k)
+    {
+        init(seed, stream);
+        jump_samples(k);
+    }
     __device__ __forceinline__ float uniform() { return __ull2float_rn((uint64_t)next() + 1ull) * 2.3283064365386963e-10f; }
     // 1 - uniform(), computed from the integer so it is not lost to cancellation near 1.
     __device__ __forceinline__ float one_minus_uniform_from(uint32_t x) { return __uint2float_rn(~x) * 2.3283064365386963e-10f; }
+};
+#endif
+
+// ------------------------------------------------------------------ traversal stack
+// The binary traversal keeps the bottom CPT_SHORT_STACK entries of its stack in shared memory
+// and the rest in local memory.  Every kernel that traverses the BVH2 is launched with
+// short_stack_bytes(threads per block) of dynamic shared memory; thread t owns the column
+// t, t + T, t + 2T, ... (T = threads per block), so a warp's pushes and pops hit 32 distinct banks.
+#define CPT_SHORT_STACK 16
+inline constexpr size_t short_stack_bytes(int threads) { return (size_t)CPT_SHORT_STACK * threads * sizeof(int); }
+
+#ifdef __CUDACC__
+struct ShortStack {
+    int* col;     // this thread's column in the block's dynamic shared array
+    int stride;   // threads per block
+    int spill[CPT_STACK - CPT_SHORT_STACK];
+    __device__ __forceinline__ void init()
+    {
+        extern __shared__ int cpt_short_stack_smem[];
+        const int t = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+        col = cpt_short_stack_smem + t;
+        stride = blockDim.x * blockDim.y * blockDim.z;
+    }
+    __device__ __forceinline__ void put(int i, int v)
+    {
+        if (i < CPT_SHORT_STACK) col[i * stride] = v;
+        else spill[i - CPT_SHORT_STACK] = v;
+    }
+    __device__ __forceinline__ int get(int i) const
+    {
+        return i < CPT_SHORT_STACK ? col[i * stride] : spill[i - CPT_SHORT_STACK];
+    }
 };
 #endif
 

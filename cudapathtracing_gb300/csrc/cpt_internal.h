@@ -94,6 +94,8 @@ struct WavefrontTuning {
     int grid_shade, block_shade;
     bool use_graph;
     cudaStream_t capture_stream; // non-default stream used only to capture the iteration graph
+    cudaStream_t side_stream;    // second capture stream: shadow rays traced beside extension rays
+    cudaEvent_t fork, join;      // capture-time dependencies between the two streams
 };
 
 cpt_status launch_render_wavefront(const SceneView& view, const RenderArgs& args, cudaStream_t stream,

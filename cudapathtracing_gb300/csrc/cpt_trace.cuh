@@ -82,6 +82,42 @@ __device__ __forceinline__ bool hit_leaf(const SceneView& s, int k, float3 o, fl
     return hit_light(s.lights[__float_as_int(r1.x)], o, d, 0.001f, tmax, t);
 }
 
+// Occlusion test of leaf k for a shadow ray aimed at light `skip`: any primitive hit in
+// [0.001, tmax] occludes, except that light itself.
+__device__ __forceinline__ bool occludes_leaf(const SceneView& s, int k, float3 o, float3 d, float tmax, int skip)
+{
+    const float4* r = s.leaf_rec + 3 * (size_t)k;
+    float4 r0 = ldg4(r), r1 = ldg4(r + 1);
+    int kind = __float_as_int(r1.w);
+    float t, u, v;
+    if (kind == CPT_KIND_TRI) {
+        float4 r2 = ldg4(r + 2);
+        return hit_triangle(o, d, f3(r0.x, r0.y, r0.z), f3(r1.x, r1.y, r1.z), f3(r2.x, r2.y, r2.z), 0.001f, tmax, t, u,
+                            v);
+    }
+    if (kind == CPT_KIND_SPHERE) return hit_sphere(o, d, f3(r0.x, r0.y, r0.z), r1.x, 0.001f, tmax, t);
+    int li = __float_as_int(r1.x);
+    return li != skip && hit_light(s.lights[li], o, d, 0.001f, tmax, t);
+}
+
+// One leaf reached by a traversal.  Closest-hit queries (ANY false) keep the nearest hit in
+// [0.001, best]; occlusion queries (ANY true) return true at the first occluder.
+template <bool ANY>
+__device__ __forceinline__ bool visit_leaf(const SceneView& s, int leaf, float3 o, float3 d, float& best, Hit& hit,
+                                           int skip)
+{
+    if (ANY) {
+        if (!occludes_leaf(s, leaf, o, d, best, skip)) return false;
+        hit.leaf = leaf;
+        return true;
+    }
+    float t, u, v;
+    if (hit_leaf(s, leaf, o, d, best, t, u, v)) {
+        best = t; hit.t = t; hit.u = u; hit.v = v; hit.leaf = leaf;
+    }
+    return false;
+}
+
 // Inverse direction for slab tests.  A zero component (an axis-parallel ray, e.g. a cosine
 // sample with r1 = 1 from a floor) would make 1/d infinite and turn slab distances into NaN,
 // which the min/max chain then drops: boxes are wrongly accepted or rejected.  Components
@@ -108,9 +144,11 @@ __device__ __forceinline__ uint32_t word_of(const float4& f, int w)
 // first (the reference tests leaves as it reaches them); the traversal continues with the first
 // internal child and keeps the rest as one node-group entry (first child index, internal-slot
 // mask, remaining hit bits) on the stack, as in compressed wide BVH traversal (Ylitie et al.
-// 2017).  Boxes are tested against the closest hit so far, so far subtrees are culled.
+// 2017).  Boxes are tested against the closest hit so far, so far subtrees are culled.  With ANY
+// the walk is an occlusion query (visit_leaf) that stops at the first occluder.
+template <bool ANY>
 __device__ __forceinline__ bool trace_closest_wide(const SceneView& s, float3 o, float3 d, float tmin, float tmax,
-                                                   Hit& hit, int* err)
+                                                   Hit& hit, int* err, int skip)
 {
     const float3 idir = safe_inverse(d);
     const uint32_t first = 7u ^ ((d.x < 0.f ? 1u : 0u) | (d.y < 0.f ? 2u : 0u) | (d.z < 0.f ? 4u : 0u));
@@ -151,10 +189,7 @@ __device__ __forceinline__ bool trace_closest_wide(const SceneView& s, float3 o,
             const uint32_t slot = (uint32_t)(__ffs(lhits) - 1) ^ first;
             lhits &= lhits - 1;
             const int leaf = ~(int)(slot < 4 ? word_of(f1, slot & 3) : word_of(f2, slot & 3));
-            float t, u, v;
-            if (hit_leaf(s, leaf, o, d, best, t, u, v)) {
-                best = t; hit.t = t; hit.u = u; hit.v = v; hit.leaf = leaf;
-            }
+            if (visit_leaf<ANY>(s, leaf, o, d, best, hit, skip)) return true;
         }
         // Continue with the first hit internal child; the others stay on the stack as one group
         // (this node, remaining hit bits) and are read back from the node when popped.
@@ -188,13 +223,16 @@ __device__ __forceinline__ bool trace_closest_wide(const SceneView& s, float3 o,
 }
 
 // Binary-node traversal (Aila–Laine node layout): near child first, far child pushed.  The
-// stack cannot overflow for Karras trees over 64-bit keys (at most 65 levels).
+// stack (ShortStack: shared memory, then local memory) holds at most one entry per level.  ANY as in
+// trace_closest_wide.
+template <bool ANY>
 __device__ __forceinline__ bool trace_closest_bvh2(const SceneView& s, float3 o, float3 d, float tmin, float tmax,
-                                                   Hit& hit, int* err)
+                                                   Hit& hit, int* err, int skip)
 {
     const float3 idir = safe_inverse(d);
     const float3 ood = f3(o.x * idir.x, o.y * idir.y, o.z * idir.z);
-    int stack[CPT_STACK];
+    ShortStack stack;
+    stack.init();
     int sp = 0;
     int node = 0;
     float best = tmax;
@@ -215,13 +253,8 @@ __device__ __forceinline__ bool trace_closest_bvh2(const SceneView& s, float3 o,
         float bf = fminf(fminf(fmaxf(bx0, bx1), fmaxf(by0, by1)), fminf(fmaxf(bz0, bz1), best));
         int ca = __float_as_int(n3.x), cb = __float_as_int(n3.y);
         bool ha = an <= af, hb = bn <= bf;
-        float t, u, v;
-        if (ha && ca < 0 && hit_leaf(s, ~ca, o, d, best, t, u, v)) {
-            best = t; hit.t = t; hit.u = u; hit.v = v; hit.leaf = ~ca;
-        }
-        if (hb && cb < 0 && hit_leaf(s, ~cb, o, d, best, t, u, v)) {
-            best = t; hit.t = t; hit.u = u; hit.v = v; hit.leaf = ~cb;
-        }
+        if (ha && ca < 0 && visit_leaf<ANY>(s, ~ca, o, d, best, hit, skip)) return true;
+        if (hb && cb < 0 && visit_leaf<ANY>(s, ~cb, o, d, best, hit, skip)) return true;
         bool ta = ha && ca >= 0, tb = hb && cb >= 0;
         if (ta && tb) {
             bool anear = an <= bn;
@@ -229,7 +262,7 @@ __device__ __forceinline__ bool trace_closest_bvh2(const SceneView& s, float3 o,
                 if (err) atomicOr(err, CPT_DEVERR_STACK);
                 break;
             }
-            stack[sp++] = anear ? cb : ca;
+            stack.put(sp++, anear ? cb : ca);
             node = anear ? ca : cb;
         } else if (ta) {
             node = ca;
@@ -237,7 +270,7 @@ __device__ __forceinline__ bool trace_closest_bvh2(const SceneView& s, float3 o,
             node = cb;
         } else {
             if (sp == 0) break;
-            node = stack[--sp];
+            node = stack.get(--sp);
         }
     }
     return hit.leaf >= 0;
@@ -247,14 +280,15 @@ __device__ __forceinline__ bool trace_closest_bvh2(const SceneView& s, float3 o,
 // One ray's traversal state, advanced one node per call, so that a warp can refill lanes whose
 // ray finished with new rays instead of waiting for its slowest lane (dynamic ray fetching,
 // Aila & Laine 2009).  The visit order and pruning are those of trace_closest_bvh2.
+template <bool ANY>
 struct Bvh2Walk {
     float3 o, d, idir, ood;
     float tmin, best;
-    int node, sp;
+    int node, sp, skip;
     Hit hit;
-    int stack[CPT_STACK];
+    ShortStack stack;   // init() once per kernel, before the first start()
 
-    __device__ __forceinline__ void start(float3 o_, float3 d_, float tmin_, float tmax_)
+    __device__ __forceinline__ void start(float3 o_, float3 d_, float tmin_, float tmax_, int skip_)
     {
         o = o_;
         d = d_;
@@ -264,6 +298,7 @@ struct Bvh2Walk {
         best = tmax_;
         node = 0;
         sp = 0;
+        skip = skip_;
         hit.leaf = -1;
         hit.t = tmax_;
         hit.u = hit.v = 0.f;
@@ -286,13 +321,8 @@ struct Bvh2Walk {
         float bf = fminf(fminf(fmaxf(bx0, bx1), fmaxf(by0, by1)), fminf(fmaxf(bz0, bz1), best));
         int ca = __float_as_int(n3.x), cb = __float_as_int(n3.y);
         bool ha = an <= af, hb = bn <= bf;
-        float t, u, v;
-        if (ha && ca < 0 && hit_leaf(s, ~ca, o, d, best, t, u, v)) {
-            best = t; hit.t = t; hit.u = u; hit.v = v; hit.leaf = ~ca;
-        }
-        if (hb && cb < 0 && hit_leaf(s, ~cb, o, d, best, t, u, v)) {
-            best = t; hit.t = t; hit.u = u; hit.v = v; hit.leaf = ~cb;
-        }
+        if (ha && ca < 0 && visit_leaf<ANY>(s, ~ca, o, d, best, hit, skip)) return true;
+        if (hb && cb < 0 && visit_leaf<ANY>(s, ~cb, o, d, best, hit, skip)) return true;
         bool ta = ha && ca >= 0, tb = hb && cb >= 0;
         if (ta && tb) {
             bool anear = an <= bn;
@@ -300,7 +330,7 @@ struct Bvh2Walk {
                 if (err) atomicOr(err, CPT_DEVERR_STACK);
                 return true;
             }
-            stack[sp++] = anear ? cb : ca;
+            stack.put(sp++, anear ? cb : ca);
             node = anear ? ca : cb;
         } else if (ta) {
             node = ca;
@@ -308,7 +338,7 @@ struct Bvh2Walk {
             node = cb;
         } else {
             if (sp == 0) return true;
-            node = stack[--sp];
+            node = stack.get(--sp);
         }
         return false;
     }
@@ -323,14 +353,16 @@ __device__ __forceinline__ uint32_t lane_mask_lt()
 
 // Traces work items [0, n) through the BVH2 with dynamic fetching: every loop trip each busy lane
 // advances its ray by one node, and idle lanes take the next items from *fetch (one atomic per
-// warp).  load(i, o, d, tmin, tmax) supplies item i's ray, store(i, hit) takes its result.  All
+// warp).  load(i, o, d, tmin, tmax, skip) supplies item i's ray (skip: the light an occlusion
+// query aims at), store(i, hit) takes its result (for ANY, hit.leaf >= 0 means occluded).  All
 // 32 lanes of every warp must call this together.  Returns the number of rays traced by the lane.
-template <typename Load, typename Store>
+template <bool ANY, typename Load, typename Store>
 __device__ __forceinline__ uint32_t trace_items_bvh2(const SceneView& s, int n, int* fetch, int* err, Load load,
                                                      Store store)
 {
     const int lane = threadIdx.x & 31;
-    Bvh2Walk w;
+    Bvh2Walk<ANY> w;
+    w.stack.init();
     int item = -1;
     bool exhausted = false;
     uint32_t rays = 0;
@@ -347,8 +379,9 @@ __device__ __forceinline__ uint32_t trace_items_bvh2(const SceneView& s, int n, 
                 if (r < n) {
                     float3 o, d;
                     float tmn, tmx;
-                    load(r, o, d, tmn, tmx);
-                    w.start(o, d, tmn, tmx);
+                    int skip = -1;
+                    load(r, o, d, tmn, tmx, skip);
+                    w.start(o, d, tmn, tmx, skip);
                     item = r;
                     rays++;
                 }
@@ -366,25 +399,34 @@ __device__ __forceinline__ uint32_t trace_items_bvh2(const SceneView& s, int n, 
 // Closest hit over [tmin (boxes), tmax]; false on a miss.  WIDE selects the traversal layout at
 // compile time (each kernel is instantiated for the layout the scene was built with), so a
 // kernel carries the registers and code of one traversal only.  *err gets CPT_DEVERR_STACK if a
-// fixed stack would overflow.
-template <bool WIDE>
+// fixed stack would overflow.  With ANY the query is an occlusion test (see occluded).
+template <bool WIDE, bool ANY = false>
 __device__ __forceinline__ bool trace_closest(const SceneView& s, float3 o, float3 d, float tmin, float tmax, Hit& hit,
-                                              int* err)
+                                              int* err, int skip = -1)
 {
     hit.leaf = -1;
     hit.t = tmax;
     hit.u = hit.v = 0.f;
     if (s.n_prims <= 0) return false;
     if (s.n_internal == 0) {
-        float t, u, v;
-        if (hit_leaf(s, 0, o, d, tmax, t, u, v)) {
-            hit.t = t; hit.u = u; hit.v = v; hit.leaf = 0;
-            return true;
-        }
-        return false;
+        float best = tmax;
+        visit_leaf<ANY>(s, 0, o, d, best, hit, skip);
+        return hit.leaf >= 0;
     }
-    if (WIDE) return trace_closest_wide(s, o, d, tmin, tmax, hit, err);
-    return trace_closest_bvh2(s, o, d, tmin, tmax, hit, err);
+    if (WIDE) return trace_closest_wide<ANY>(s, o, d, tmin, tmax, hit, err, skip);
+    return trace_closest_bvh2<ANY>(s, o, d, tmin, tmax, hit, err, skip);
+}
+
+// Visibility of light `light` along a shadow ray whose hit on that light is at t_light (from
+// hit_light with the same origin and direction).  The reference's test is "the closest hit is
+// that light" (Render.cu:178-181); except for exact ties in t it equals "nothing but that light is
+// hit in [0.001, t_light]", which this occlusion query answers and which stops at the first
+// occluder instead of searching for the closest one.
+template <bool WIDE>
+__device__ __forceinline__ bool occluded(const SceneView& s, float3 o, float3 d, float t_light, int light, int* err)
+{
+    Hit h;
+    return trace_closest<WIDE, true>(s, o, d, 0.001f, t_light, h, err, light);
 }
 
 }  // namespace cpt

@@ -5,7 +5,8 @@
 //     Opaque with pdf 1/(width*width), emission ignored after the first NEE, the sigma_maj = 25
 //     volume), with the same order of random draws so that paths match the FP64 oracle.
 //   estimator CONFIG: the config estimator (depth limit, RR from rr_depth on, Lambertian,
-//     per-material IOR, homogeneous media with sigma_t and albedo).
+//     per-material IOR, homogeneous media with sigma_t and albedo), with one PCG32 sub-stream
+//     per sample and group-wise sample sums (Pcg32::init_sample, sample_group).
 #include <cuda_runtime.h>
 
 #include "cpt_internal.h"
@@ -158,10 +159,12 @@ __device__ PixelResult pixel_config(const SceneView& s, int i, int j, const Rend
     out.gdepth = CPT_INF_F;
     out.galb = f3(0.f, 0.f, 0.f);
     const DevCamera& cam = s.cam;
-    Pcg32 rng;
-    rng.init(a.seed, (uint64_t)j * cam.width + i);
-    float3 pix = f3(0.f, 0.f, 0.f);
+    const uint64_t stream = (uint64_t)j * cam.width + i;
+    const int group = sample_group(a.spp);
+    float3 pix = f3(0.f, 0.f, 0.f), gsum = f3(0.f, 0.f, 0.f);
     for (int sample = 0; sample < a.spp; ++sample) {
+        Pcg32 rng;
+        rng.init_sample(a.seed, stream, (uint32_t)sample);
         float rx = rng.uniform();
         float ry = rng.uniform();
         float3 o = cam.look_from;
@@ -220,7 +223,7 @@ __device__ PixelResult pixel_config(const SceneView& s, int i, int j, const Rend
                 if (count_emission) rad = rad + thr * sf.color;
                 break;
             }
-            if (depth == 0 && out.gdepth >= CPT_INF_F) {
+            if (depth == 0 && sample < group && out.gdepth >= CPT_INF_F) {   // first surface hit of group 0
                 out.gn = sf.normal;
                 out.gdepth = sqrtf(len2(cam.look_from - sf.pos));
                 out.galb = sf.color;
@@ -236,11 +239,10 @@ __device__ PixelResult pixel_config(const SceneView& s, int i, int j, const Rend
                     float3 dir = unit3(lp - sf.pos);
                     float cs_ = dot3(dir, sf.normal), cl_ = dot3(-dir, L.normal);
                     if (!(cs_ > 0.f && cl_ > 0.f)) continue;   // cannot contribute: no shadow ray
-                    Hit lh2;
-                    trace_closest<WIDE>(s,sf.pos, dir, 0.001f, CPT_INF_F, lh2, a.err);
+                    float tl;
+                    if (!hit_light(L, sf.pos, dir, 0.001f, CPT_INF_F, tl)) continue;   // cannot see the light
                     out.rays++;
-                    int obst = prim_of(s, lh2);
-                    if (obst == k) {
+                    if (!occluded<WIDE>(s, sf.pos, dir, tl, k, a.err)) {
                         float3 fr = bsdf_eval(sf, d, dir);
                         float g = cs_ * cl_ / len2(lp - sf.pos) * area;
                         rad = rad + thr * (L.color * fr * g);
@@ -265,7 +267,11 @@ __device__ PixelResult pixel_config(const SceneView& s, int i, int j, const Rend
             o = sf.pos;
             d = dir;
         }
-        pix = pix + rad;
+        gsum = gsum + rad;
+        if ((sample + 1) % group == 0 || sample + 1 == a.spp) {
+            pix = pix + gsum;
+            gsum = f3(0.f, 0.f, 0.f);
+        }
     }
     out.rgb = pix / (float)a.spp;
     return out;
@@ -324,12 +330,14 @@ cpt_status launch_render_megakernel(const SceneView& view, const RenderArgs& arg
     dim3 block(bx, by);
     dim3 grid((view.cam.width + bx - 1) / bx, (rows + by - 1) / by);
     const bool wide = view.wide != nullptr;
+    if (bx * by > 512) return fail(CPT_ERR_INVALID_ARGUMENT, "render block: at most 512 threads");
+    const size_t smem = short_stack_bytes(bx * by);
     if (args.estimator == CPT_ESTIMATOR_REFERENCE) {
-        if (wide) k_render<0, true><<<grid, block, 0, stream>>>(view, args);
-        else k_render<0, false><<<grid, block, 0, stream>>>(view, args);
+        if (wide) k_render<0, true><<<grid, block, smem, stream>>>(view, args);
+        else k_render<0, false><<<grid, block, smem, stream>>>(view, args);
     } else {
-        if (wide) k_render<1, true><<<grid, block, 0, stream>>>(view, args);
-        else k_render<1, false><<<grid, block, 0, stream>>>(view, args);
+        if (wide) k_render<1, true><<<grid, block, smem, stream>>>(view, args);
+        else k_render<1, false><<<grid, block, smem, stream>>>(view, args);
     }
     CPT_CUDA(cudaGetLastError());
     add_launches(1);

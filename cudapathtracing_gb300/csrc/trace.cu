@@ -26,9 +26,9 @@ __global__ void k_trace(SceneView s, const float4* __restrict__ rays, uint64_t n
 __global__ void __launch_bounds__(128) k_trace_dyn(SceneView s, const float4* __restrict__ rays, int n,
                                                    float4* __restrict__ hits, int* err, int* fetch)
 {
-    trace_items_bvh2(
+    trace_items_bvh2<false>(
         s, n, fetch, err,
-        [&](int i, float3& o, float3& d, float& tmn, float& tmx) {
+        [&](int i, float3& o, float3& d, float& tmn, float& tmx, int&) {
             float4 a = __ldg(rays + 2 * (size_t)i), b = __ldg(rays + 2 * (size_t)i + 1);
             o = f3(a.x, a.y, a.z);
             d = f3(b.x, b.y, b.z);
@@ -50,21 +50,22 @@ cpt_status launch_trace(const SceneView& view, const cpt_ray* rays, uint64_t n, 
     if (((uintptr_t)rays & 15u) || ((uintptr_t)hits & 15u))
         return fail(CPT_ERR_INVALID_ARGUMENT, "cpt_trace_closest: rays and hits must be 16-byte aligned");
     const unsigned T = 128;
+    const size_t smem = short_stack_bytes(T);
     uint64_t blocks = (n + T - 1) / T;
     if (blocks > 0x7fffffffull) return fail(CPT_ERR_INVALID_ARGUMENT, "cpt_trace_closest: too many rays");
     if (!view.wide && view.n_internal > 0 && n < 0x7fffffffull) {
         int dev = 0, sms = 0, per_sm = 0;
         CPT_CUDA(cudaGetDevice(&dev));
         CPT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        CPT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_dyn, T, 0));
+        CPT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_dyn, T, smem));
         int* fetch = d_err + 1;   // the scene's work counter
         CPT_CUDA(cudaMemsetAsync(fetch, 0, sizeof(int), stream));
-        k_trace_dyn<<<std::max(1, per_sm) * sms, T, 0, stream>>>(view, (const float4*)rays, (int)n, (float4*)hits,
-                                                                 d_err, fetch);
+        k_trace_dyn<<<std::max(1, per_sm) * sms, T, smem, stream>>>(view, (const float4*)rays, (int)n, (float4*)hits,
+                                                                    d_err, fetch);
     } else if (view.wide)
-        k_trace<true><<<(unsigned)blocks, T, 0, stream>>>(view, (const float4*)rays, n, (float4*)hits, d_err);
+        k_trace<true><<<(unsigned)blocks, T, smem, stream>>>(view, (const float4*)rays, n, (float4*)hits, d_err);
     else
-        k_trace<false><<<(unsigned)blocks, T, 0, stream>>>(view, (const float4*)rays, n, (float4*)hits, d_err);
+        k_trace<false><<<(unsigned)blocks, T, smem, stream>>>(view, (const float4*)rays, n, (float4*)hits, d_err);
     CPT_CUDA(cudaGetLastError());
     add_launches(1);
     return CPT_OK;

@@ -1,14 +1,17 @@
 // wavefront.cu — the wavefront integrator (config estimator).
 //
-// Paths live in M slots (structure of arrays).  Each slot owns one pixel at a time and runs that
-// pixel's samples in sequence with the pixel's own PCG32 stream, drawing the same numbers in the
-// same order as the megakernel (render.cu, pixel_config), so both integrators compute the same
-// estimator.  One iteration is four persistent kernels over compacted queues:
+// Paths live in M slots (structure of arrays).  Work items are (pixel, sample group) pairs, group
+// major: each slot takes an item, runs that group's samples in sequence with the samples' own
+// PCG32 sub-streams (Pcg32::init_sample), drawing the same numbers in the same order as the
+// megakernel (render.cu, pixel_config), and stores the group sum; k_wf_finish adds a pixel's group
+// sums in group order.  Both integrators therefore compute the same estimator, and a pixel's groups
+// run in parallel, so the last iterations are not left to the slowest pixels' full sample counts.
+// One iteration is four persistent kernels over compacted queues:
 //
 //   k_wf_trace    closest hit of every queued extension ray            (queue Q_i)
-//   k_wf_shadow   closest hit of every queued next-event shadow ray     (queue S_i)
+//   k_wf_shadow   occlusion query of every queued next-event shadow ray (queue S_i)
 //   k_wf_resolve  slots whose last sample ended with shadow rays in flight: add the visible
-//                 light contributions, write the pixel, take the next pixel  (queue R_i)
+//                 light contributions, store the group sum, take the next item  (queue R_i)
 //   k_wf_shade    one path vertex per slot: add last iteration's visible light contributions,
 //                 then medium / miss / emission / NEE (appends to S_{i+1}) / Russian roulette /
 //                 BSDF sampling (appends to Q_{i+1}); a finished sample starts the next one
@@ -43,9 +46,9 @@ enum : uint32_t {
 };
 
 struct Wf {
-    int M, L, spp, first_pix, end_pix, W;
+    int M, L, first_pix, npix, S, n_items;
     int* pixel;
-    int* spp_done;
+    int* sample;            // index of the sample in flight (within the pixel)
     uint32_t* flags;
     int* depth;
     int* guard;
@@ -56,7 +59,8 @@ struct Wf {
     float4* thr;
     float4* rad;
     float4* radp;
-    float4* pix;
+    float4* pix;            // sum of the item's finished samples
+    float4* part;           // group sums, [group][pixel - first_pix]
     float2* med;
     float4* hit;
     int* q;                 // 2 * M
@@ -66,7 +70,7 @@ struct Wf {
     float4* sd;
     float4* sc;
     int* svis;
-    int* cnt;               // [0,1] Q sizes, [2,3] R sizes, [4,5] S sizes, [6] next pixel
+    int* cnt;               // [0,1] Q sizes, [2,3] R sizes, [4,5] S sizes, [6] next item
     unsigned long long* rays;
     int* err;
 };
@@ -103,12 +107,14 @@ __device__ __forceinline__ uint8_t to_u8(float x)
     return (uint8_t)(254.99f * c);
 }
 
-// New sample for slot s of pixel `pixel`: camera ray (two draws), fresh path state.
-__device__ __forceinline__ void start_sample(const SceneView& s, const Wf& w, int slot, int pixel, Pcg32& rng,
-                                             uint32_t& fl)
+// Sample k of pixel `pixel` in slot `slot`: its generator, camera ray (two draws), fresh path state.
+__device__ __forceinline__ void start_sample(const SceneView& s, const Wf& w, uint64_t seed, int slot, int pixel,
+                                             int k, Pcg32& rng, uint32_t& fl)
 {
     int W = s.cam.width;
     int i = pixel % W, j = pixel / W;
+    rng.init_sample(seed, (uint64_t)pixel, (uint32_t)k);
+    w.sample[slot] = k;
     float rx = rng.uniform();
     float ry = rng.uniform();
     w.o[slot] = w0(s.cam.look_from);
@@ -120,46 +126,44 @@ __device__ __forceinline__ void start_sample(const SceneView& s, const Wf& w, in
     fl = (fl & ~F_INM) | F_CE;
 }
 
-__device__ __forceinline__ void write_pixel(const SceneView& s, const Wf& w, const RenderArgs& a, int slot, int pixel,
-                                            uint32_t fl)
+// The item in the slot is done: store its group sum (and a miss G-buffer entry when no sample of
+// group 0 found a surface).
+__device__ __forceinline__ void finish_item(const Wf& w, const RenderArgs& a, int slot, int pixel, uint32_t fl)
 {
-    float3 p = xyz(w.pix[slot]) / (float)a.spp;
-    size_t off = (size_t)pixel;
-    if (a.flags & CPT_RENDER_ACCUMULATE) {
-        a.rgb[3 * off] += p.x;
-        a.rgb[3 * off + 1] += p.y;
-        a.rgb[3 * off + 2] += p.z;
-    } else {
-        a.rgb[3 * off] = p.x;
-        a.rgb[3 * off + 1] = p.y;
-        a.rgb[3 * off + 2] = p.z;
-    }
-    if (a.rgba8) reinterpret_cast<uchar4*>(a.rgba8)[off] = make_uchar4(to_u8(p.x), to_u8(p.y), to_u8(p.z), 255);
-    if (a.gbuf && !(fl & F_GBUF)) {
-        float4* g = reinterpret_cast<float4*>(a.gbuf) + 2 * off;
-        g[0] = make_float4(0.f, 0.f, 0.f, CPT_INF_F);
-        g[1] = make_float4(0.f, 0.f, 0.f, 0.f);
+    const int g = (w.sample[slot] - 1) / w.S;
+    const size_t off = (size_t)(pixel - w.first_pix);
+    w.part[(size_t)g * w.npix + off] = w.pix[slot];
+    if (g == 0 && a.gbuf && !(fl & F_GBUF)) {
+        float4* gb = reinterpret_cast<float4*>(a.gbuf) + 2 * (size_t)pixel;
+        gb[0] = make_float4(0.f, 0.f, 0.f, CPT_INF_F);
+        gb[1] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
 }
 
-// Takes the next unrendered pixel for the slot (or leaves it idle) and queues its first ray.
-__device__ __forceinline__ void next_pixel(const SceneView& s, const Wf& w, const RenderArgs& a, int slot, int nq)
+// Starts item `item` (group major) in the slot with its first sample.
+__device__ __forceinline__ void start_item(const SceneView& s, const Wf& w, const RenderArgs& a, int slot, int item)
 {
-    int p = atomicAdd(&w.cnt[6], 1);
-    if (p >= w.end_pix) {
+    const int g = item / w.npix;
+    const int p = w.first_pix + (item - g * w.npix);
+    uint32_t fl = g == 0 ? 0u : F_GBUF;   // only group 0 writes the G-buffer
+    Pcg32 rng;
+    w.pixel[slot] = p;
+    w.pix[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
+    w.nee[slot] = 0;
+    start_sample(s, w, a.seed, slot, p, g * w.S, rng, fl);
+    w.flags[slot] = fl;
+    w.rng[slot] = rng.state;
+}
+
+// Takes the next item for the slot (or leaves it idle) and queues its first ray.
+__device__ __forceinline__ void next_item(const SceneView& s, const Wf& w, const RenderArgs& a, int slot, int nq)
+{
+    int item = atomicAdd(&w.cnt[6], 1);
+    if (item >= w.n_items) {
         w.pixel[slot] = -1;
         return;
     }
-    Pcg32 rng;
-    rng.init(a.seed, (uint64_t)p);
-    uint32_t fl = 0;
-    w.pixel[slot] = p;
-    w.spp_done[slot] = 0;
-    w.pix[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
-    w.nee[slot] = 0;
-    start_sample(s, w, slot, p, rng, fl);
-    w.flags[slot] = fl;
-    w.rng[slot] = rng.state;
+    start_item(s, w, a, slot, item);
     append(w.q + (size_t)nq * w.M, &w.cnt[nq], slot);
 }
 
@@ -167,24 +171,35 @@ __global__ void k_wf_init(SceneView s, Wf w, RenderArgs a)
 {
     int slot = blockIdx.x * blockDim.x + threadIdx.x;
     if (slot >= w.M) return;
-    int p = w.first_pix + slot;
     if (slot == 0) {
         w.cnt[0] = w.M;
         w.cnt[1] = w.cnt[2] = w.cnt[3] = w.cnt[4] = w.cnt[5] = 0;
-        w.cnt[6] = w.first_pix + w.M;
+        w.cnt[6] = w.M;
         w.cnt[8] = w.cnt[9] = w.cnt[10] = w.cnt[11] = 0;
     }
-    Pcg32 rng;
-    rng.init(a.seed, (uint64_t)p);
-    uint32_t fl = 0;
-    w.pixel[slot] = p;
-    w.spp_done[slot] = 0;
-    w.pix[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
-    w.nee[slot] = 0;
-    start_sample(s, w, slot, p, rng, fl);
-    w.flags[slot] = fl;
-    w.rng[slot] = rng.state;
-    w.q[slot] = slot;   // Q_0 holds every slot in order; its size is set by the host
+    start_item(s, w, a, slot, slot);
+    w.q[slot] = slot;   // Q_0 holds every slot in order
+}
+
+// Pixel = (sum of its group sums in group order) / spp, as the megakernel adds them.
+__global__ void k_wf_finish(Wf w, RenderArgs a, int groups)
+{
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= w.npix) return;
+    float3 sum = f3(0.f, 0.f, 0.f);
+    for (int g = 0; g < groups; ++g) sum = sum + xyz(w.part[(size_t)g * w.npix + p]);
+    float3 v = sum / (float)a.spp;
+    size_t off = (size_t)(w.first_pix + p);
+    if (a.flags & CPT_RENDER_ACCUMULATE) {
+        a.rgb[3 * off] += v.x;
+        a.rgb[3 * off + 1] += v.y;
+        a.rgb[3 * off + 2] += v.z;
+    } else {
+        a.rgb[3 * off] = v.x;
+        a.rgb[3 * off + 1] = v.y;
+        a.rgb[3 * off + 2] = v.z;
+    }
+    if (a.rgba8) reinterpret_cast<uchar4*>(a.rgba8)[off] = make_uchar4(to_u8(v.x), to_u8(v.y), to_u8(v.z), 255);
 }
 
 template <bool WIDE>
@@ -202,9 +217,9 @@ __global__ void __launch_bounds__(256) k_wf_trace(SceneView s, Wf w, int par)
     const int* q = w.q + (size_t)par * w.M;
     uint32_t rays = 0;
     if (!WIDE && s.n_internal > 0) {
-        rays = trace_items_bvh2(
+        rays = trace_items_bvh2<false>(
             s, n, &w.cnt[8 + 2 * par], w.err,
-            [&](int i, float3& o, float3& d, float& tmn, float& tmx) {
+            [&](int i, float3& o, float3& d, float& tmn, float& tmx, int&) {
                 int slot = q[i];
                 o = xyz(w.o[slot]);
                 d = xyz(w.d[slot]);
@@ -234,28 +249,23 @@ __global__ void __launch_bounds__(256) k_wf_shadow(SceneView s, Wf w, int par)
     const int* sq = w.sq + (size_t)par * w.M * w.L;
     uint32_t rays = 0;
     if (!WIDE && s.n_internal > 0) {
-        rays = trace_items_bvh2(
+        rays = trace_items_bvh2<true>(
             s, n, &w.cnt[9 + 2 * par], w.err,
-            [&](int i, float3& o, float3& d, float& tmn, float& tmx) {
+            [&](int i, float3& o, float3& d, float& tmn, float& tmx, int& skip) {
                 int e = sq[i];
+                float4 dd = w.sd[e];
                 o = xyz(w.so[e]);
-                d = xyz(w.sd[e]);
+                d = xyz(dd);
                 tmn = 0.001f;
-                tmx = CPT_INF_F;
+                tmx = dd.w;
+                skip = e % w.L;
             },
-            [&](int i, const Hit& h) {
-                int e = sq[i];
-                int obst = h.leaf >= 0 ? __float_as_int(ldg4(s.leaf_rec + 3 * (size_t)h.leaf).w) : -1;
-                w.svis[e] = obst == e % w.L ? 1 : 0;
-            });
+            [&](int i, const Hit& h) { w.svis[sq[i]] = h.leaf < 0 ? 1 : 0; });
     } else {
         for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
             int e = sq[idx];
-            int k = e % w.L;
-            Hit h;
-            bool hit = trace_closest<WIDE>(s, xyz(w.so[e]), xyz(w.sd[e]), 0.001f, CPT_INF_F, h, w.err);
-            int obst = hit ? __float_as_int(ldg4(s.leaf_rec + 3 * (size_t)h.leaf).w) : -1;
-            w.svis[e] = obst == k ? 1 : 0;
+            float4 dd = w.sd[e];
+            w.svis[e] = occluded<WIDE>(s, xyz(w.so[e]), xyz(dd), dd.w, e % w.L, w.err) ? 0 : 1;
             rays++;
         }
     }
@@ -283,8 +293,8 @@ __global__ void __launch_bounds__(128) k_wf_resolve(SceneView s, Wf w, RenderArg
         float3 acc = add_visible(w, slot, w.nee[slot], xyz(w.radp[slot]));
         w.pix[slot] = w0(xyz(w.pix[slot]) + acc);
         w.nee[slot] = 0;
-        write_pixel(s, w, a, slot, w.pixel[slot], w.flags[slot]);
-        next_pixel(s, w, a, slot, nq);
+        finish_item(w, a, slot, w.pixel[slot], w.flags[slot]);
+        next_item(s, w, a, slot, nq);
     }
 }
 
@@ -393,11 +403,13 @@ __global__ void __launch_bounds__(128) k_wf_shade(SceneView s, Wf w, RenderArgs 
                                 float3 dir = unit3(lp - sf.pos);
                                 float cs_ = dot3(dir, sf.normal), cl_ = dot3(-dir, L.normal);
                                 if (!(cs_ > 0.f && cl_ > 0.f)) continue;
+                                float tl;
+                                if (!hit_light(L, sf.pos, dir, 0.001f, CPT_INF_F, tl)) continue;
                                 float3 fr = bsdf_eval(sf, d, dir);
                                 float g = cs_ * cl_ / len2(lp - sf.pos) * area;
                                 int e = slot * w.L + k;
                                 w.so[e] = w0(sf.pos);
-                                w.sd[e] = w0(dir);
+                                w.sd[e] = make_float4(dir.x, dir.y, dir.z, tl);   // occlusion query up to the light
                                 w.sc[e] = w0(thr * (L.color * fr * g));
                                 nee |= 1 << k;
                             }
@@ -440,21 +452,20 @@ __global__ void __launch_bounds__(128) k_wf_shade(SceneView s, Wf w, RenderArgs 
             to_trace = true;
         } else {
             // the sample ended
-            int done = w.spp_done[slot] + 1;
-            w.spp_done[slot] = done;
+            const int k = w.sample[slot] + 1;   // next sample of the pixel
             if (nee) {
                 w.radp[slot] = w0(rad);
                 fl |= F_NEE_PREV;
             } else {
                 w.pix[slot] = w0(xyz(w.pix[slot]) + rad);
             }
-            if (done < a.spp) {
-                start_sample(s, w, slot, pixel, rng, fl);
+            if (k % w.S != 0 && k < a.spp) {   // the item's group has samples left
+                start_sample(s, w, a.seed, slot, pixel, k, rng, fl);
                 to_trace = true;
-            } else if (nee) {
-                to_resolve = true;
             } else {
-                write_pixel(s, w, a, slot, pixel, fl);
+                w.sample[slot] = k;
+                if (nee) to_resolve = true;
+                else finish_item(w, a, slot, pixel, fl);
             }
         }
         w.flags[slot] = fl;
@@ -464,23 +475,36 @@ __global__ void __launch_bounds__(128) k_wf_shade(SceneView s, Wf w, RenderArgs 
                 if ((nee >> k) & 1) append(w.sq + (size_t)nq * w.M * w.L, &w.cnt[4 + nq], slot * w.L + k);
         if (to_trace) append(w.q + (size_t)nq * w.M, &w.cnt[nq], slot);
         if (to_resolve) append(w.rq + (size_t)nq * w.M, &w.cnt[2 + nq], slot);
-        if (!cont && !to_trace && !to_resolve) next_pixel(s, w, a, slot, nq);
+        if (!cont && !to_trace && !to_resolve) next_item(s, w, a, slot, nq);
     }
 }
 
 // CHUNK iterations: trace, shadow, resolve, shade, with the traversal of the scene's layout.
+// When capturing with a side stream, the shadow kernel is forked onto it so that the two
+// traversal kernels of an iteration overlap (each one's tail fills with the other's warps).
 void enqueue_chunk(const SceneView& view, const Wf& w, const RenderArgs& args, int gt, int bt, int gs, int bs,
-                   cudaStream_t st)
+                   cudaStream_t st, const WavefrontTuning* fork)
 {
     const bool wide = view.wide != nullptr;
     for (int it = 0; it < CHUNK; ++it) {
         int par = it & 1;
+        cudaStream_t ss = st;
+        if (fork) {
+            cudaEventRecord(fork->fork, st);
+            cudaStreamWaitEvent(fork->side_stream, fork->fork, 0);
+            ss = fork->side_stream;
+        }
+        const size_t smem = short_stack_bytes(bt);
         if (wide) {
-            k_wf_trace<true><<<gt, bt, 0, st>>>(view, w, par);
-            k_wf_shadow<true><<<gt, bt, 0, st>>>(view, w, par);
+            k_wf_trace<true><<<gt, bt, smem, st>>>(view, w, par);
+            k_wf_shadow<true><<<gt, bt, smem, ss>>>(view, w, par);
         } else {
-            k_wf_trace<false><<<gt, bt, 0, st>>>(view, w, par);
-            k_wf_shadow<false><<<gt, bt, 0, st>>>(view, w, par);
+            k_wf_trace<false><<<gt, bt, smem, st>>>(view, w, par);
+            k_wf_shadow<false><<<gt, bt, smem, ss>>>(view, w, par);
+        }
+        if (fork) {
+            cudaEventRecord(fork->join, ss);
+            cudaStreamWaitEvent(st, fork->join, 0);
         }
         k_wf_resolve<<<gs, bs, 0, st>>>(view, w, args, par);
         k_wf_shade<<<gs, bs, 0, st>>>(view, w, args, par);
@@ -498,12 +522,12 @@ cpt_status carve(char*& p, size_t& left, T** out, size_t count)
     return CPT_OK;
 }
 
-size_t wf_bytes(int M, int L)
+size_t wf_bytes(int M, int L, size_t n_items)
 {
     size_t m = (size_t)M, ml = (size_t)M * std::max(L, 1);
     auto a = [](size_t b) { return align_up(b, 256); };
-    return a(m * 4) * 6 + a(m * 8) + a(m * 16) * 8 + a(m * 8) + a(2 * m * 4) * 2 + a(2 * ml * 4) + a(ml * 16) * 3 +
-           a(ml * 4) + a(64);
+    return a(m * 4) * 6 + a(m * 8) + a(m * 16) * 8 + a(n_items * 16) + a(m * 8) + a(2 * m * 4) * 2 +
+           a(2 * ml * 4) + a(ml * 16) * 3 + a(ml * 4) + a(64);
 }
 
 }  // namespace
@@ -517,18 +541,23 @@ cpt_status launch_render_wavefront(const SceneView& view, const RenderArgs& args
     if (npix <= 0) return CPT_OK;
     int L = std::max(view.n_lights, 1);
     if (view.n_lights > 30) return fail(CPT_ERR_UNSUPPORTED, "wavefront integrator: at most 30 lights");
-    int M = std::min(npix, std::max(tune.slots, 1024));
+    if (args.spp <= 0) return fail(CPT_ERR_INVALID_ARGUMENT, "spp must be positive");
+    const int S = sample_group(args.spp);
+    const int groups = (args.spp + S - 1) / S;
+    const size_t n_items = (size_t)groups * (size_t)npix;
+    if (n_items > (size_t)INT32_MAX / 2) return fail(CPT_ERR_UNSUPPORTED, "wavefront integrator: too many pixel groups");
+    int M = (int)std::min(n_items, (size_t)std::max(tune.slots, 1024));
     Wf w;
     std::memset(&w, 0, sizeof w);
     w.M = M;
     w.L = L;
-    w.spp = args.spp;
     w.first_pix = first;
-    w.end_pix = end;
-    w.W = W;
+    w.npix = npix;
+    w.S = S;
+    w.n_items = (int)n_items;
     w.rays = args.ray_counter;
     w.err = args.err;
-    size_t bytes = wf_bytes(M, L);
+    size_t bytes = wf_bytes(M, L, n_items);
     char* base = nullptr;
     CPT_CUDA(cudaMallocAsync((void**)&base, bytes, stream));
     char* p = base;
@@ -537,8 +566,9 @@ cpt_status launch_render_wavefront(const SceneView& view, const RenderArgs& args
     cpt_status st = CPT_OK;
 #define CARVE(f, n)                                   \
     if (st == CPT_OK) st = carve(p, left, &w.f, (n));
-    CARVE(pixel, M) CARVE(spp_done, M) CARVE(flags, M) CARVE(depth, M) CARVE(guard, M) CARVE(nee, M)
+    CARVE(pixel, M) CARVE(sample, M) CARVE(flags, M) CARVE(depth, M) CARVE(guard, M) CARVE(nee, M)
     CARVE(rng, M) CARVE(o, M) CARVE(d, M) CARVE(thr, M) CARVE(rad, M) CARVE(radp, M) CARVE(pix, M) CARVE(hit, M)
+    CARVE(part, n_items)
     CARVE(so, ml) CARVE(med, M) CARVE(q, 2 * (size_t)M) CARVE(rq, 2 * (size_t)M) CARVE(sq, 2 * ml) CARVE(sd, ml)
     CARVE(sc, ml) CARVE(svis, ml) CARVE(cnt, 16)
 #undef CARVE
@@ -558,7 +588,7 @@ cpt_status launch_render_wavefront(const SceneView& view, const RenderArgs& args
         // Capture CHUNK iterations (4 launches each) once; replay until the queues drain.
         cudaStream_t cs = tune.capture_stream;
         CPT_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
-        enqueue_chunk(view, w, args, gt, bt, gs, bs, cs);
+        enqueue_chunk(view, w, args, gt, bt, gs, bs, cs, tune.side_stream ? &tune : nullptr);
         cudaError_t ce = cudaStreamEndCapture(cs, &graph);
         if (ce != cudaSuccess) {
             cudaFreeAsync(base, stream);
@@ -578,7 +608,7 @@ cpt_status launch_render_wavefront(const SceneView& view, const RenderArgs& args
         if (use_graph) {
             CPT_CUDA(cudaGraphLaunch(exec, stream));
         } else {
-            enqueue_chunk(view, w, args, gt, bt, gs, bs, stream);
+            enqueue_chunk(view, w, args, gt, bt, gs, bs, stream, nullptr);
         }
         add_launches(4 * CHUNK);
         CPT_CUDA(cudaMemcpyAsync(host_cnt, w.cnt, sizeof host_cnt, cudaMemcpyDeviceToHost, stream));
@@ -589,6 +619,10 @@ cpt_status launch_render_wavefront(const SceneView& view, const RenderArgs& args
         }
     }
     if (exec) cudaGraphExecDestroy(exec);
+    if (drained) {
+        k_wf_finish<<<(npix + 255) / 256, 256, 0, stream>>>(w, args, groups);
+        add_launches(1);
+    }
     cudaFreeAsync(base, stream);
     CPT_CUDA(cudaGetLastError());
     if (!drained) return fail(CPT_ERR_TIMEOUT, "wavefront integrator did not drain");
@@ -604,8 +638,9 @@ cpt_status wavefront_grids(int sm_count, int block_trace, int block_shade, int* 
 {
     int bt = 0, bs = 0;
     int bt2 = 0;
-    CPT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bt, k_wf_trace<true>, block_trace, 0));
-    CPT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bt2, k_wf_trace<false>, block_trace, 0));
+    const size_t smem = short_stack_bytes(block_trace);
+    CPT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bt, k_wf_trace<true>, block_trace, smem));
+    CPT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bt2, k_wf_trace<false>, block_trace, smem));
     bt = std::min(bt, bt2);
     CPT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bs, k_wf_shade, block_shade, 0));
     *grid_trace = std::max(1, bt) * sm_count;

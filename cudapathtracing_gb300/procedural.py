@@ -49,6 +49,22 @@ class PCG32Streams:
         """(x + 1) * 2^-32 in (0, 1], as double."""
         return (self.next().astype(np.float64) + 1.0) * (1.0 / 4294967296.0)
 
+    def advance(self, delta: int) -> "PCG32Streams":
+        """Moves every stream `delta` draws ahead in O(log delta) (LCG jump-ahead, Brown 1994)."""
+        cm, cp = _MULT, self.inc.copy()
+        am, ap = np.uint64(1), np.zeros_like(self.state)
+        delta = int(delta)
+        with np.errstate(over="ignore"):
+            while delta:
+                if delta & 1:
+                    am = am * cm
+                    ap = ap * cm + cp
+                cp = (cm + np.uint64(1)) * cp
+                cm = cm * cm
+                delta >>= 1
+            self.state = am * self.state + ap
+        return self
+
 
 def pcg32_sequence(seed: int, n: int, stream: int = 0) -> np.ndarray:
     """n consecutive uniforms of one stream."""

@@ -84,7 +84,26 @@ struct Rng {
         next();
     }
     double uniform() { return ((double)next() + 1.0) * (1.0 / 4294967296.0); }   // (0, 1]
+    // delta draws ahead in O(log delta) (LCG jump-ahead, Brown 1994)
+    void advance(uint64_t delta)
+    {
+        uint64_t cm = 6364136223846793005ULL, cp = inc, am = 1, ap = 0;
+        while (delta) {
+            if (delta & 1u) {
+                am *= cm;
+                ap = ap * cm + cp;
+            }
+            cp *= cm + 1;
+            cm *= cm;
+            delta >>= 1;
+        }
+        state = am * state + ap;
+    }
 };
+
+// Config estimator: sample k of a pixel uses the pixel's stream k * 2^32 draws ahead; sample
+// radiance is summed in groups of sampleGroup(spp) samples, group sums added in order.
+static int sampleGroup(int spp) { return spp <= 256 ? 8 : (spp + 31) / 32; }
 
 // ------------------------------------------------------------------ scene objects
 enum MatType { M_NONE = 0, M_LIGHT = 1, M_OPAQUE = 2, M_SPEC = 3, M_ROUGH = 4, M_VOLUME = 5, M_LAMBERT = 6 };
@@ -939,12 +958,14 @@ static PixelOut renderPixelConfig(const Scene& s, int i, int j, const cpt_render
 {
     PixelOut out = {};
     int offset = j * s.width + i;
-    Rng st;
-    st.init(p.seed, (uint64_t)offset);
-    V3 pix = v3(0, 0, 0);
+    const int group = sampleGroup(p.spp);
+    V3 pix = v3(0, 0, 0), gsum = v3(0, 0, 0);
     uint64_t rays = 0;
     out.gDepth = INF;
     for (int sample = 0; sample < p.spp; ++sample) {
+        Rng st;
+        st.init(p.seed, (uint64_t)offset);
+        st.advance((uint64_t)sample << 32);
         double rx = st.uniform();
         double ry = st.uniform();
         Ray ray = cameraRay(s, i, j, rx, ry);
@@ -996,7 +1017,7 @@ static PixelOut renderPixelConfig(const Scene& s, int i, int j, const cpt_render
                 if (countEmission) rad = rad + thr * rec.hitColor;
                 break;
             }
-            if (depth == 0 && out.gDepth >= INF) {
+            if (depth == 0 && sample < group && out.gDepth >= INF) {
                 out.gN = rec.normal;
                 out.gDepth = length(s.lookFrom - rec.hitPos);
                 out.gAlbedo = rec.hitColor;
@@ -1014,6 +1035,8 @@ static PixelOut renderPixelConfig(const Scene& s, int i, int j, const cpt_render
                     if (!(cs > 0.0 && cl > 0.0)) continue;   // cannot contribute: no shadow ray
                     Ray sr = {rec.hitPos, dir};
                     HitRecord lrec;
+                    // a ray that misses the light itself (an invisible light) cannot see it: not traced
+                    if (!hitLight(L, sr, lrec, 0.001, INF)) continue;
                     int obst = traverse(s, sr, lrec);
                     rays++;
                     if (obst == k) {
@@ -1041,7 +1064,11 @@ static PixelOut renderPixelConfig(const Scene& s, int i, int j, const cpt_render
             ray.o = rec.hitPos;
             ray.d = dir;
         }
-        pix = pix + rad;
+        gsum = gsum + rad;
+        if ((sample + 1) % group == 0 || sample + 1 == p.spp) {
+            pix = pix + gsum;
+            gsum = v3(0, 0, 0);
+        }
     }
     pix = v3(pix.x / p.spp, pix.y / p.spp, pix.z / p.spp);
     out.rgb = pix;

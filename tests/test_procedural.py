@@ -45,3 +45,20 @@ def test_camera_height_rule():
     assert Camera(1920, 16.0 / 9.0).height == 1080
     assert Camera(800, 16.0 / 9.0).height == 450
     assert Camera(10, 100.0).height == 1
+
+
+def test_pcg32_jump_ahead_matches_stepping():
+    """advance(n) equals n draws (config-estimator sample streams start k * 2^32 draws ahead)."""
+    streams = np.arange(5, dtype=np.uint64) * np.uint64(7919)
+    for n in (0, 1, 2, 7, 64, 1000):
+        a = P.PCG32Streams(11, streams)
+        b = P.PCG32Streams(11, streams)
+        for _ in range(n):
+            a.next()
+        b.advance(n)
+        assert np.array_equal(a.state, b.state)
+        assert np.array_equal(a.next(), b.next())
+    # jumps compose: 3 * 2^32 in one step or in three
+    a = P.PCG32Streams(3, streams).advance(3 << 32)
+    b = P.PCG32Streams(3, streams).advance(1 << 32).advance(1 << 32).advance(1 << 32)
+    assert np.array_equal(a.state, b.state)
