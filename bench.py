@@ -191,11 +191,14 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="cpt", choices=["cpt", "reference"])
     ap.add_argument("--workload", default="spheres_1080p", choices=sorted(WORKLOADS))
-    ap.add_argument("--integrator", default="megakernel", choices=["megakernel", "wavefront"])
+    ap.add_argument("--integrator", default="wavefront", choices=["megakernel", "wavefront"])
+    ap.add_argument("--no-compare", action="store_true",
+                    help="skip timing the megakernel beside the wavefront integrator")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--spp", type=int, default=0, help="override the workload's spp (profiling captures)")
     ap.add_argument("--e2e-steps", type=int, default=2, help="steps of the end-to-end leg (0: skip)")
     ap.add_argument("--bvh-width", type=int, default=2, choices=[2, 8], help="traversal layout")
+    ap.add_argument("--no-autotune", action="store_true", help="use the library defaults (no autotuner)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference_arm(args)
@@ -226,6 +229,14 @@ def main():
     seed = 1000 * rank
 
     trace_only = args.workload == "icosphere_10M"
+    tuner, tuned = None, None
+    if not trace_only and not args.no_autotune:
+        # launch shapes from the autotuner (cached per device and workload; tuning is not timed)
+        from cudapathtracing_gb300 import autotune
+        tuner = autotune.Autotuner(ctx, cache_path=os.path.join(ROOT, "cudapathtracing_gb300", "_build",
+                                                                "tune_cache.json"),
+                                   probe_spp=min(16, wl["spp"]), repeats=2)
+        tuned = tuner.tune(scene, dict(wl, seed=seed), integ)
     if trace_only:
         from cudapathtracing_gb300 import procedural as P
         n_rays = 10_000_000
@@ -270,6 +281,32 @@ def main():
         barrier()
     launches = _lib.lib().cpt_launch_count() - launches0
     elapsed = ev0.elapsed_time(ev1) / 1e3
+
+    # the megakernel on the same scene, seeds and steps (the integrator the wavefront must beat)
+    compare = None
+    if not trace_only and integ == abi.INTEGRATOR_WAVEFRONT and not args.no_compare:
+        mk_tuned = tuner.tune(scene, dict(wl, seed=seed), abi.INTEGRATOR_MEGAKERNEL) if tuner else None
+        scene.render(rgb=rgb, rgba8=rgba, stream=stream.cuda_stream, integrator=abi.INTEGRATOR_MEGAKERNEL,
+                     seed=seed, **wl)
+        barrier()
+        mk_rays, mk_ms = 0, []
+        c0, c1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        c0.record(stream)
+        for i in range(args.steps):
+            scene.buildBVH(stream.cuda_stream)
+            r = scene.render(rgb=rgb, rgba8=rgba, stream=stream.cuda_stream, integrator=abi.INTEGRATOR_MEGAKERNEL,
+                             seed=seed + args.warmup + i, **wl)
+            mk_rays += r["rays"]
+            mk_ms.append(r["ms"])
+        c1.record(stream)
+        barrier()
+        mk_el = c0.elapsed_time(c1) / 1e3
+        compare = {"integrator": "megakernel", "value": round(mk_rays / mk_el / 1e6, 3), "unit": "Mrays/s",
+                   "ms_per_step": round(mk_el / args.steps * 1e3, 3),
+                   "render_ms": round(float(np.mean(mk_ms)), 3),
+                   "tuned": mk_tuned.to_json()["knobs"] if mk_tuned else None}
+        if tuner:   # back to the wavefront's choice for the end-to-end leg
+            tuner.tune(scene, dict(wl, seed=seed), integ)
     if world > 1:
         import torch.distributed as dist
         t = torch.tensor([elapsed, float(rays)], device="cuda", dtype=torch.float64)
@@ -345,19 +382,24 @@ def main():
         "warmup": args.warmup, "ms_per_step": round(elapsed / args.steps * 1e3, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": args.workload, "width": W, "height": H, "spp": wl["spp"],
-                   "triangles": desc.num_triangles, "integrator": args.integrator, "bvh_width": args.bvh_width,
+                   "triangles": desc.num_triangles, "integrator": args.integrator,
+                   "bvh_width": int(tuned.knobs["bvh_width"]) if tuned else args.bvh_width,
                    "estimator": "config" if wl["estimator"] == 1 else "reference",
                    "max_depth": wl["max_depth"], "rr_depth": wl["rr_depth"], "rr_prob": wl["rr_prob"],
                    "step": "LBVH build + full render", "l2": "inputs larger than L2 (BVH + leaf records)",
                    "build_ms": round(float(np.mean(build_ms)), 3), "rays_per_step": int(rays_per_launch),
-                   "parallelism": f"replicas x{world}"},
+                   "parallelism": f"replicas x{world}",
+                   "tuned": ({"knobs": tuned.to_json()["knobs"], "probe_mrays": round(tuned.score, 1),
+                              "probe_default_mrays": round(tuned.default_score, 1)} if tuned else None)},
         "e2e": {"value": round(e2e_rays / e2e_t / 1e6, 3), "unit": "Mrays/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "steps": e2e_steps},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,
-                     "kernel": "k_trace" if trace_only else ("k_wf_*" if args.integrator == "wavefront" else "k_render"),
+                     "kernel": "k_trace_dyn" if trace_only else (
+                         "k_wf_* (every launch of one render)" if args.integrator == "wavefront" else "k_render"),
                      "kernel_ms": round(k_ms, 3), "bytes_per_ray": round(bpr, 1), "peak_source": peak_src},
         "cpu_baseline": cpu,
+        "megakernel_same_run": compare,
         "clocks": clk.summary(),
         "gpu_launches": int(launches),
     }

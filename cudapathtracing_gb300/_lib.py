@@ -41,6 +41,7 @@ def lib():
             "cpt_context_set_render_block": (S, [P, C.c_int, C.c_int]),
             "cpt_context_set_wavefront": (S, [P, C.c_int, C.c_int, C.c_int, C.c_int]),
             "cpt_context_set_bvh_width": (S, [P, C.c_int]),
+            "cpt_context_set_short_stack": (S, [P, C.c_int]),
             "cpt_ini_load": (S, [C.c_char_p, C.POINTER(P)]),
             "cpt_ini_describe": (S, [P, C.POINTER(abi.cpt_scene_desc)]),
             "cpt_ini_free": (S, [P]),

@@ -49,6 +49,9 @@ class Context:
         check(lib().cpt_context_set_wavefront(self.h, slots, block_trace, block_shade, use_graph),
               "cpt_context_set_wavefront")
 
+    def set_short_stack(self, entries: int) -> None:
+        check(lib().cpt_context_set_short_stack(self.h, entries), "cpt_context_set_short_stack")
+
     def close(self):
         if self.h:
             lib().cpt_context_destroy(self.h)

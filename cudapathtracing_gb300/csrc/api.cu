@@ -52,7 +52,8 @@ struct cpt_context {
 };
 
 namespace cpt {
-cpt_status wavefront_grids(int sm_count, int block_trace, int block_shade, int* grid_trace, int* grid_shade);
+cpt_status wavefront_grids(int sm_count, int block_trace, int block_shade, int short_entries, int* grid_trace,
+                           int* grid_shade);
 size_t wide_scratch_bytes(uint32_t n);
 cpt_status build_wide(uint32_t n, const int2* child, const float4* node_box, const float4* leaf_box, float4* wide,
                       void* scratch, size_t scratch_bytes, cudaStream_t stream, uint32_t* num_wide);
@@ -436,7 +437,8 @@ CPT_EXPORT cpt_status cpt_context_create(int device, cpt_context** out)
     c->render_block_x = 16;
     c->render_block_y = 8;
     std::memset(&c->wf, 0, sizeof c->wf);
-    c->wf.slots = 1 << 20;
+    c->wf.slots = 1 << 21;
+    c->wf.short_stack = CPT_SHORT_STACK;
     c->wf.block_trace = 128;
     c->wf.block_shade = 128;
     c->wf.use_graph = true;
@@ -465,9 +467,8 @@ CPT_EXPORT cpt_status cpt_context_set_wavefront(cpt_context* ctx, int slots, int
                                                 int use_graph)
 {
     auto ok_block = [](int b, int hi) { return b >= 32 && b <= hi && b % 32 == 0; };
-    if (!ctx || slots < 1024 || !ok_block(block_trace, 512) || !ok_block(block_shade, 1024))
-        return fail(CPT_ERR_INVALID_ARGUMENT,
-                    "wavefront: slots >= 1024, blocks multiples of 32 (trace <= 512, shade <= 1024)");
+    if (!ctx || slots < 1024 || !ok_block(block_trace, 256) || !ok_block(block_shade, 256))
+        return fail(CPT_ERR_INVALID_ARGUMENT, "wavefront: slots >= 1024, blocks multiples of 32 in [32, 256]");
     ctx->wf.slots = slots;
     ctx->wf.block_trace = block_trace;
     ctx->wf.block_shade = block_shade;
@@ -484,6 +485,15 @@ CPT_EXPORT cpt_status cpt_context_set_bvh_width(cpt_context* ctx, int width)
 }
 
 // Internal tuning knob (the autotuner's setter): render block shape.
+CPT_EXPORT cpt_status cpt_context_set_short_stack(cpt_context* ctx, int entries)
+{
+    if (!ctx || (entries != 8 && entries != 16 && entries != 24 && entries != 32))
+        return fail(CPT_ERR_INVALID_ARGUMENT, "short stack: 8, 16, 24 or 32 entries");
+    ctx->wf.short_stack = entries;
+    ctx->wf_grids_ready = false;
+    return CPT_OK;
+}
+
 CPT_EXPORT cpt_status cpt_context_set_render_block(cpt_context* ctx, int bx, int by)
 {
     if (!ctx || bx <= 0 || by <= 0 || (bx * by) % 32 || bx * by > 512)   // short stacks: <= 32 KB shared
@@ -752,7 +762,7 @@ CPT_EXPORT cpt_status cpt_render(cpt_scene* s, const cpt_render_params* p, const
     if (p->integrator == CPT_INTEGRATOR_WAVEFRONT) {
         cpt_context* c = s->ctx;
         if (!c->wf_grids_ready) {
-            st = wavefront_grids(c->sm_count, c->wf.block_trace, c->wf.block_shade, &c->wf.grid_trace,
+            st = wavefront_grids(c->sm_count, c->wf.block_trace, c->wf.block_shade, c->wf.short_stack, &c->wf.grid_trace,
                                  &c->wf.grid_shade);
             c->wf_grids_ready = st == CPT_OK;
         }

@@ -158,18 +158,24 @@ struct Pcg32 {
 #endif
 
 // ------------------------------------------------------------------ traversal stack
-// The binary traversal keeps the bottom CPT_SHORT_STACK entries of its stack in shared memory
-// and the rest in local memory.  Every kernel that traverses the BVH2 is launched with
-// short_stack_bytes(threads per block) of dynamic shared memory; thread t owns the column
+// The binary traversal keeps the bottom SHORT entries of its stack in shared memory and the rest
+// in local memory.  Every kernel that traverses the BVH2 with a short stack is launched with
+// short_stack_bytes(threads per block, SHORT) of dynamic shared memory; thread t owns the column
 // t, t + T, t + 2T, ... (T = threads per block), so a warp's pushes and pops hit 32 distinct banks.
+// The wavefront's trace kernels are instantiated for the depths the autotuner may pick.
 #define CPT_SHORT_STACK 16
-inline constexpr size_t short_stack_bytes(int threads) { return (size_t)CPT_SHORT_STACK * threads * sizeof(int); }
+inline constexpr size_t short_stack_bytes(int threads, int entries = CPT_SHORT_STACK)
+{
+    return (size_t)entries * threads * sizeof(int);
+}
 
 #ifdef __CUDACC__
-struct ShortStack {
+template <int SHORT>
+struct ShortStackN {
+    static_assert(SHORT > 0 && SHORT < CPT_STACK, "short stack depth");
     int* col;     // this thread's column in the block's dynamic shared array
     int stride;   // threads per block
-    int spill[CPT_STACK - CPT_SHORT_STACK];
+    int spill[CPT_STACK - SHORT];
     __device__ __forceinline__ void init()
     {
         extern __shared__ int cpt_short_stack_smem[];
@@ -179,13 +185,19 @@ struct ShortStack {
     }
     __device__ __forceinline__ void put(int i, int v)
     {
-        if (i < CPT_SHORT_STACK) col[i * stride] = v;
-        else spill[i - CPT_SHORT_STACK] = v;
+        if (i < SHORT) col[i * stride] = v;
+        else spill[i - SHORT] = v;
     }
-    __device__ __forceinline__ int get(int i) const
-    {
-        return i < CPT_SHORT_STACK ? col[i * stride] : spill[i - CPT_SHORT_STACK];
-    }
+    __device__ __forceinline__ int get(int i) const { return i < SHORT ? col[i * stride] : spill[i - SHORT]; }
+};
+using ShortStack = ShortStackN<CPT_SHORT_STACK>;
+
+// The whole stack in local memory (no shared memory needed at launch).
+struct LocalStack {
+    int s[CPT_STACK];
+    __device__ __forceinline__ void init() {}
+    __device__ __forceinline__ void put(int i, int v) { s[i] = v; }
+    __device__ __forceinline__ int get(int i) const { return s[i]; }
 };
 #endif
 

@@ -92,6 +92,7 @@ struct WavefrontTuning {
     int slots;                   // path slots (the wavefront size)
     int grid_trace, block_trace; // persistent grids
     int grid_shade, block_shade;
+    int short_stack;             // traversal stack entries kept in shared memory (8, 16, 24, 32)
     bool use_graph;
     cudaStream_t capture_stream; // non-default stream used only to capture the iteration graph
     cudaStream_t side_stream;    // second capture stream: shadow rays traced beside extension rays

@@ -225,13 +225,13 @@ __device__ __forceinline__ bool trace_closest_wide(const SceneView& s, float3 o,
 // Binary-node traversal (Aila–Laine node layout): near child first, far child pushed.  The
 // stack (ShortStack: shared memory, then local memory) holds at most one entry per level.  ANY as in
 // trace_closest_wide.
-template <bool ANY>
+template <bool ANY, typename Stack>
 __device__ __forceinline__ bool trace_closest_bvh2(const SceneView& s, float3 o, float3 d, float tmin, float tmax,
                                                    Hit& hit, int* err, int skip)
 {
     const float3 idir = safe_inverse(d);
     const float3 ood = f3(o.x * idir.x, o.y * idir.y, o.z * idir.z);
-    ShortStack stack;
+    Stack stack;
     stack.init();
     int sp = 0;
     int node = 0;
@@ -280,13 +280,13 @@ __device__ __forceinline__ bool trace_closest_bvh2(const SceneView& s, float3 o,
 // One ray's traversal state, advanced one node per call, so that a warp can refill lanes whose
 // ray finished with new rays instead of waiting for its slowest lane (dynamic ray fetching,
 // Aila & Laine 2009).  The visit order and pruning are those of trace_closest_bvh2.
-template <bool ANY>
+template <bool ANY, typename Stack>
 struct Bvh2Walk {
     float3 o, d, idir, ood;
     float tmin, best;
     int node, sp, skip;
     Hit hit;
-    ShortStack stack;   // init() once per kernel, before the first start()
+    Stack stack;   // init() once per kernel, before the first start()
 
     __device__ __forceinline__ void start(float3 o_, float3 d_, float tmin_, float tmax_, int skip_)
     {
@@ -356,12 +356,12 @@ __device__ __forceinline__ uint32_t lane_mask_lt()
 // warp).  load(i, o, d, tmin, tmax, skip) supplies item i's ray (skip: the light an occlusion
 // query aims at), store(i, hit) takes its result (for ANY, hit.leaf >= 0 means occluded).  All
 // 32 lanes of every warp must call this together.  Returns the number of rays traced by the lane.
-template <bool ANY, typename Load, typename Store>
+template <bool ANY, typename Stack = ShortStack, typename Load, typename Store>
 __device__ __forceinline__ uint32_t trace_items_bvh2(const SceneView& s, int n, int* fetch, int* err, Load load,
                                                      Store store)
 {
     const int lane = threadIdx.x & 31;
-    Bvh2Walk<ANY> w;
+    Bvh2Walk<ANY, Stack> w;
     w.stack.init();
     int item = -1;
     bool exhausted = false;
@@ -399,8 +399,9 @@ __device__ __forceinline__ uint32_t trace_items_bvh2(const SceneView& s, int n, 
 // Closest hit over [tmin (boxes), tmax]; false on a miss.  WIDE selects the traversal layout at
 // compile time (each kernel is instantiated for the layout the scene was built with), so a
 // kernel carries the registers and code of one traversal only.  *err gets CPT_DEVERR_STACK if a
-// fixed stack would overflow.  With ANY the query is an occlusion test (see occluded).
-template <bool WIDE, bool ANY = false>
+// fixed stack would overflow.  With ANY the query is an occlusion test (see occluded).  Stack is
+// where the binary traversal keeps its stack (ShortStack needs short_stack_bytes at launch).
+template <bool WIDE, bool ANY = false, typename Stack = ShortStack>
 __device__ __forceinline__ bool trace_closest(const SceneView& s, float3 o, float3 d, float tmin, float tmax, Hit& hit,
                                               int* err, int skip = -1)
 {
@@ -414,7 +415,7 @@ __device__ __forceinline__ bool trace_closest(const SceneView& s, float3 o, floa
         return hit.leaf >= 0;
     }
     if (WIDE) return trace_closest_wide<ANY>(s, o, d, tmin, tmax, hit, err, skip);
-    return trace_closest_bvh2<ANY>(s, o, d, tmin, tmax, hit, err, skip);
+    return trace_closest_bvh2<ANY, Stack>(s, o, d, tmin, tmax, hit, err, skip);
 }
 
 // Visibility of light `light` along a shadow ray whose hit on that light is at t_light (from
@@ -422,11 +423,11 @@ __device__ __forceinline__ bool trace_closest(const SceneView& s, float3 o, floa
 // that light" (Render.cu:178-181); except for exact ties in t it equals "nothing but that light is
 // hit in [0.001, t_light]", which this occlusion query answers and which stops at the first
 // occluder instead of searching for the closest one.
-template <bool WIDE>
+template <bool WIDE, typename Stack = ShortStack>
 __device__ __forceinline__ bool occluded(const SceneView& s, float3 o, float3 d, float t_light, int light, int* err)
 {
     Hit h;
-    return trace_closest<WIDE, true>(s, o, d, 0.001f, t_light, h, err, light);
+    return trace_closest<WIDE, true, Stack>(s, o, d, 0.001f, t_light, h, err, light);
 }
 
 }  // namespace cpt

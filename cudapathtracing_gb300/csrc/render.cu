@@ -9,6 +9,8 @@
 //     per sample and group-wise sample sums (Pcg32::init_sample, sample_group).
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "cpt_internal.h"
 #include "cpt_shade.cuh"
 
@@ -17,6 +19,11 @@ namespace cpt {
 namespace {
 
 constexpr int ITER_LIMIT = 1 << 16;   // bound on loop trips per sample (error word on overflow)
+
+// Traversal stack of the megakernel: local memory.  (A shared-memory short stack made this
+// 122-register kernel slower on GB300; the wavefront's trace kernels use one.)
+using MkStack = LocalStack;
+constexpr size_t mk_stack_smem(int threads) { return std::is_same<MkStack, ShortStack>::value ? short_stack_bytes(threads) : 0; }
 
 __device__ __forceinline__ float3 camera_dir(const DevCamera& c, int i, int j, float rx, float ry)   // Camera.cuh:37-43
 {
@@ -62,7 +69,7 @@ __device__ PixelResult pixel_reference(const SceneView& s, int i, int j, const R
                 break;
             }
             Hit h;
-            bool hit = trace_closest<WIDE>(s,o, d, 0.001f, CPT_INF_F, h, a.err);
+            bool hit = trace_closest<WIDE, false, MkStack>(s, o, d, 0.001f, CPT_INF_F, h, a.err);
             out.rays++;
             Surf sf;
             if (hit) make_surface(s, o, d, h, true, sf);
@@ -70,7 +77,7 @@ __device__ PixelResult pixel_reference(const SceneView& s, int i, int j, const R
                 const float sig = 25.0f;
                 o = sf.pos;
                 Hit vh;
-                bool vhit = trace_closest<WIDE>(s,o, d, 0.001f, CPT_INF_F, vh, a.err);
+                bool vhit = trace_closest<WIDE, false, MkStack>(s, o, d, 0.001f, CPT_INF_F, vh, a.err);
                 out.rays++;
                 if (!vhit) continue;
                 float dmax = vh.t;
@@ -93,7 +100,7 @@ __device__ PixelResult pixel_reference(const SceneView& s, int i, int j, const R
                     o = pos;
                     d = nd;
                     pos = sf.pos + t * nd;
-                    vhit = trace_closest<WIDE>(s,o, d, 0.001f, CPT_INF_F, vh, a.err);
+                    vhit = trace_closest<WIDE, false, MkStack>(s, o, d, 0.001f, CPT_INF_F, vh, a.err);
                     out.rays++;
                     if (vhit) dmax = vh.t;
                     t = -logf(rng.one_minus_uniform_from(rng.next())) / sig;
@@ -122,7 +129,7 @@ __device__ PixelResult pixel_reference(const SceneView& s, int i, int j, const R
                 float3 lp = L.center + ((ua - 0.5f) * lw) * L.eu + ((ub - 0.5f) * lh) * L.ev;
                 float3 dir = unit3(lp - sf.pos);
                 Hit lh2;
-                trace_closest<WIDE>(s,sf.pos, dir, 0.001f, CPT_INF_F, lh2, a.err);
+                trace_closest<WIDE, false, MkStack>(s, sf.pos, dir, 0.001f, CPT_INF_F, lh2, a.err);
                 out.rays++;
                 int obst = prim_of(s, lh2);
                 if (dot3(dir, sf.normal) > 0.f && dot3(-dir, L.normal) > 0.f && obst == k) {
@@ -179,7 +186,7 @@ __device__ PixelResult pixel_config(const SceneView& s, int i, int j, const Rend
                 break;
             }
             Hit h;
-            bool hit = trace_closest<WIDE>(s,o, d, 0.001f, CPT_INF_F, h, a.err);
+            bool hit = trace_closest<WIDE, false, MkStack>(s, o, d, 0.001f, CPT_INF_F, h, a.err);
             out.rays++;
             if (in_medium) {
                 float t_hit = hit ? h.t : CPT_INF_F;
@@ -242,7 +249,7 @@ __device__ PixelResult pixel_config(const SceneView& s, int i, int j, const Rend
                     float tl;
                     if (!hit_light(L, sf.pos, dir, 0.001f, CPT_INF_F, tl)) continue;   // cannot see the light
                     out.rays++;
-                    if (!occluded<WIDE>(s, sf.pos, dir, tl, k, a.err)) {
+                    if (!occluded<WIDE, MkStack>(s, sf.pos, dir, tl, k, a.err)) {
                         float3 fr = bsdf_eval(sf, d, dir);
                         float g = cs_ * cl_ / len2(lp - sf.pos) * area;
                         rad = rad + thr * (L.color * fr * g);
@@ -331,7 +338,7 @@ cpt_status launch_render_megakernel(const SceneView& view, const RenderArgs& arg
     dim3 grid((view.cam.width + bx - 1) / bx, (rows + by - 1) / by);
     const bool wide = view.wide != nullptr;
     if (bx * by > 512) return fail(CPT_ERR_INVALID_ARGUMENT, "render block: at most 512 threads");
-    const size_t smem = short_stack_bytes(bx * by);
+    const size_t smem = mk_stack_smem(bx * by);
     if (args.estimator == CPT_ESTIMATOR_REFERENCE) {
         if (wide) k_render<0, true><<<grid, block, smem, stream>>>(view, args);
         else k_render<0, false><<<grid, block, smem, stream>>>(view, args);

@@ -17,7 +17,7 @@
 //                 BSDF sampling (appends to Q_{i+1}); a finished sample starts the next one
 //
 // Queues are appended with warp-aggregated atomics; counters for iteration i+1 are cleared by
-// k_wf_trace of iteration i.  The host replays a CUDA graph of CPT_WF_CHUNK iterations and reads
+// k_wf_trace of iteration i.  The host replays a CUDA graph of CHUNK iterations and reads
 // the queue sizes after each replay to stop.
 #include <cooperative_groups.h>
 #include <cooperative_groups/reduce.h>
@@ -202,7 +202,7 @@ __global__ void k_wf_finish(Wf w, RenderArgs a, int groups)
     if (a.rgba8) reinterpret_cast<uchar4*>(a.rgba8)[off] = make_uchar4(to_u8(v.x), to_u8(v.y), to_u8(v.z), 255);
 }
 
-template <bool WIDE>
+template <bool WIDE, int SHORT>
 __global__ void __launch_bounds__(256) k_wf_trace(SceneView s, Wf w, int par)
 {
     const int n = w.cnt[par];
@@ -217,7 +217,7 @@ __global__ void __launch_bounds__(256) k_wf_trace(SceneView s, Wf w, int par)
     const int* q = w.q + (size_t)par * w.M;
     uint32_t rays = 0;
     if (!WIDE && s.n_internal > 0) {
-        rays = trace_items_bvh2<false>(
+        rays = trace_items_bvh2<false, ShortStackN<SHORT>>(
             s, n, &w.cnt[8 + 2 * par], w.err,
             [&](int i, float3& o, float3& d, float& tmn, float& tmx, int&) {
                 int slot = q[i];
@@ -242,14 +242,14 @@ __global__ void __launch_bounds__(256) k_wf_trace(SceneView s, Wf w, int par)
     count_rays(w.rays, rays);
 }
 
-template <bool WIDE>
+template <bool WIDE, int SHORT>
 __global__ void __launch_bounds__(256) k_wf_shadow(SceneView s, Wf w, int par)
 {
     const int n = w.cnt[4 + par];
     const int* sq = w.sq + (size_t)par * w.M * w.L;
     uint32_t rays = 0;
     if (!WIDE && s.n_internal > 0) {
-        rays = trace_items_bvh2<true>(
+        rays = trace_items_bvh2<true, ShortStackN<SHORT>>(
             s, n, &w.cnt[9 + 2 * par], w.err,
             [&](int i, float3& o, float3& d, float& tmn, float& tmx, int& skip) {
                 int e = sq[i];
@@ -283,7 +283,7 @@ __device__ __forceinline__ float3 add_visible(const Wf& w, int slot, int mask, f
     return acc;
 }
 
-__global__ void __launch_bounds__(128) k_wf_resolve(SceneView s, Wf w, RenderArgs a, int par)
+__global__ void __launch_bounds__(256) k_wf_resolve(SceneView s, Wf w, RenderArgs a, int par)
 {
     const int n = w.cnt[2 + par];
     const int nq = par ^ 1;
@@ -298,7 +298,7 @@ __global__ void __launch_bounds__(128) k_wf_resolve(SceneView s, Wf w, RenderArg
     }
 }
 
-__global__ void __launch_bounds__(128) k_wf_shade(SceneView s, Wf w, RenderArgs a, int par)
+__global__ void __launch_bounds__(256) k_wf_shade(SceneView s, Wf w, RenderArgs a, int par)
 {
     const int n = w.cnt[par];
     const int nq = par ^ 1;
@@ -479,13 +479,31 @@ __global__ void __launch_bounds__(128) k_wf_shade(SceneView s, Wf w, RenderArgs 
     }
 }
 
+using WfKernel = void (*)(SceneView, Wf, int);
+struct TracePair {
+    WfKernel trace, shadow;
+};
+
+// The trace kernels for the scene's layout and the short-stack depth (binary layout only).
+TracePair trace_pair(bool wide, int short_entries)
+{
+    if (wide) return {k_wf_trace<true, CPT_SHORT_STACK>, k_wf_shadow<true, CPT_SHORT_STACK>};
+    switch (short_entries) {
+    case 8: return {k_wf_trace<false, 8>, k_wf_shadow<false, 8>};
+    case 24: return {k_wf_trace<false, 24>, k_wf_shadow<false, 24>};
+    case 32: return {k_wf_trace<false, 32>, k_wf_shadow<false, 32>};
+    default: return {k_wf_trace<false, 16>, k_wf_shadow<false, 16>};
+    }
+}
+
 // CHUNK iterations: trace, shadow, resolve, shade, with the traversal of the scene's layout.
 // When capturing with a side stream, the shadow kernel is forked onto it so that the two
 // traversal kernels of an iteration overlap (each one's tail fills with the other's warps).
 void enqueue_chunk(const SceneView& view, const Wf& w, const RenderArgs& args, int gt, int bt, int gs, int bs,
-                   cudaStream_t st, const WavefrontTuning* fork)
+                   int short_entries, cudaStream_t st, const WavefrontTuning* fork)
 {
-    const bool wide = view.wide != nullptr;
+    const TracePair kp = trace_pair(view.wide != nullptr, short_entries);
+    const size_t smem = short_stack_bytes(bt, short_entries);
     for (int it = 0; it < CHUNK; ++it) {
         int par = it & 1;
         cudaStream_t ss = st;
@@ -494,14 +512,8 @@ void enqueue_chunk(const SceneView& view, const Wf& w, const RenderArgs& args, i
             cudaStreamWaitEvent(fork->side_stream, fork->fork, 0);
             ss = fork->side_stream;
         }
-        const size_t smem = short_stack_bytes(bt);
-        if (wide) {
-            k_wf_trace<true><<<gt, bt, smem, st>>>(view, w, par);
-            k_wf_shadow<true><<<gt, bt, smem, ss>>>(view, w, par);
-        } else {
-            k_wf_trace<false><<<gt, bt, smem, st>>>(view, w, par);
-            k_wf_shadow<false><<<gt, bt, smem, ss>>>(view, w, par);
-        }
+        kp.trace<<<gt, bt, smem, st>>>(view, w, par);
+        kp.shadow<<<gt, bt, smem, ss>>>(view, w, par);
         if (fork) {
             cudaEventRecord(fork->join, ss);
             cudaStreamWaitEvent(st, fork->join, 0);
@@ -588,7 +600,7 @@ cpt_status launch_render_wavefront(const SceneView& view, const RenderArgs& args
         // Capture CHUNK iterations (4 launches each) once; replay until the queues drain.
         cudaStream_t cs = tune.capture_stream;
         CPT_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
-        enqueue_chunk(view, w, args, gt, bt, gs, bs, cs, tune.side_stream ? &tune : nullptr);
+        enqueue_chunk(view, w, args, gt, bt, gs, bs, tune.short_stack, cs, tune.side_stream ? &tune : nullptr);
         cudaError_t ce = cudaStreamEndCapture(cs, &graph);
         if (ce != cudaSuccess) {
             cudaFreeAsync(base, stream);
@@ -608,7 +620,7 @@ cpt_status launch_render_wavefront(const SceneView& view, const RenderArgs& args
         if (use_graph) {
             CPT_CUDA(cudaGraphLaunch(exec, stream));
         } else {
-            enqueue_chunk(view, w, args, gt, bt, gs, bs, stream, nullptr);
+            enqueue_chunk(view, w, args, gt, bt, gs, bs, tune.short_stack, stream, nullptr);
         }
         add_launches(4 * CHUNK);
         CPT_CUDA(cudaMemcpyAsync(host_cnt, w.cnt, sizeof host_cnt, cudaMemcpyDeviceToHost, stream));
@@ -634,13 +646,22 @@ cpt_status launch_render_wavefront(const SceneView& view, const RenderArgs& args
 namespace cpt {
 
 // Persistent grid sizes: resident blocks per SM (occupancy) x SMs, for the given block sizes.
-cpt_status wavefront_grids(int sm_count, int block_trace, int block_shade, int* grid_trace, int* grid_shade)
+cpt_status wavefront_grids(int sm_count, int block_trace, int block_shade, int short_entries, int* grid_trace,
+                           int* grid_shade)
 {
     int bt = 0, bs = 0;
     int bt2 = 0;
-    const size_t smem = short_stack_bytes(block_trace);
-    CPT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bt, k_wf_trace<true>, block_trace, smem));
-    CPT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bt2, k_wf_trace<false>, block_trace, smem));
+    const size_t smem = short_stack_bytes(block_trace, short_entries);
+    const TracePair wide = trace_pair(true, short_entries), bin = trace_pair(false, short_entries);
+    cudaFuncAttributes fa[3];
+    CPT_CUDA(cudaFuncGetAttributes(&fa[0], wide.trace));
+    CPT_CUDA(cudaFuncGetAttributes(&fa[1], bin.trace));
+    CPT_CUDA(cudaFuncGetAttributes(&fa[2], k_wf_shade));
+    if (block_trace > std::min(fa[0].maxThreadsPerBlock, fa[1].maxThreadsPerBlock) ||
+        block_shade > fa[2].maxThreadsPerBlock)
+        return fail(CPT_ERR_INVALID_ARGUMENT, "wavefront block size above the kernels' limit");
+    CPT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bt, wide.trace, block_trace, smem));
+    CPT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bt2, bin.trace, block_trace, smem));
     bt = std::min(bt, bt2);
     CPT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bs, k_wf_shade, block_shade, 0));
     *grid_trace = std::max(1, bt) * sm_count;

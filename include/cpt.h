@@ -211,10 +211,12 @@ cpt_status cpt_context_destroy(cpt_context* ctx);
  * at most 512).  The defaults are 16 x 8. */
 cpt_status cpt_context_set_render_block(cpt_context* ctx, int block_x, int block_y);
 /* Wavefront integrator tuning: number of path slots (>= 1024; the wavefront size), thread-block
- * sizes of the trace (at most 512) and shade (at most 1024) kernels (multiples of 32), and
- * whether iterations are replayed from a captured CUDA graph.  Defaults: 1,048,576 slots, 128,
- * 128, graphs on. */
+ * sizes of the trace and shade kernels (multiples of 32, at most 256), and whether iterations
+ * are replayed from a captured CUDA graph.  Defaults: 2,097,152 slots, 128, 128, graphs on. */
 cpt_status cpt_context_set_wavefront(cpt_context* ctx, int slots, int block_trace, int block_shade, int use_graph);
+/* Depth of the wavefront trace kernels' shared-memory short stack (8, 16, 24 or 32 entries; the
+ * rest of the traversal stack is in local memory).  Default 16. */
+cpt_status cpt_context_set_short_stack(cpt_context* ctx, int entries);
 /* Traversal layout built by later cpt_lbvh_build / cpt_lbvh_refit calls: 2 = binary nodes with
  * both child boxes per 64-byte node (the default), 8 = the compressed 8-wide BVH (96-byte nodes,
  * 8-bit quantised child boxes, direction-ordered slots). */

@@ -105,11 +105,28 @@ def test_wavefront_matches_megakernel(ctx, name, slots, graph, width):
     try:
         wf = s.render(integrator=abi.INTEGRATOR_WAVEFRONT, **prm)
     finally:
-        ctx.set_wavefront(1 << 20, 128, 128, 1)
+        ctx.set_wavefront(1 << 21, 128, 128, 1)
     exact = (wf["rgb"] == mk["rgb"]).all(-1).mean()
     print(f"wavefront == megakernel on {exact:.5f} of pixels; rays {wf['rays']} vs {mk['rays']}")
     compare(wf["rgb"], mk["rgb"].astype(np.float64), match_frac=0.999, mean_tol=1e-3)
     assert abs(wf["rays"] - mk["rays"]) <= 1e-3 * mk["rays"]
+
+
+def test_wavefront_tuning_limits(ctx):
+    """Block sizes above the kernels' launch bounds are refused before any launch."""
+    for bt, bs in [(512, 128), (128, 512), (96, 48)]:
+        with pytest.raises(Exception):
+            ctx.set_wavefront(1 << 20, bt, bs, 1)
+    with pytest.raises(Exception):
+        ctx.set_render_block(32, 32)
+    ctx.set_wavefront(1 << 21, 256, 256, 1)
+    d = P.cornell_box(width=32)
+    s = api.Scene(ctx, d).init()
+    try:
+        r = s.render(integrator=abi.INTEGRATOR_WAVEFRONT, **config_params("cornell", spp=2))
+    finally:
+        ctx.set_wavefront(1 << 21, 128, 128, 1)
+    assert r["rays"] > 0
 
 
 def test_wavefront_gbuffer_and_rows(ctx):
@@ -158,3 +175,24 @@ def test_gbuffer_and_device_outputs(ctx):
     hitmask = gb[..., 3].cpu().numpy() < 999999.0
     assert hitmask.mean() > 0.9
     assert np.allclose(np.linalg.norm(n[hitmask], axis=-1), 1.0, atol=1e-4)
+
+
+def test_autotuner_cache_reproducible(ctx, tmp_path):
+    """Tuning picks a configuration no slower than the defaults on its probe (margin rule), stores
+    it, and a second tuner with the same cache applies the same choice without timing."""
+    from cudapathtracing_gb300 import autotune
+    d = P.cornell_box(width=48)
+    s = api.Scene(ctx, d).init()
+    prm = config_params("cornell", spp=2)
+    path = str(tmp_path / "tune.json")
+    try:
+        t1 = autotune.Autotuner(ctx, cache_path=path, probe_spp=2, repeats=1)
+        ch = t1.tune(s, prm, abi.INTEGRATOR_WAVEFRONT)
+        assert ch.trials and ch.trials[0]["config"]["slots"] == autotune.DEFAULTS["slots"]
+        assert ch.score >= ch.default_score
+        ch2 = autotune.Autotuner(ctx, cache_path=path).tune(s, prm, abi.INTEGRATOR_WAVEFRONT)
+        assert ch2.knobs == ch.knobs
+        r = s.render(integrator=abi.INTEGRATOR_WAVEFRONT, **prm)
+        assert r["rays"] > 0
+    finally:
+        autotune.Autotuner(ctx, cache_path=path).apply(autotune.DEFAULTS, s)
