@@ -42,6 +42,8 @@ def lib():
             "cpt_context_set_wavefront": (S, [P, C.c_int, C.c_int, C.c_int, C.c_int]),
             "cpt_context_set_bvh_width": (S, [P, C.c_int]),
             "cpt_context_set_short_stack": (S, [P, C.c_int]),
+            "cpt_filter_bilateral": (S, [P, P, P, P, C.c_int32, C.c_int32, C.POINTER(abi.cpt_filter_params), P]),
+            "cpt_filter_temporal": (S, [P, P, P, P, C.POINTER(abi.cpt_camera), C.POINTER(abi.cpt_camera), C.c_float, P]),
             "cpt_ini_load": (S, [C.c_char_p, C.POINTER(P)]),
             "cpt_ini_describe": (S, [P, C.POINTER(abi.cpt_scene_desc)]),
             "cpt_ini_free": (S, [P]),

@@ -69,6 +69,16 @@ class cpt_sphere(C.Structure):
     ]
 
 
+class cpt_filter_params(C.Structure):
+    _fields_ = [("sigma_g", C.c_float), ("sigma_r", C.c_float), ("sigma_n", C.c_float), ("sigma_d", C.c_float),
+                ("radius", C.c_int32)]
+
+
+def filter_params(sigma_g=8.0, sigma_r=5.0, sigma_n=0.1, sigma_d=0.2, radius=16) -> cpt_filter_params:
+    """Defaults of the reference's real-time filter (Window.cu:11-14, Render.cuh:8)."""
+    return cpt_filter_params(sigma_g, sigma_r, sigma_n, sigma_d, radius)
+
+
 class cpt_camera(C.Structure):
     _fields_ = [
         ("width", C.c_int32),

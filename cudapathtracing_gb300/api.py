@@ -9,6 +9,8 @@
   Scene.render(...)               — render (Render.cu:16), STATIC mode
   Scene.trace(rays)               — traverseIterative (BVH.cuh:282) for a batch of rays
   Device.buildBVH(...)            — the device-pointer build on caller-owned buffers
+  filter_bilateral / filter_temporal — gaussianSeparate (Render.cu:356-398) / addPrevious
+                                    (Render.cu:400-420) on device tensors
 
 Everything goes through the C ABI; there is no Python or CPU compute path.
 """
@@ -235,3 +237,28 @@ class Device:
                                           _vp(out["leaf_boxes"]), _vp(scratch), scratch.numel() * scratch.element_size(),
                                           _vp(stream)),
               "cpt_lbvh_build_device")
+
+
+def _cam(c):
+    return c.to_c() if hasattr(c, "to_c") else c
+
+
+def filter_bilateral(ctx: Context, rgb, gbuf, out=None, params: abi.cpt_filter_params | None = None, stream=None):
+    """Joint-bilateral filter of a device image [H, W, 3] float32 with the renderer's G-buffer
+    [H, W, 8] float32; returns `out` (allocated like rgb when None)."""
+    import torch
+    if out is None:
+        out = torch.empty_like(rgb)
+    H, W = int(rgb.shape[0]), int(rgb.shape[1])
+    check(lib().cpt_filter_bilateral(ctx.h, _vp(rgb), _vp(gbuf), _vp(out), W, H,
+                                     C.byref(params) if params is not None else None, _vp(stream)),
+          "cpt_filter_bilateral")
+    return out
+
+
+def filter_temporal(ctx: Context, rgb, prev, gbuf, camera, prev_camera, alpha: float = 0.1, stream=None):
+    """In place: rgb = alpha * rgb + (1 - alpha) * prev at the reprojected pixel (device tensors)."""
+    c, pc = _cam(camera), _cam(prev_camera)
+    check(lib().cpt_filter_temporal(ctx.h, _vp(rgb), _vp(prev), _vp(gbuf), C.byref(c), C.byref(pc), float(alpha),
+                                    _vp(stream)), "cpt_filter_temporal")
+    return rgb

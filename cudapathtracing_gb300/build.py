@@ -19,7 +19,8 @@ NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibility=hidden,-ffp-contract=off",
           "-I" + INCLUDE, "-I" + CSRC]
-SOURCES = ["lbvh.cu", "wide.cu", "trace.cu", "render.cu", "wavefront.cu", "api.cu", "ini.cpp", "lbvh_static.cu"]
+SOURCES = ["lbvh.cu", "wide.cu", "trace.cu", "render.cu", "wavefront.cu", "filter.cu", "api.cu", "ini.cpp",
+           "lbvh_static.cu"]
 
 
 def _compile(src: str, extra: list[str]) -> str:

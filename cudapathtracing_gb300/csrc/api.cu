@@ -416,6 +416,10 @@ cpt_status check_device_error(cpt_scene* s, cudaStream_t stream)
 
 }  // namespace
 
+namespace cpt {
+DevCamera camera_of(const cpt_camera& c) { return make_camera(c); }
+}  // namespace cpt
+
 // ---------------------------------------------------------------- exported API
 CPT_EXPORT int cpt_abi_version(void) { return CPT_ABI_VERSION; }
 
@@ -485,6 +489,27 @@ CPT_EXPORT cpt_status cpt_context_set_bvh_width(cpt_context* ctx, int width)
 }
 
 // Internal tuning knob (the autotuner's setter): render block shape.
+CPT_EXPORT cpt_status cpt_filter_bilateral(cpt_context* ctx, const float* rgb, const float* gbuf, float* out,
+                                           int32_t width, int32_t height, const cpt_filter_params* params,
+                                           void* stream)
+{
+    if (!ctx) return fail(CPT_ERR_INVALID_ARGUMENT, "cpt_filter_bilateral: null context");
+    cpt_filter_params p = {8.0f, 5.0f, 0.1f, 0.2f, 16};   // Window.cu:11-14, Render.cuh:8
+    if (params) p = *params;
+    if (rgb == out) return fail(CPT_ERR_INVALID_ARGUMENT, "cpt_filter_bilateral: out must not alias rgb");
+    CPT_CUDA(cudaSetDevice(ctx->device));
+    return filter_bilateral(rgb, gbuf, out, width, height, p, (cudaStream_t)stream);
+}
+
+CPT_EXPORT cpt_status cpt_filter_temporal(cpt_context* ctx, float* rgb, const float* prev_rgb, const float* gbuf,
+                                          const cpt_camera* camera, const cpt_camera* prev_camera, float alpha,
+                                          void* stream)
+{
+    if (!ctx || !camera || !prev_camera) return fail(CPT_ERR_INVALID_ARGUMENT, "cpt_filter_temporal: null argument");
+    CPT_CUDA(cudaSetDevice(ctx->device));
+    return filter_temporal(rgb, prev_rgb, gbuf, *camera, *prev_camera, alpha, (cudaStream_t)stream);
+}
+
 CPT_EXPORT cpt_status cpt_context_set_short_stack(cpt_context* ctx, int entries)
 {
     if (!ctx || (entries != 8 && entries != 16 && entries != 24 && entries != 32))

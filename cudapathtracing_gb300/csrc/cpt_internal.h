@@ -102,4 +102,11 @@ struct WavefrontTuning {
 cpt_status launch_render_wavefront(const SceneView& view, const RenderArgs& args, cudaStream_t stream,
                                    const WavefrontTuning& tune);
 
+// The reference's joint-bilateral and temporal filters (filter.cu); device buffers.
+DevCamera camera_of(const cpt_camera& c);
+cpt_status filter_bilateral(const float* rgb, const float* gbuf, float* out, int W, int H, const cpt_filter_params& p,
+                            cudaStream_t stream);
+cpt_status filter_temporal(float* rgb, const float* prev, const float* gbuf, const cpt_camera& cam,
+                           const cpt_camera& prev_cam, float alpha, cudaStream_t stream);
+
 }  // namespace cpt

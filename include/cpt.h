@@ -193,6 +193,14 @@ typedef struct cpt_render_stats {
     double ms;          /* device time of the render */
 } cpt_render_stats;
 
+/* Joint-bilateral filter parameters (gaussianSeparate, Render.cu:356-398).  Defaults (NULL
+ * params): sigma_g 8, sigma_r 5, sigma_n 0.1, sigma_d 0.2 (Window.cu:11-14), radius 16
+ * (KERNEL_RADIUS, Render.cuh:8). */
+typedef struct cpt_filter_params {
+    float sigma_g, sigma_r, sigma_n, sigma_d;
+    int32_t radius;
+} cpt_filter_params;
+
 typedef struct cpt_context cpt_context;
 typedef struct cpt_scene cpt_scene;
 
@@ -307,6 +315,20 @@ cpt_status cpt_trace_closest(cpt_scene* scene, const cpt_ray* rays, uint64_t n, 
                              int on_device, void* stream);
 
 /* ---- render --------------------------------------------------------------------- */
+/* The reference's real-time denoiser on device buffers (W*H float3 images, row 0 at the
+ * bottom; gbuf = the renderer's G-buffer, 2 float4 per pixel).
+ * cpt_filter_bilateral: separable joint-bilateral filter, horizontal then vertical pass
+ *   (gaussianSeparate, Render.cu:356-398, as run by main.cu:99-103); out must not alias rgb.
+ * cpt_filter_temporal: rgb = alpha * rgb + (1 - alpha) * prev_rgb at the pixel where the
+ *   previous camera saw this pixel's first hit (addPrevious, Render.cu:400-420;
+ *   Camera::getPrePositionInImg, Camera.cuh:103-132); the reference uses alpha 0.1, or 0.4
+ *   while the camera moves.  The hit position is rebuilt from the G-buffer depth along the
+ *   pixel-centre ray. */
+cpt_status cpt_filter_bilateral(cpt_context* ctx, const float* rgb, const float* gbuf, float* out, int32_t width,
+                                int32_t height, const cpt_filter_params* params, void* stream);
+cpt_status cpt_filter_temporal(cpt_context* ctx, float* rgb, const float* prev_rgb, const float* gbuf,
+                               const cpt_camera* camera, const cpt_camera* prev_camera, float alpha, void* stream);
+
 /* Renders the scene's camera view (render, Render.cu:16-261, STATIC mode). */
 cpt_status cpt_render(cpt_scene* scene, const cpt_render_params* params, const cpt_render_output* out,
                       void* stream, cpt_render_stats* stats);

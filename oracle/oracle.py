@@ -73,6 +73,10 @@ def ref_lib():
         lib.ref_render.argtypes = [P, C.c_int, C.c_uint64, C.c_int, C.c_int, P, P, C.c_int]
         lib.ref_ini_dump.restype = C.c_int
         lib.ref_ini_dump.argtypes = [C.c_char_p, P, C.c_int]
+        if hasattr(lib, "ref_gaussian_separate"):
+            D = C.c_double
+            lib.ref_gaussian_separate.argtypes = [P, P, P, D, D, D, D, C.c_int, C.c_int, C.c_int]
+            lib.ref_add_previous.argtypes = [P, P, P, C.POINTER(abi.cpt_camera), P, P, C.c_int]
         _ref = lib
     return _ref
 
@@ -196,3 +200,34 @@ def ref_ini_dump(path: str) -> np.ndarray:
     buf = np.zeros(65536)
     n = lib.ref_ini_dump(path.encode(), _p(buf), buf.size)
     return buf[:n].copy()
+
+
+def ref_bilateral(rgb, gbuf4, sigma_g=8.0, sigma_r=5.0, sigma_n=0.1, sigma_d=0.2):
+    """The reference's gaussianSeparate run twice as in main.cu:99-103 (horizontal pass, copyPic,
+    vertical pass), on FP64 copies; radius is the compiled KERNEL_RADIUS (16)."""
+    L = ref_lib()
+    if L is None:
+        raise RuntimeError("oracle/_ref was not built (the reference is not mounted here)")
+    H, W, _ = rgb.shape
+    pic = np.ascontiguousarray(rgb, dtype=np.float64).copy()
+    before = pic.copy()
+    g = np.ascontiguousarray(gbuf4, dtype=np.float64)
+    L.ref_gaussian_separate(_p(pic), _p(before), _p(g), sigma_g, sigma_r, sigma_n, sigma_d, W, H, 1)
+    before = pic.copy()
+    L.ref_gaussian_separate(_p(pic), _p(before), _p(g), sigma_g, sigma_r, sigma_n, sigma_d, W, H, 0)
+    return pic
+
+
+def ref_temporal(rgb, prev, gpos, camera, pre_from, pre_at, moving):
+    """The reference's addPrevious over the image (alpha 0.1, or 0.4 when moving)."""
+    L = ref_lib()
+    if L is None:
+        raise RuntimeError("oracle/_ref was not built (the reference is not mounted here)")
+    pic = np.ascontiguousarray(rgb, dtype=np.float64).copy()
+    pv = np.ascontiguousarray(prev, dtype=np.float64)
+    gp = np.ascontiguousarray(gpos, dtype=np.float64)
+    pf = np.asarray(pre_from, dtype=np.float64)
+    pa = np.asarray(pre_at, dtype=np.float64)
+    cam = camera.to_c() if hasattr(camera, "to_c") else camera
+    L.ref_add_previous(_p(pic), _p(pv), _p(gp), C.byref(cam), _p(pf), _p(pa), int(moving))
+    return pic

@@ -347,3 +347,38 @@ REF_API int ref_ini_dump(const char* path, double* out, int cap)
     if (n <= cap) std::memcpy(out, v.data(), sizeof(double) * n);
     return n;
 }
+
+// The reference's real-time filters run as plain loops over their own kernels
+// (gaussianSeparate, Render.cu:356-398; addPrevious, Render.cu:400-420).  Images are W*H
+// double3; gbuf4 is W*H double4 (normal, depth); gpos W*H double3 (INF on a miss).
+REF_API void ref_gaussian_separate(double* pic, double* before, const double* gbuf4, double sg, double sr, double sn,
+                                   double sd, int W, int H, int horizontal)
+{
+    blockDim = dim3(1, 1, 1);
+    threadIdx = make_uint3(0, 0, 0);
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            blockIdx = make_uint3(x, y, 0);
+            gaussianSeparate((double3*)pic, (double3*)before, (double4*)gbuf4, sg, sr, sn, sd, W, H, horizontal != 0);
+        }
+}
+
+REF_API void ref_add_previous(double* pic, double* prev, double* gpos, const cpt_camera* cur, const double* pre_from,
+                              const double* pre_at, int moving)
+{
+    Camera* cam = (Camera*)std::malloc(sizeof(Camera));
+    new (cam) Camera(cur->width, cur->aspect_ratio, d3(cur->background), d3(cur->look_from), d3(cur->look_at),
+                     cur->vfov_deg, std::string());
+    cam->preLookFrom = make_double3(pre_from[0], pre_from[1], pre_from[2]);
+    cam->preLookAt = make_double3(pre_at[0], pre_at[1], pre_at[2]);
+    cam->isMoving = moving != 0;
+    blockDim = dim3(1, 1, 1);
+    threadIdx = make_uint3(0, 0, 0);
+    for (int y = 0; y < cam->height; ++y)
+        for (int x = 0; x < cam->width; ++x) {
+            blockIdx = make_uint3(x, y, 0);
+            addPrevious((double3*)pic, (double3*)prev, (double3*)gpos, cam, cam->width, cam->height);
+        }
+    cam->~Camera();
+    std::free(cam);
+}
