@@ -43,6 +43,15 @@ def lib():
             "cpt_context_set_bvh_width": (S, [P, C.c_int]),
             "cpt_context_set_short_stack": (S, [P, C.c_int]),
             "cpt_filter_bilateral": (S, [P, P, P, P, C.c_int32, C.c_int32, C.POINTER(abi.cpt_filter_params), P]),
+            "cpt_denoiser_create": (S, [C.c_int, C.c_uint64, C.POINTER(P)]),
+            "cpt_denoiser_destroy": (S, [P]),
+            "cpt_denoiser_num_params": (C.c_uint64, [P]),
+            "cpt_denoiser_get_params": (S, [P, P]),
+            "cpt_denoiser_set_params": (S, [P, P]),
+            "cpt_denoiser_get_grads": (S, [P, P]),
+            "cpt_denoiser_train_step": (S, [P, C.c_int32, C.c_int32, C.c_int32, P, P, P, C.c_float, C.c_int32,
+                                            C.POINTER(C.c_float), P]),
+            "cpt_denoise": (S, [P, C.c_int32, C.c_int32, C.c_int32, P, P, P, P]),
             "cpt_filter_temporal": (S, [P, P, P, P, C.POINTER(abi.cpt_camera), C.POINTER(abi.cpt_camera), C.c_float, P]),
             "cpt_ini_load": (S, [C.c_char_p, C.POINTER(P)]),
             "cpt_ini_describe": (S, [P, C.POINTER(abi.cpt_scene_desc)]),

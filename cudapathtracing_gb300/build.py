@@ -19,7 +19,7 @@ NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibility=hidden,-ffp-contract=off",
           "-I" + INCLUDE, "-I" + CSRC]
-SOURCES = ["lbvh.cu", "wide.cu", "trace.cu", "render.cu", "wavefront.cu", "filter.cu", "api.cu", "ini.cpp",
+SOURCES = ["lbvh.cu", "wide.cu", "trace.cu", "render.cu", "wavefront.cu", "filter.cu", "kpcn.cu", "api.cu", "ini.cpp",
            "lbvh_static.cu"]
 
 

@@ -329,6 +329,28 @@ cpt_status cpt_filter_bilateral(cpt_context* ctx, const float* rgb, const float*
 cpt_status cpt_filter_temporal(cpt_context* ctx, float* rgb, const float* prev_rgb, const float* gbuf,
                                const cpt_camera* camera, const cpt_camera* prev_camera, float alpha, void* stream);
 
+/* ---- learned denoiser (no counterpart in the reference) --------------------------------
+ * Kernel-predicting U-Net (5 levels, 32-64-96-128-160 channels, 3x3 convolutions, a predicted
+ * 5x5 filter per pixel applied to the noisy radiance), trained and run on the library's own
+ * BF16 tensor-core kernels with FP32 accumulation.  Parameters are one FP32 array
+ * (cpt_denoiser_num_params floats: per convolution W[9][cin][cout] then b[cout]).
+ * Images are device buffers: rgb and target [n][h][w][3] f32, gbuf [n][h][w][8] f32 (the
+ * renderer's G-buffer).  Training crops must be multiples of 16; cpt_denoise takes any size. */
+typedef struct cpt_denoiser cpt_denoiser;
+cpt_status cpt_denoiser_create(int device, uint64_t seed, cpt_denoiser** out);
+cpt_status cpt_denoiser_destroy(cpt_denoiser* d);
+uint64_t cpt_denoiser_num_params(const cpt_denoiser* d);
+cpt_status cpt_denoiser_get_params(cpt_denoiser* d, float* host_out);
+cpt_status cpt_denoiser_set_params(cpt_denoiser* d, const float* host_in); /* also resets Adam */
+cpt_status cpt_denoiser_get_grads(cpt_denoiser* d, float* host_out);      /* of the last train step */
+/* One step: forward, loss = mean |log(1 + out) - log(1 + target)|, backward, and (update != 0)
+ * an Adam step with learning rate lr.  *loss (optional) receives the loss before the update. */
+cpt_status cpt_denoiser_train_step(cpt_denoiser* d, int32_t n, int32_t h, int32_t w, const float* rgb,
+                                   const float* gbuf, const float* target, float lr, int32_t update, float* loss,
+                                   void* stream);
+cpt_status cpt_denoise(cpt_denoiser* d, int32_t n, int32_t h, int32_t w, const float* rgb, const float* gbuf,
+                       float* out, void* stream);
+
 /* Renders the scene's camera view (render, Render.cu:16-261, STATIC mode). */
 cpt_status cpt_render(cpt_scene* scene, const cpt_render_params* params, const cpt_render_output* out,
                       void* stream, cpt_render_stats* stats);
