@@ -49,6 +49,7 @@ def lib():
             "cpt_denoiser_get_params": (S, [P, P]),
             "cpt_denoiser_set_params": (S, [P, P]),
             "cpt_denoiser_get_grads": (S, [P, P]),
+            "cpt_denoiser_export": (S, [P, C.c_char_p, P, C.c_uint64, C.POINTER(C.c_uint64)]),
             "cpt_denoiser_train_step": (S, [P, C.c_int32, C.c_int32, C.c_int32, P, P, P, C.c_float, C.c_int32,
                                             C.POINTER(C.c_float), P]),
             "cpt_denoise": (S, [P, C.c_int32, C.c_int32, C.c_int32, P, P, P, P]),

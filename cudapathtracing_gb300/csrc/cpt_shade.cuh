@@ -169,6 +169,11 @@ __device__ __forceinline__ float3 bsdf_eval(const Surf& sf, float3 ray_d, float3
         float F = fresnel_dielectric(n, V, rr);
         return (reflect ? F : 1.0f - F) * sf.color / ct;
     } else if (!reflect) {
+        // Only the rough dielectric transmits.  For the conductor this branch is reached only by
+        // a grazing direction whose cosine changes sign when it is renormalised in FP32 (the
+        // caller saw it above the surface); it has no transmission lobe (and no sampled
+        // microfacet normal), so it contributes nothing.
+        if (sf.type != M_ROUGH) return f3(0.f, 0.f, 0.f);
         float rr = sf.front ? sf.eta : (1.0f / sf.eta);
         float D = ggx_D(sf.ax, sf.ay, n, sf.wm);
         if (dot3(sf.wm, V) < 0.f) V = -V;

@@ -345,7 +345,7 @@ __global__ void k_upsample_back(Geo gc, View gout, View gin)
 }
 
 // ------------------------------------------------------------------ features and kernel apply
-__device__ __forceinline__ float log_lum(float3 c) { return logf(1.0f + fmaxf(0.f, 0.2126f * c.x + 0.7152f * c.y + 0.0722f * c.z)); }
+__device__ __forceinline__ float log_lum(float3 c) { return log1pf(fmaxf(0.f, 0.2126f * c.x + 0.7152f * c.y + 0.0722f * c.z)); }
 
 // Images: rgb [N][Hr][Wr][3] f32, gbuf [N][Hr][Wr][8] f32 (renderer layout) -> features
 // [N][H][W][IN_CH] bf16 and radiance [N][H][W][3] f32 on the padded geometry g.
@@ -363,9 +363,9 @@ __global__ void k_features(Geo g, int Hr, int Wr, const float* __restrict__ rgb,
             const size_t o = ((size_t)b * Hr + y) * Wr + x;
             r = f3(fmaxf(rgb[3 * o], 0.f), fmaxf(rgb[3 * o + 1], 0.f), fmaxf(rgb[3 * o + 2], 0.f));
             const float* gb = gbuf + 8 * o;
-            f[0] = logf(1.f + r.x);
-            f[1] = logf(1.f + r.y);
-            f[2] = logf(1.f + r.z);
+            f[0] = log1pf(r.x);
+            f[1] = log1pf(r.y);
+            f[2] = log1pf(r.z);
             f[3] = gb[4];
             f[4] = gb[5];
             f[5] = gb[6];
@@ -385,17 +385,18 @@ __global__ void k_features(Geo g, int Hr, int Wr, const float* __restrict__ rgb,
             f[7] = ny;
             const float d = gb[3];
             f[8] = d >= CPT_INF_F ? 1.f : d / (1.f + d);
-            float m = 0.f, m2 = 0.f;
-            for (int dy = -1; dy <= 1; ++dy)
-                for (int dx = -1; dx <= 1; ++dx) {
-                    const int xx = min(max(x + dx, 0), Wr - 1), yy = min(max(y + dy, 0), Hr - 1);
-                    const size_t q = ((size_t)b * Hr + yy) * Wr + xx;
-                    const float l = log_lum(f3(rgb[3 * q], rgb[3 * q + 1], rgb[3 * q + 2]));
-                    m += l;
-                    m2 += l * l;
-                }
+            // 3x3 variance, two-pass (no cancellation of m2 - m^2 in FP32)
+            float l9[9], m = 0.f;
+            for (int k = 0; k < 9; ++k) {
+                const int xx = min(max(x + k % 3 - 1, 0), Wr - 1), yy = min(max(y + k / 3 - 1, 0), Hr - 1);
+                const size_t q = ((size_t)b * Hr + yy) * Wr + xx;
+                l9[k] = log_lum(f3(rgb[3 * q], rgb[3 * q + 1], rgb[3 * q + 2]));
+                m += l9[k];
+            }
             m /= 9.f;
-            f[9] = fmaxf(m2 / 9.f - m * m, 0.f);
+            float var = 0.f;
+            for (int k = 0; k < 9; ++k) var += (l9[k] - m) * (l9[k] - m);
+            f[9] = var / 9.f;
         }
         __nv_bfloat16* fo = feat + p * IN_CH;
 #pragma unroll
@@ -480,7 +481,7 @@ __global__ void k_loss(Geo g, int Hr, int Wr, const float* __restrict__ out, con
             if (real) {
                 const float o = out[3 * p + c];
                 const float t = target[(((size_t)b * Hr + y) * Wr + x) * 3 + c];
-                const float lo = logf(1.f + fmaxf(o, 0.f)), lt = logf(1.f + fmaxf(t, 0.f));
+                const float lo = log1pf(fmaxf(o, 0.f)), lt = log1pf(fmaxf(t, 0.f));
                 const float d = lo - lt;
                 s += fabsf(d);
                 gr = o > 0.f ? scale * (d > 0.f ? 1.f : (d < 0.f ? -1.f : 0.f)) / (1.f + o) : 0.f;
@@ -926,6 +927,59 @@ CPT_EXPORT cpt_status cpt_denoiser_get_grads(cpt_denoiser* d, float* host)
     CPT_CUDA(cudaSetDevice(d->net.device));
     CPT_CUDA(cudaMemcpy(host, d->net.gw, d->net.n_params * sizeof(float), cudaMemcpyDeviceToHost));
     return CPT_OK;
+}
+
+// Copies one internal tensor of the last forward/backward pass (for tests): activations as BF16
+// values widened to float, gradients as float.  *count receives the number of elements.
+CPT_EXPORT cpt_status cpt_denoiser_export(cpt_denoiser* d, const char* name, float* host, uint64_t capacity,
+                                          uint64_t* count)
+{
+    if (!d || !name || !count) return fail(CPT_ERR_INVALID_ARGUMENT, "cpt_denoiser_export: null argument");
+    kpcn::Net& n = d->net;
+    if (!n.arena) return fail(CPT_ERR_INVALID_ARGUMENT, "cpt_denoiser_export: nothing computed yet");
+    const long* P = n.P;
+    struct T {
+        const char* name;
+        const void* ptr;
+        long elems;
+        bool b16;
+    } table[] = {
+        {"X0", n.X0, P[0] * kpcn::IN_CH, true}, {"A0a", n.A0a, P[0] * 32, true}, {"cat0", n.cat0, P[0] * 96, true},
+        {"p1", n.p1, P[1] * 32, true}, {"A1a", n.A1a, P[1] * 64, true}, {"cat1", n.cat1, P[1] * 160, true},
+        {"p2", n.p2, P[2] * 64, true}, {"A2a", n.A2a, P[2] * 96, true}, {"cat2", n.cat2, P[2] * 224, true},
+        {"p3", n.p3, P[3] * 96, true}, {"A3a", n.A3a, P[3] * 128, true}, {"cat3", n.cat3, P[3] * 288, true},
+        {"p4", n.p4, P[4] * 128, true}, {"A4a", n.A4a, P[4] * 160, true}, {"A4b", n.A4b, P[4] * 160, true},
+        {"D3a", n.D3a, P[3] * 128, true}, {"D3b", n.D3b, P[3] * 128, true}, {"D2a", n.D2a, P[2] * 96, true},
+        {"D2b", n.D2b, P[2] * 96, true}, {"D1a", n.D1a, P[1] * 64, true}, {"D1b", n.D1b, P[1] * 64, true},
+        {"D0a", n.D0a, P[0] * 32, true}, {"D0b", n.D0b, P[0] * 32, true},
+        {"logits", n.logits, P[0] * kpcn::OUT_CH, false}, {"out", n.out, P[0] * 3, false},
+        {"G_D0b", n.G_D0b, P[0] * 32, false}, {"G_D0a", n.G_D0a, P[0] * 32, false},
+        {"G_cat0", n.G_cat0, P[0] * 96, false}, {"G_D1b", n.G_D1b, P[1] * 64, false},
+        {"G_cat1", n.G_cat1, P[1] * 160, false}, {"G_D2b", n.G_D2b, P[2] * 96, false},
+        {"G_cat2", n.G_cat2, P[2] * 224, false}, {"G_D3b", n.G_D3b, P[3] * 128, false},
+        {"G_cat3", n.G_cat3, P[3] * 288, false}, {"G_A4b", n.G_A4b, P[4] * 160, false},
+        {"G_p4", n.G_p4, P[4] * 128, false}, {"G_p3", n.G_p3, P[3] * 96, false}, {"G_p2", n.G_p2, P[2] * 64, false},
+        {"G_p1", n.G_p1, P[1] * 32, false}, {"G_A0a", n.G_A0a, P[0] * 32, false},
+    };
+    for (const T& t : table) {
+        if (std::strcmp(t.name, name) != 0) continue;
+        *count = (uint64_t)t.elems;
+        if (!host || capacity < (uint64_t)t.elems) return CPT_OK;
+        CPT_CUDA(cudaSetDevice(n.device));
+        CPT_CUDA(cudaDeviceSynchronize());
+        if (t.b16) {
+            std::vector<uint16_t> raw(t.elems);
+            CPT_CUDA(cudaMemcpy(raw.data(), t.ptr, t.elems * 2, cudaMemcpyDeviceToHost));
+            for (long i = 0; i < t.elems; ++i) {
+                uint32_t u = (uint32_t)raw[i] << 16;
+                std::memcpy(&host[i], &u, 4);
+            }
+        } else {
+            CPT_CUDA(cudaMemcpy(host, t.ptr, t.elems * 4, cudaMemcpyDeviceToHost));
+        }
+        return CPT_OK;
+    }
+    return fail(CPT_ERR_INVALID_ARGUMENT, "cpt_denoiser_export: unknown tensor");
 }
 
 CPT_EXPORT cpt_status cpt_denoiser_train_step(cpt_denoiser* d, int32_t n, int32_t h, int32_t w, const float* rgb,

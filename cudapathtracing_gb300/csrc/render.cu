@@ -145,7 +145,7 @@ __device__ PixelResult pixel_reference(const SceneView& s, int i, int j, const R
             float3 dir;
             float pdf;
             bsdf_sample(sf, d, dir, pdf, r1, r2, r3);
-            if (pdf <= 0.f) break;
+            if (!(pdf > 0.f)) break;   // also ends the path on a NaN pdf (0/0 at a grazing direction)
             float3 fr = bsdf_eval(sf, d, dir);
             thr = thr * (fr * fabsf(dot3(dir, sf.normal)) / pdf / P);
             o = sf.pos;
@@ -268,7 +268,7 @@ __device__ PixelResult pixel_config(const SceneView& s, int i, int j, const Rend
             float3 dir;
             float pdf;
             bsdf_sample(sf, d, dir, pdf, r1, r2, r3);
-            if (pdf <= 0.f) break;
+            if (!(pdf > 0.f)) break;   // also ends the path on a NaN pdf (0/0 at a grazing direction)
             float3 fr = bsdf_eval(sf, d, dir);
             thr = thr * (fr * fabsf(dot3(dir, sf.normal)) / pdf / P);
             o = sf.pos;

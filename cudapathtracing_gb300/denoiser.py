@@ -69,6 +69,15 @@ class Denoiser:
         check(lib().cpt_denoiser_get_grads(self.h, a.ctypes.data_as(C.c_void_p)), "cpt_denoiser_get_grads")
         return a
 
+    def export(self, name: str) -> np.ndarray:
+        """An internal tensor of the last pass, flattened (see cpt_denoiser_export)."""
+        cnt = C.c_uint64()
+        check(lib().cpt_denoiser_export(self.h, name.encode(), None, 0, C.byref(cnt)), "cpt_denoiser_export")
+        a = np.empty(cnt.value, dtype=np.float32)
+        check(lib().cpt_denoiser_export(self.h, name.encode(), a.ctypes.data_as(C.c_void_p), cnt.value, C.byref(cnt)),
+              "cpt_denoiser_export")
+        return a
+
     def train_step(self, rgb, gbuf, target, lr: float = 1e-3, update: bool = True, stream=None) -> float:
         n, h, w = int(rgb.shape[0]), int(rgb.shape[1]), int(rgb.shape[2])
         loss = C.c_float()

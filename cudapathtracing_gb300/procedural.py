@@ -332,3 +332,66 @@ def spheres_scene(num_spheres: int = 200, level: int = 5, width: int = 1920, see
     d.bounds_max = tuple(pts.max(0))
     d.camera = Camera(width, 16.0 / 9.0, (0.0, 7.0, 24.0), (0.0, 1.0, 0.0), 40.0, (0.05, 0.06, 0.08))
     return d
+
+
+def random_scene(seed: int, width: int = 256, aspect: float = 1.0, max_level: int = 6,
+                 max_objects: int = 6) -> SceneDesc:
+    """A seeded scene of the icosphere-microbench type (denoiser training data and serving jobs).
+
+    All draws come in order from one PCG32 stream (seed, stream 0): the number of displaced
+    icospheres in [1, max_objects]; per sphere a subdivision level in [4, max_level], radius
+    [0.4, 1.4], position x, z in [-4, 4] resting on the ground, a noise offset, a colour, and a
+    material (Lambertian / GGX with roughness U[0.05, 0.8] / dielectric IOR 1.5, equal odds);
+    with odds 0.3 a homogeneous volume box (sigma_t U[0.3, 1.0], albedo 0.8); one or two area
+    lights 8-12 units up (side 2-4, radiance 8-20); a camera orbiting at distance 8-12, height
+    1.5-6, looking at (0, 0.8, 0) with a 35-50 degree field of view.  Ground: [-30, 30]^2 at y = 0."""
+    g = PCG32Streams(seed, np.array([0], dtype=np.uint64))
+    u = lambda: float(g.uniform()[0])
+    d = SceneDesc()
+    ground = d.add_material((0.3 + 0.5 * u(), 0.3 + 0.5 * u(), 0.3 + 0.5 * u()), 0.5, 0.5, M_LAMBERTIAN)
+    parts = [np.array([[-30, 0, -30, -30, 0, 30, 30, 0, -30], [30, 0, -30, -30, 0, 30, 30, 0, 30]], np.float64)]
+    mats = [ground, ground]
+    n_obj = 1 + min(int(u() * max_objects), max_objects - 1)
+    for k in range(n_obj):
+        level = 4 + min(int(u() * (max_level - 3)), max_level - 4)
+        rad = 0.4 + u()
+        x, z = u() * 8.0 - 4.0, u() * 8.0 - 4.0
+        off = (u() * 16.0, u() * 16.0, u() * 16.0)
+        col = (0.15 + 0.8 * u(), 0.15 + 0.8 * u(), 0.15 + 0.8 * u())
+        kind = min(int(u() * 3), 2)
+        rough = 0.05 + 0.75 * u()
+        if kind == 0:
+            m = d.add_material(col, 0.5, 0.5, M_LAMBERTIAN)
+        elif kind == 1:
+            m = d.add_material(col, rough, rough, M_OPAQUE)
+        else:
+            m = d.add_material((1.0, 1.0, 1.0), 0.5, 0.5, M_SPECULAR_DIELECTRIC, eta=1.5)
+        t = displaced_icosphere(level, 0.1, 0, off) * rad
+        t = t.reshape(-1, 3, 3) + np.array([x, rad, z])
+        parts.append(t.reshape(-1, 9))
+        mats.extend([m] * t.shape[0])
+    if u() < 0.3:
+        vol = d.add_material((1.0, 1.0, 1.0), 0.5, 0.5, M_VOLUME, sigma_t=0.3 + 0.7 * u(), albedo=0.8)
+        c = (u() * 6.0 - 3.0, 1.0, u() * 6.0 - 3.0)
+        for q in _box_quads(c, (2.0, 2.0, 2.0), 360.0 * u()):
+            for t in _quad(*q):
+                parts.append(np.asarray(t, np.float64)[None, :])
+                mats.append(vol)
+    d.tri_vertices = np.concatenate(parts, 0).astype(np.float32)
+    d.tri_material = np.array(mats, np.uint32)
+    for _ in range(1 + int(u() < 0.5)):
+        side = 2.0 + 2.0 * u()
+        c = (u() * 10.0 - 5.0, 8.0 + 4.0 * u(), u() * 10.0 - 5.0)
+        e = 8.0 + 12.0 * u()
+        d.lights.append(dict(center=c, normal=(0.0, -1.0, 0.0), width=side, height=side, color=(e, e, e),
+                             visible=1))
+    ang = 2.0 * math.pi * u()
+    dist = 8.0 + 4.0 * u()
+    h = 1.5 + 4.5 * u()
+    fov = 35.0 + 15.0 * u()
+    pts = d.tri_vertices.reshape(-1, 3).astype(np.float64)
+    d.bounds_min = tuple(pts.min(0))
+    d.bounds_max = tuple(pts.max(0))
+    d.camera = Camera(width, aspect, (dist * math.sin(ang), h, dist * math.cos(ang)), (0.0, 0.8, 0.0), fov,
+                      (0.04 + 0.06 * u(), 0.05 + 0.06 * u(), 0.08 + 0.06 * u()))
+    return d

@@ -66,17 +66,14 @@ def features(rgb, gbuf, H, W, rnd=bf16):
     d = gbuf[..., 3].astype(np.float64)
     X[:, :Hr, :Wr, 8] = np.where(d >= INF, 1.0, d / (1.0 + d))
     lum = np.log1p(np.maximum(0.0, 0.2126 * rgb[..., 0] + 0.7152 * rgb[..., 1] + 0.0722 * rgb[..., 2]))
-    m = np.zeros_like(lum)
-    m2 = np.zeros_like(lum)
+    nb = []
     for dy in (-1, 0, 1):
         for dx in (-1, 0, 1):
             yy = np.clip(np.arange(Hr) + dy, 0, Hr - 1)
             xx = np.clip(np.arange(Wr) + dx, 0, Wr - 1)
-            l = lum[:, yy][:, :, xx]
-            m += l
-            m2 += l * l
-    m /= 9.0
-    X[:, :Hr, :Wr, 9] = np.maximum(m2 / 9.0 - m * m, 0.0)
+            nb.append(lum[:, yy][:, :, xx])
+    nb = np.stack(nb)
+    X[:, :Hr, :Wr, 9] = ((nb - nb.mean(0)) ** 2).mean(0)
     return rnd(X), rad
 
 
@@ -187,6 +184,48 @@ class Net:
         self.a, self.wts, self.nb, self.out = a, wts, nb, out
         return out[:, :Hr, :Wr]
 
+    def use_activations(self, ex, rgb, gbuf):
+        """Replaces the forward activations by another implementation's (ex: name -> flat array,
+        as cpt_denoiser_export names them), so that backward() checks that implementation's
+        backward pass on its own forward values (identical ReLU masks) instead of re-deriving
+        them: in a deep BF16 network the two forward passes drift apart by rounding, and a
+        pre-activation within a rounding step of zero can take the other side of the ReLU."""
+        N, Hr, Wr, _ = rgb.shape
+        H, W = (Hr + 15) // 16 * 16, (Wr + 15) // 16 * 16
+        self.dims = (N, H, W, Hr, Wr)
+        chans = {"X0": 32, "A0a": 32, "cat0": 96, "p1": 32, "A1a": 64, "cat1": 160, "p2": 64, "A2a": 96,
+                 "cat2": 224, "p3": 96, "A3a": 128, "cat3": 288, "p4": 128, "A4a": 160, "A4b": 160, "D3a": 128,
+                 "D3b": 128, "D2a": 96, "D2b": 96, "D1a": 64, "D1b": 64, "D0a": 32, "D0b": 32, "logits": 32}
+        level = {"X0": 0, "A0a": 0, "cat0": 0, "p1": 1, "A1a": 1, "cat1": 1, "p2": 2, "A2a": 2, "cat2": 2, "p3": 3,
+                 "A3a": 3, "cat3": 3, "p4": 4, "A4a": 4, "A4b": 4, "D3a": 3, "D3b": 3, "D2a": 2, "D2b": 2, "D1a": 1,
+                 "D1b": 1, "D0a": 0, "D0b": 0, "logits": 0}
+        a = {k: np.asarray(ex[k], np.float64).reshape(N, H >> level[k], W >> level[k], c) for k, c in chans.items()}
+        a["A0b"], a["A1b"] = a["cat0"][..., 64:], a["cat1"][..., 96:]
+        a["A2b"], a["A3b"] = a["cat2"][..., 128:], a["cat3"][..., 160:]
+        self.a = a
+        _, rad = features(rgb, gbuf, H, W, self.r)
+        logits = a["logits"][..., :KS * KS]
+        e = np.exp(logits - logits.max(-1, keepdims=True))
+        self.wts = e / e.sum(-1, keepdims=True)
+        self.nb = rad.reshape(N, H * W, 3)[:, kernel_offsets(H, W, Hr, Wr)]
+        self.out = (self.wts[..., None] * self.nb).sum(-2)
+
+    def layer_outputs(self):
+        """Each convolution recomputed from this Net's stored inputs: {output name: (value, layer)}."""
+        a, w, b, R = self.a, self.w, self.b, self.r
+        cv = lambda i, x: R(np.maximum(conv(x, w[i], b[i]), 0.0))
+        pairs = [("A0a", 0, "X0"), ("A0b", 1, "A0a"), ("A1a", 2, "p1"), ("A1b", 3, "A1a"), ("A2a", 4, "p2"),
+                 ("A2b", 5, "A2a"), ("A3a", 6, "p3"), ("A3b", 7, "A3a"), ("A4a", 8, "p4"), ("A4b", 9, "A4a"),
+                 ("D3a", 10, "cat3"), ("D3b", 11, "D3a"), ("D2a", 12, "cat2"), ("D2b", 13, "D2a"),
+                 ("D1a", 14, "cat1"), ("D1b", 15, "D1a"), ("D0a", 16, "cat0"), ("D0b", 17, "D0a")]
+        out = {name: (cv(i, a[src]), i) for name, i, src in pairs}
+        out["logits"] = (conv(a["D0b"], w[18], b[18]), 18)
+        out["p1"] = (R(pool(a["A0b"])), -1)
+        out["p2"] = (R(pool(a["A1b"])), -1)
+        out["p3"] = (R(pool(a["A2b"])), -1)
+        out["p4"] = (R(pool(a["A3b"])), -1)
+        return out
+
     def loss(self, target):
         N, H, W, Hr, Wr = self.dims
         o = self.out[:, :Hr, :Wr]
@@ -213,32 +252,37 @@ class Net:
             return conv_dgrad(dz, w[i]) if need_dx else None
 
         rb = lambda g, act: R(g * (act > 0))
-        g = layer(18, a["D0b"], dz)
-        g = layer(17, a["D0a"], rb(g, a["D0b"]))
+        G = self.g = {}   # activation gradients, named as the library's cpt_denoiser_export
+        g = G["G_D0b"] = layer(18, a["D0b"], dz)
+        g = G["G_D0a"] = layer(17, a["D0a"], rb(g, a["D0b"]))
         gcat0 = layer(16, a["cat0"], rb(g, a["D0a"]))
-        g = up_back(gcat0[..., :64])
+        g = G["G_D1b"] = up_back(gcat0[..., :64])
         g = layer(15, a["D1a"], rb(g, a["D1b"]))
         gcat1 = layer(14, a["cat1"], rb(g, a["D1a"]))
-        g = up_back(gcat1[..., :96])
+        g = G["G_D2b"] = up_back(gcat1[..., :96])
         g = layer(13, a["D2a"], rb(g, a["D2b"]))
         gcat2 = layer(12, a["cat2"], rb(g, a["D2a"]))
-        g = up_back(gcat2[..., :128])
+        g = G["G_D3b"] = up_back(gcat2[..., :128])
         g = layer(11, a["D3a"], rb(g, a["D3b"]))
         gcat3 = layer(10, a["cat3"], rb(g, a["D3a"]))
-        g = up_back(gcat3[..., :160])
+        g = G["G_A4b"] = up_back(gcat3[..., :160])
         g = layer(9, a["A4a"], rb(g, a["A4b"]))
-        g = layer(8, a["p4"], rb(g, a["A4a"]))
+        g = G["G_p4"] = layer(8, a["p4"], rb(g, a["A4a"]))
         g = gcat3[..., 160:] + pool_back(g)
+        G["G_cat3"] = np.concatenate([gcat3[..., :160], g], -1)
         g = layer(7, a["A3a"], rb(g, a["A3b"]))
-        g = layer(6, a["p3"], rb(g, a["A3a"]))
+        g = G["G_p3"] = layer(6, a["p3"], rb(g, a["A3a"]))
         g = gcat2[..., 128:] + pool_back(g)
+        G["G_cat2"] = np.concatenate([gcat2[..., :128], g], -1)
         g = layer(5, a["A2a"], rb(g, a["A2b"]))
-        g = layer(4, a["p2"], rb(g, a["A2a"]))
+        g = G["G_p2"] = layer(4, a["p2"], rb(g, a["A2a"]))
         g = gcat1[..., 96:] + pool_back(g)
+        G["G_cat1"] = np.concatenate([gcat1[..., :96], g], -1)
         g = layer(3, a["A1a"], rb(g, a["A1b"]))
-        g = layer(2, a["p1"], rb(g, a["A1a"]))
+        g = G["G_p1"] = layer(2, a["p1"], rb(g, a["A1a"]))
         g = gcat0[..., 64:] + pool_back(g)
-        g = layer(1, a["A0a"], rb(g, a["A0b"]))
+        G["G_cat0"] = np.concatenate([gcat0[..., :64], g], -1)
+        g = G["G_A0a"] = layer(1, a["A0a"], rb(g, a["A0b"]))
         layer(0, a["X0"], rb(g, a["A0a"]), need_dx=False)
         flat = []
         for i in range(19):

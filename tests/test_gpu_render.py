@@ -29,6 +29,7 @@ def compare(gpu_rgb, ref_rgb, match_frac=MATCH_FRAC, mean_tol=MEAN_TOL):
     r = ref_rgb
     ok = (np.abs(g - r) <= PIX_TOL * np.maximum(1.0, np.abs(r))).all(-1)
     frac = ok.mean()
+    assert np.isfinite(g).all(), "non-finite pixels"
     mrel = abs(g.mean() - r.mean()) / max(r.mean(), 1e-9)
     print(f"match {frac:.5f}  mean rel {mrel:.2e}  max abs {np.abs(g - r).max():.3e}")
     assert frac >= match_frac, frac
