@@ -184,6 +184,28 @@ def run_reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
+def denoise_eval(ctx, scenes=(0, 1, 2), size=512):
+    """Held-out seeded scenes at size x size: the smallest spp (of a fixed ladder) at which the
+    plain render, and the denoised render, reach display-space RMSE 0.01 against an 8192-spp
+    render of another seed, and their device times (render, plus denoiser)."""
+    from cudapathtracing_gb300 import procedural as P, training as T
+    from cudapathtracing_gb300.denoiser import Denoiser
+    net = Denoiser()
+    net.load(T.DEFAULT_WEIGHTS)
+    out = []
+    for k in scenes:
+        r = T.evaluate(ctx, net, P.random_scene(T.EVAL_SEED0 + k, width=size))
+        best_bil = min(row["bilateral"] for row in r["rows"])
+        out.append({"scene_seed": T.EVAL_SEED0 + k, "plain_spp": r["plain_spp"], "plain_ms": r["plain_ms"],
+                    "denoised_spp": r["denoised_spp"], "denoised_ms": r["denoised_ms"],
+                    "speedup": None if r["speedup"] is None else round(r["speedup"], 2),
+                    "bilateral_best_rmse": round(best_bil, 4)})
+    sp = [o["speedup"] for o in out if o["speedup"]]
+    return {"target_rmse": 0.01, "size": f"{size}x{size}", "reference_spp": 8192,
+            "space": "sqrt-gamma display values clamped to [0,1]", "scenes": out,
+            "speedup_geomean": round(float(np.exp(np.mean(np.log(sp)))), 2) if len(sp) == len(out) else None}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -199,6 +221,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=2, help="steps of the end-to-end leg (0: skip)")
     ap.add_argument("--bvh-width", type=int, default=2, choices=[2, 8], help="traversal layout")
     ap.add_argument("--no-autotune", action="store_true", help="use the library defaults (no autotuner)")
+    ap.add_argument("--no-denoise-eval", action="store_true",
+                    help="skip the wall-time-to-RMSE comparison of denoised and plain renders")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference_arm(args)
@@ -369,6 +393,14 @@ def main():
     if os.path.exists(tpath):
         traffic = json.load(open(tpath)).get("bytes_per_launch")
 
+    # second half of the metric: wall time to display-space RMSE 0.01, denoised vs plain spp
+    denoise = None
+    if not trace_only and not args.no_denoise_eval:
+        try:
+            denoise = denoise_eval(ctx)
+        except Exception as e:  # reported, never required
+            denoise = {"error": str(e)}
+
     cpu = None
     if not args.no_cpu_baseline:
         try:
@@ -400,6 +432,7 @@ def main():
                      "kernel_ms": round(k_ms, 3), "bytes_per_ray": round(bpr, 1), "peak_source": peak_src},
         "cpu_baseline": cpu,
         "megakernel_same_run": compare,
+        "denoise": denoise,
         "clocks": clk.summary(),
         "gpu_launches": int(launches),
     }

@@ -7,7 +7,7 @@ display space (sqrt, clamped to [0, 1], per channel over all pixels, as pic2RGBW
 Render.cu:462-481) against a high-spp render of a held-out scene, for the plain render, the
 reference's bilateral filter and the denoiser, and the wall time each needs to reach a target RMSE.
 
-    python -m cudapathtracing_gb300.training --scenes 384 --steps 3000 --out weights.npz
+    python -m cudapathtracing_gb300.training --scenes 768 --steps 6000 --out weights.npz
 """
 from __future__ import annotations
 
@@ -37,7 +37,7 @@ def render(ctx, scene, spp: int, seed: int, integrator=abi.INTEGRATOR_WAVEFRONT,
     return rgb, gb, r["ms"]
 
 
-def make_dataset(ctx, n_scenes: int, size: int = 256, spp_in=(1, 4, 16), spp_ref: int = 1024,
+def make_dataset(ctx, n_scenes: int, size: int = 256, spp_in=(1, 4, 16, 64), spp_ref: int = 2048,
                  seed0: int = TRAIN_SEED0, log=print):
     """Stacked device tensors noisy [M, S, S, 3], gbuf [M, S, S, 8], target [M, S, S, 3] with
     M = n_scenes * len(spp_in) (one target per scene, shared by its inputs)."""
@@ -89,7 +89,7 @@ def train(net: Denoiser, data, steps: int, batch: int = 8, lr: float = 1e-3, lr_
 
 
 def evaluate(ctx, net: Denoiser, desc, ref_spp: int = 8192, plain_spps=(1, 4, 16, 64, 256, 1024, 2048),
-             denoise_spps=(1, 4, 16, 64), target_rmse: float = 0.01, seed: int = 17):
+             denoise_spps=(1, 4, 16, 32, 64, 128, 256), target_rmse: float = 0.01, seed: int = 17):
     """RMSE and wall time of plain, bilateral-filtered and denoised renders against a high-spp
     reference (another seed), and the time each needs to reach target_rmse (None if it does not).
     Times are device milliseconds of the render (and of the filter / denoiser) at that spp."""
@@ -132,10 +132,10 @@ def evaluate(ctx, net: Denoiser, desc, ref_spp: int = 8192, plain_spps=(1, 4, 16
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--scenes", type=int, default=384)
+    ap.add_argument("--scenes", type=int, default=768)
     ap.add_argument("--size", type=int, default=256)
-    ap.add_argument("--spp-ref", type=int, default=1024)
-    ap.add_argument("--steps", type=int, default=3000)
+    ap.add_argument("--spp-ref", type=int, default=2048)
+    ap.add_argument("--steps", type=int, default=6000)
     ap.add_argument("--batch", type=int, default=8)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--seed", type=int, default=0)
@@ -156,7 +156,7 @@ def main():
           flush=True)
     os.makedirs(os.path.dirname(os.path.abspath(args.out)), exist_ok=True)
     net.save(args.out)
-    for k in range(2):
+    for k in range(3):
         res = evaluate(ctx, net, P.random_scene(EVAL_SEED0 + k, width=args.eval_size))
         print(f"held-out scene {k}: plain reaches {res['target_rmse']} at {res['plain_spp']} spp "
               f"({res['plain_ms']} ms), denoised at {res['denoised_spp']} spp ({res['denoised_ms']} ms), "
