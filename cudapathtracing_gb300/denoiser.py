@@ -117,3 +117,51 @@ class Denoiser:
             self.close()
         except Exception:
             pass
+
+
+def main():
+    """Times inference on one image and a training step on a batch of crops (random inputs):
+    python -m cudapathtracing_gb300.denoiser --size 1920x1080 --batch 8 --crop 256"""
+    import argparse
+    import time
+    import torch
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--size", default="1920x1080")
+    ap.add_argument("--batch", type=int, default=8)
+    ap.add_argument("--crop", type=int, default=256)
+    ap.add_argument("--reps", type=int, default=5)
+    a = ap.parse_args()
+    W, H = (int(x) for x in a.size.split("x"))
+    net = Denoiser(seed=0)
+    rgb = torch.rand(1, H, W, 3, device="cuda")
+    gb = torch.rand(1, H, W, 8, device="cuda")
+    out = torch.empty_like(rgb)
+    for _ in range(3):
+        net.denoise(rgb, gb, out)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(a.reps):
+        net.denoise(rgb, gb, out)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / a.reps
+    Hp, Wp = (H + 15) // 16 * 16, (W + 15) // 16 * 16
+    lv = [0, 0, 1, 1, 2, 2, 3, 3, 4, 4, 3, 3, 2, 2, 1, 1, 0, 0, 0]
+    flops = 2 * Hp * Wp * 9 * sum(ci * co / 4 ** l for (ci, co, _), l in zip(SPECS, lv))
+    print(f"inference {W}x{H}: {ms:.3f} ms, convolutions {flops / 1e12:.3f} TFLOP -> {flops / ms / 1e9:.1f} TFLOP/s")
+    c = a.crop
+    r = torch.rand(a.batch, c, c, 3, device="cuda")
+    g = torch.rand(a.batch, c, c, 8, device="cuda")
+    t = torch.rand(a.batch, c, c, 3, device="cuda")
+    for _ in range(3):
+        net.train_step(r, g, t, lr=1e-5)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(a.reps):
+        net.train_step(r, g, t, lr=1e-5)
+    torch.cuda.synchronize()
+    print(f"train step {a.batch}x{c}x{c}: {(time.perf_counter() - t0) / a.reps * 1e3:.3f} ms")
+
+
+if __name__ == "__main__":
+    main()
