@@ -204,6 +204,17 @@ class Scene:
         check(lib().cpt_render(self.h, C.byref(params), C.byref(out), _vp(stream), C.byref(st)), "cpt_render")
         return dict(rgb=rgb, rgba8=rgba8, gbuffer=gbuffer, rays=int(st.rays), paths=int(st.paths), ms=float(st.ms))
 
+    def pick(self, x: int, y: int) -> int:
+        """getObject (Render.cu:485-496): primitive under pixel (x, y), -1 on a miss or a light."""
+        out = C.c_int32()
+        check(lib().cpt_pick(self.h, int(x), int(y), C.byref(out)), "cpt_pick")
+        return out.value
+
+    def set_material(self, first: int, end: int, alpha_x: float, alpha_y: float, glass: bool) -> None:
+        """changeMaterial (Render.cu:498-522) over primitives [first, end)."""
+        check(lib().cpt_scene_set_material(self.h, int(first), int(end), float(alpha_x), float(alpha_y),
+                                           1 if glass else 0), "cpt_scene_set_material")
+
     def close(self):
         if self.h:
             lib().cpt_scene_destroy(self.h)

@@ -76,6 +76,7 @@ struct cpt_scene {
     uint32_t* sphere_mat;
     DevLight* lights;
     DevMaterial* mats;
+    uint32_t n_mats;
     double* extra_c;
     float4* extra_box;
     // LBVH
@@ -281,6 +282,7 @@ cpt_status create_scene(cpt_context* ctx, const cpt_scene_desc* d, cpt_scene** o
         sph_mat[i] = S.material;
     }
     std::vector<DevMaterial> mats(d->num_materials);
+    s->n_mats = d->num_materials;
     for (uint32_t i = 0; i < d->num_materials; ++i) {
         const cpt_material& m = d->materials[i];
         DevMaterial& dm = mats[i];
@@ -699,6 +701,86 @@ CPT_EXPORT cpt_status cpt_lbvh_export(const cpt_scene* s, uint64_t* keys, uint32
         cpt_status st = boxes(s->leaf_box, n, leaf_boxes);
         if (st != CPT_OK) return st;
     }
+    return CPT_OK;
+}
+
+namespace {
+__global__ void k_fill_u32(uint32_t* p, uint32_t n, uint32_t v)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = v;
+}
+}  // namespace
+
+// getObject (Render.cu:485-496): one ray through the centre of pixel (x, y) (row 0 at the bottom,
+// Camera::getSampleRay, Camera.cuh:44-48); the closest primitive in the reference's numbering, or
+// -1 on a miss or a light (lights carry no material).
+CPT_EXPORT cpt_status cpt_pick(cpt_scene* s, int32_t x, int32_t y, int32_t* prim)
+{
+    if (!s || !prim) return fail(CPT_ERR_INVALID_ARGUMENT, "cpt_pick: null argument");
+    if (!s->built && s->n) return fail(CPT_ERR_NOT_BUILT, "cpt_pick: build the LBVH first");
+    *prim = -1;
+    if (x < 0 || y < 0 || x >= s->cam.width || y >= s->cam.height) return CPT_OK;
+    CPT_CUDA(cudaSetDevice(s->ctx->device));
+    const DevCamera& c = s->cam;
+    float3 p = c.pixel_center + (float)x * c.delta_h + (float)y * c.delta_v;
+    cpt_ray r;
+    std::memset(&r, 0, sizeof r);
+    r.origin[0] = c.look_from.x;
+    r.origin[1] = c.look_from.y;
+    r.origin[2] = c.look_from.z;
+    r.direction[0] = p.x - c.look_from.x;
+    r.direction[1] = p.y - c.look_from.y;
+    r.direction[2] = p.z - c.look_from.z;
+    r.tmin = 0.001f;
+    r.tmax = CPT_INF_F;
+    cpt_hit h;
+    cpt_status st = cpt_trace_closest(s, &r, 1, &h, 0, nullptr);
+    if (st != CPT_OK) return st;
+    if (h.prim >= (int32_t)s->n_lights) *prim = h.prim;
+    return CPT_OK;
+}
+
+// changeMaterial (Render.cu:498-522): primitives [first, end) get roughness (alpha_x, alpha_y) and
+// the Opaque type, or SpecularDielectric when glass != 0; lights are left alone.  The range gets a
+// new material (a copy of its first primitive's, edited), so other primitives sharing the old one
+// are unchanged, as with the reference's per-object material copies.
+CPT_EXPORT cpt_status cpt_scene_set_material(cpt_scene* s, uint32_t first, uint32_t end, double alpha_x,
+                                             double alpha_y, int32_t glass)
+{
+    if (!s) return fail(CPT_ERR_INVALID_ARGUMENT, "cpt_scene_set_material: null scene");
+    first = std::max(first, s->n_lights);
+    end = std::min(end, s->n);
+    if (first >= end) return CPT_OK;
+    CPT_CUDA(cudaSetDevice(s->ctx->device));
+    const uint32_t sph0 = s->n_lights, tri0 = s->n_lights + s->n_spheres;
+    uint32_t old_mi = 0;
+    if (first < tri0) CPT_CUDA(cudaMemcpy(&old_mi, s->sphere_mat + (first - sph0), 4, cudaMemcpyDeviceToHost));
+    else CPT_CUDA(cudaMemcpy(&old_mi, s->tri_mat + (first - tri0), 4, cudaMemcpyDeviceToHost));
+    DevMaterial m;
+    CPT_CUDA(cudaMemcpy(&m, s->mats + old_mi, sizeof m, cudaMemcpyDeviceToHost));
+    m.ax = (float)alpha_x;
+    m.ay = (float)alpha_y;
+    m.type = glass ? CPT_M_SPECULAR_DIELECTRIC : CPT_M_OPAQUE;
+    DevMaterial* grown = nullptr;
+    CPT_CUDA(cudaMalloc((void**)&grown, (s->n_mats + 1) * sizeof(DevMaterial)));
+    CPT_CUDA(cudaMemcpy(grown, s->mats, s->n_mats * sizeof(DevMaterial), cudaMemcpyDeviceToDevice));
+    CPT_CUDA(cudaMemcpy(grown + s->n_mats, &m, sizeof m, cudaMemcpyHostToDevice));
+    CPT_CUDA(cudaFree(s->mats));
+    s->mats = grown;
+    const uint32_t mi = s->n_mats++;
+    if (first < tri0) {
+        const uint32_t a = first - sph0, b = std::min(end, tri0) - sph0;
+        k_fill_u32<<<(b - a + 255) / 256, 256>>>(s->sphere_mat + a, b - a, mi);
+        add_launches(1);
+    }
+    if (end > tri0) {
+        const uint32_t a = std::max(first, tri0) - tri0, b = end - tri0;
+        k_fill_u32<<<(b - a + 255) / 256, 256>>>(s->tri_mat + a, b - a, mi);
+        add_launches(1);
+    }
+    CPT_CUDA(cudaGetLastError());
+    CPT_CUDA(cudaDeviceSynchronize());
     return CPT_OK;
 }
 

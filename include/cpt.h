@@ -329,6 +329,15 @@ cpt_status cpt_filter_bilateral(cpt_context* ctx, const float* rgb, const float*
 cpt_status cpt_filter_temporal(cpt_context* ctx, float* rgb, const float* prev_rgb, const float* gbuf,
                                const cpt_camera* camera, const cpt_camera* prev_camera, float alpha, void* stream);
 
+/* Picking and live material edit (getObject / changeMaterial, Render.cu:485-522, driven by
+ * Window.cu:313-346).  cpt_pick: the primitive (reference numbering) hit by the ray through the
+ * centre of pixel (x, y), row 0 at the bottom; -1 on a miss or a light.
+ * cpt_scene_set_material: primitives [first, end) take roughness (alpha_x, alpha_y) and the
+ * Opaque type, or SpecularDielectric when glass != 0 (lights are skipped). */
+cpt_status cpt_pick(cpt_scene* scene, int32_t x, int32_t y, int32_t* prim);
+cpt_status cpt_scene_set_material(cpt_scene* scene, uint32_t first, uint32_t end, double alpha_x, double alpha_y,
+                                  int32_t glass);
+
 /* ---- learned denoiser (no counterpart in the reference) --------------------------------
  * Kernel-predicting U-Net (5 levels, 32-64-96-128-160 channels, 3x3 convolutions, a predicted
  * 5x5 filter per pixel applied to the noisy radiance), trained and run on the library's own

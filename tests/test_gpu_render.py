@@ -197,3 +197,30 @@ def test_autotuner_cache_reproducible(ctx, tmp_path):
         assert r["rays"] > 0
     finally:
         autotune.Autotuner(ctx, cache_path=path).apply(autotune.DEFAULTS, s)
+
+
+def test_pick_and_material_edit(ctx):
+    """cpt_pick agrees with a closest-hit query along the pixel-centre ray; editing the picked
+    primitive's material changes the render there and nowhere it is not seen."""
+    import filters
+    d = P.cornell_box(width=64)
+    s = api.Scene(ctx, d).init()
+    cam = d.camera
+    dirs = filters.camera_rays(cam.width, cam.aspect_ratio, cam.look_from, cam.look_at, cam.vfov_deg)
+    H = s.height
+    for (x, y) in [(32, 20), (10, 40), (50, 5), (31, H - 2)]:
+        ray = np.zeros(1, abi.RAY_DTYPE)
+        ray["origin"] = cam.look_from
+        ray["direction"] = dirs[y, x]
+        ray["tmin"], ray["tmax"] = 0.001, 999999.0
+        want = int(s.trace(ray)["prim"][0])
+        want = want if want >= len(d.lights) else -1
+        assert s.pick(x, y) == want
+    assert s.pick(-1, 0) == -1 and s.pick(0, 10 ** 6) == -1
+    prm = dict(spp=4, seed=2, estimator=abi.ESTIMATOR_REFERENCE)
+    before = s.render(**prm)["rgb"]
+    pid = s.pick(32, 20)
+    assert pid >= len(d.lights)
+    s.set_material(pid, pid + 1, 0.3, 0.3, True)
+    after = s.render(**prm)["rgb"]
+    assert np.isfinite(after).all() and not np.array_equal(before, after)
