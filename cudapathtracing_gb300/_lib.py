@@ -55,6 +55,8 @@ def lib():
             "cpt_denoiser_train_step": (S, [P, C.c_int32, C.c_int32, C.c_int32, P, P, P, C.c_float, C.c_int32,
                                             C.POINTER(C.c_float), P]),
             "cpt_denoise": (S, [P, C.c_int32, C.c_int32, C.c_int32, P, P, P, P]),
+            "cpt_denoiser_set_backend": (S, [P, C.c_int32]),
+            "cpt_denoiser_check": (S, [P]),
             "cpt_filter_temporal": (S, [P, P, P, P, C.POINTER(abi.cpt_camera), C.POINTER(abi.cpt_camera), C.c_float, P]),
             "cpt_ini_load": (S, [C.c_char_p, C.POINTER(P)]),
             "cpt_ini_describe": (S, [P, C.POINTER(abi.cpt_scene_desc)]),

@@ -167,15 +167,24 @@ __global__ void __launch_bounds__(128) k_conv3x3(Geo g, View in, const __nv_bflo
     }
 }
 
+}  // namespace kpcn
+}  // namespace cpt
+
+#include "kpcn_tc.cuh"
+
+namespace cpt {
+namespace kpcn {
+
 // Weight gradient of a 3x3 convolution: dW[tap][ci][co] = sum_p X[p + off(tap), ci] dZ[p, co].
 // Block (128 threads) = one tap, a 32 x 32 (ci, co) tile, and one chunk of pixels; the chunk is
 // staged in shared memory 64 pixels at a time and multiplied on the tensor cores (warp w owns
 // ci rows 16 (w / 2) and co columns 16 (w % 2)).  Partial sums go to part[chunk][tap][ci][co]
-// and are added in chunk order by k_wgrad_reduce.
+// and are added in chunk order by k_wgrad_reduce.  The centre-tap blocks of the first ci tile
+// also sum their dZ columns into bpart[chunk][co] (the bias gradient's partial sums).
 constexpr int WG_PIX = 64;
-constexpr int WG_CHUNKS = 64;   // pixel chunks (blocks along z) per weight gradient
+constexpr int WG_CHUNKS = 256;  // pixel chunks (blocks along z) per weight gradient
 __global__ void __launch_bounds__(128) k_wgrad(Geo g, View x, View dz, int cin, int cout, long chunk_pixels,
-                                               float* __restrict__ part)
+                                               float* __restrict__ part, float* __restrict__ bpart)
 {
     __shared__ __nv_bfloat16 xs[WG_PIX][32 + 8];
     __shared__ __nv_bfloat16 zs[WG_PIX][32 + 8];
@@ -191,6 +200,8 @@ __global__ void __launch_bounds__(128) k_wgrad(Geo g, View x, View dz, int cin, 
     const __nv_bfloat16* xp = reinterpret_cast<const __nv_bfloat16*>(x.ptr);
     const __nv_bfloat16* zp = reinterpret_cast<const __nv_bfloat16*>(dz.ptr);
     float acc[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+    const bool bias_block = tap == 4 && ci_t == 0;
+    float bsum = 0.f;
     for (long pb = pbeg; pb < pend; pb += WG_PIX) {
         // stage: 64 pixels x 32 channels of X (shifted by the tap) and of dZ; 2 channels per load
         for (int e = threadIdx.x; e < WG_PIX * 16; e += 128) {
@@ -208,6 +219,8 @@ __global__ void __launch_bounds__(128) k_wgrad(Geo g, View x, View dz, int cin, 
             *reinterpret_cast<uint32_t*>(&zs[r][c2]) = zv;
         }
         __syncthreads();
+        if (bias_block && threadIdx.x < 32)
+            for (int r = 0; r < WG_PIX; ++r) bsum += __bfloat162float(zs[r][threadIdx.x]);
 #pragma unroll
         for (int kk = 0; kk < WG_PIX; kk += 16) {
             // A = X^T (rows ci, K = pixels); B = dZ (K = pixels, columns co)
@@ -226,6 +239,8 @@ __global__ void __launch_bounds__(128) k_wgrad(Geo g, View x, View dz, int cin, 
         }
         __syncthreads();
     }
+    if (bias_block && threadIdx.x < 32 && co_t * 32 + (int)threadIdx.x < cout)
+        bpart[(size_t)blockIdx.z * cout + co_t * 32 + threadIdx.x] = bsum;
     float* out = part + ((size_t)blockIdx.z * 9 + tap) * cin * cout;
 #pragma unroll
     for (int j = 0; j < 2; ++j) {
@@ -248,23 +263,6 @@ __global__ void k_wgrad_reduce(const float* __restrict__ part, int chunks, size_
         for (int c = 0; c < chunks; ++c) s += part[(size_t)c * n + i];
         grad[i] = s;
     }
-}
-
-// bias gradient: column sums of dZ over all pixels (one block per channel, fixed order)
-__global__ void k_bias_grad(View dz, long P, float* __restrict__ grad)
-{
-    __shared__ float red[256];
-    const int c = blockIdx.x;
-    const __nv_bfloat16* zp = reinterpret_cast<const __nv_bfloat16*>(dz.ptr);
-    float s = 0.f;
-    for (long p = threadIdx.x; p < P; p += blockDim.x) s += __bfloat162float(zp[p * dz.cs + dz.co + c]);
-    red[threadIdx.x] = s;
-    __syncthreads();
-    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) grad[c] = red[0];
 }
 
 // dZ = dA * (A > 0) (ReLU backward) as BF16; without relu the gradient is converted only
@@ -555,6 +553,10 @@ struct Net {
     __nv_bfloat16 *wf16 = nullptr, *wd16 = nullptr;
     long step = 0;
     bool copies_fresh = false;
+    // convolution engine: 0 = mma.sync kernel, 1 = tcgen05 kernel (kpcn_tc.cuh); descriptor byte
+    // offsets of the tcgen05 operands (K direction, M/N direction)
+    int backend = 1;
+    int* err = nullptr;
     // activations / gradients for the current geometry
     int N = 0, H = 0, W = 0;
     Geo geo[5];
@@ -567,6 +569,7 @@ struct Net {
     float *G_D0b, *G_D0a, *G_cat0, *G_D1b, *G_D1a, *G_cat1, *G_D2b, *G_D2a, *G_cat2, *G_D3b, *G_D3a, *G_cat3;
     float *G_A4b, *G_A4a, *G_p4, *G_A3a, *G_p3, *G_A2a, *G_p2, *G_A1a, *G_p1, *G_A0a;
     float* wpart = nullptr;
+    float* bpart = nullptr;   // bias-gradient partial sums per pixel chunk
 
     ~Net()
     {
@@ -577,6 +580,7 @@ struct Net {
         cudaFree(v);
         cudaFree(wf16);
         cudaFree(wd16);
+        cudaFree(err);
     }
 };
 
@@ -621,6 +625,10 @@ cpt_status net_init(Net& n, uint64_t seed)
     CPT_CUDA(cudaMalloc((void**)&n.wf16, o16 * sizeof(__nv_bfloat16)));
     CPT_CUDA(cudaMalloc((void**)&n.wd16, o16 * sizeof(__nv_bfloat16)));
     CPT_CUDA(cudaMemcpy(n.w, h.data(), off * sizeof(float), cudaMemcpyHostToDevice));
+    CPT_CUDA(cudaMalloc((void**)&n.err, sizeof(int)));
+    CPT_CUDA(cudaMemset(n.err, 0, sizeof(int)));
+    CPT_CUDA(cudaFuncSetAttribute(k_conv3x3_tc<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM_MAX));
+    CPT_CUDA(cudaFuncSetAttribute(k_conv3x3_tc<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM_MAX));
     CPT_CUDA(cudaMemset(n.gw, 0, off * sizeof(float)));
     CPT_CUDA(cudaMemset(n.m, 0, off * sizeof(float)));
     CPT_CUDA(cudaMemset(n.v, 0, off * sizeof(float)));
@@ -685,6 +693,7 @@ cpt_status ensure_geometry(Net& n, int N, int H, int W)
     size_t maxw = 0;
     for (int i = 0; i < NCONV; ++i) maxw = std::max(maxw, (size_t)9 * SPECS[i].cin * SPECS[i].cout);
     f32(&n.wpart, (long)(WG_CHUNKS * maxw));
+    f32(&n.bpart, (long)WG_CHUNKS * 512);
     size_t total = 0;
     for (auto& r : reqs) total += align_up(r.bytes, 256);
     CPT_CUDA(cudaMalloc((void**)&n.arena, total));
@@ -697,10 +706,34 @@ cpt_status ensure_geometry(Net& n, int N, int H, int W)
     return CPT_OK;
 }
 
+// tcgen05 convolution: cout split into grid.y tiles of at most 256 channels (multiples of 16)
+void conv_tc(Net& n, const __nv_bfloat16* w, const float* bias, int cout, bool relu, const Geo& g, View in, View out16,
+             View out32, cudaStream_t s)
+{
+    const long P = (long)g.N * g.H * g.W;
+    const int tiles = (cout + 255) / 256;
+    const int nt = cout / tiles;
+    int ncols = 32;
+    while (ncols < nt) ncols <<= 1;
+    const int kc = in.C % 64 == 0 ? 64 : 32;
+    // shared memory large enough that at most 512 / ncols CTAs fit on an SM (tensor memory)
+    const int max_ctas = 512 / ncols;
+    const int smem = std::max(tc_smem_bytes(kc, nt), TC_SM_SMEM / (max_ctas + 1) + 1024);
+    dim3 grid((unsigned)((P + TC_M - 1) / TC_M), (unsigned)tiles);
+    if (kc == 64)
+        k_conv3x3_tc<64><<<grid, 128, smem, s>>>(g, in, w, bias, cout, nt, ncols, relu, out16, out32, n.err);
+    else
+        k_conv3x3_tc<32><<<grid, 128, smem, s>>>(g, in, w, bias, cout, nt, ncols, relu, out16, out32, n.err);
+}
+
 void conv(Net& n, int i, const Geo& g, View in, View out16, View out32, cudaStream_t s)
 {
     const ConvSpec& c = SPECS[i];
     in.C = c.cin;
+    if (n.backend == 1) {
+        conv_tc(n, n.wf16 + n.w16off[i], n.w + n.boff[i], c.cout, c.relu, g, in, out16, out32, s);
+        return;
+    }
     const long P = (long)g.N * g.H * g.W;
     dim3 grid((unsigned)(((P + 15) / 16 + 3) / 4), (unsigned)(c.cout / 32));
     k_conv3x3<4><<<grid, 128, 0, s>>>(g, in, n.wf16 + n.w16off[i], n.w + n.boff[i], c.cout, c.relu, out16, out32,
@@ -712,6 +745,10 @@ void dgrad(Net& n, int i, const Geo& g, View dz, View gin, cudaStream_t s)
 {
     const ConvSpec& c = SPECS[i];
     dz.C = c.cout;
+    if (n.backend == 1) {
+        conv_tc(n, n.wd16 + n.w16off[i], nullptr, c.cin, false, g, dz, none(), gin, s);
+        return;
+    }
     const long P = (long)g.N * g.H * g.W;
     dim3 grid((unsigned)(((P + 15) / 16 + 3) / 4), (unsigned)(c.cin / 32));
     k_conv3x3<4><<<grid, 128, 0, s>>>(g, dz, n.wd16 + n.w16off[i], nullptr, c.cin, false, none(), gin, false);
@@ -725,10 +762,10 @@ void wgrad(Net& n, int i, const Geo& g, View x, View dz, cudaStream_t s)
     const long cp = std::max<long>(WG_PIX, ((P + WG_CHUNKS - 1) / WG_CHUNKS + WG_PIX - 1) / WG_PIX * WG_PIX);
     const int chunks = (int)((P + cp - 1) / cp);
     dim3 grid((unsigned)((c.cin + 31) / 32), (unsigned)(9 * ((c.cout + 31) / 32)), (unsigned)chunks);
-    k_wgrad<<<grid, 128, 0, s>>>(g, x, dz, c.cin, c.cout, cp, n.wpart);
+    k_wgrad<<<grid, 128, 0, s>>>(g, x, dz, c.cin, c.cout, cp, n.wpart, n.bpart);
     const size_t cnt = (size_t)9 * c.cin * c.cout;
     k_wgrad_reduce<<<grid_for((long)cnt), 256, 0, s>>>(n.wpart, chunks, cnt, n.gw + n.woff[i]);
-    k_bias_grad<<<c.cout, 256, 0, s>>>(dz, P, n.gw + n.boff[i]);
+    k_wgrad_reduce<<<1, 256, 0, s>>>(n.bpart, chunks, (size_t)c.cout, n.gw + n.boff[i]);
 }
 
 void relu_back(const Geo& g, View g32, View act, int C, bool relu, View dz, cudaStream_t s)
@@ -890,6 +927,27 @@ CPT_EXPORT cpt_status cpt_denoiser_create(int device, uint64_t seed, cpt_denoise
         return st;
     }
     *out = d;
+    return CPT_OK;
+}
+
+// Convolution engine: 0 = mma.sync kernel, 1 = tcgen05 kernel (the default).
+CPT_EXPORT cpt_status cpt_denoiser_set_backend(cpt_denoiser* d, int32_t backend)
+{
+    if (!d || backend < 0 || backend > 1) return fail(CPT_ERR_INVALID_ARGUMENT, "cpt_denoiser_set_backend: 0 or 1");
+    d->net.backend = backend;
+    return CPT_OK;
+}
+
+// Device error word of the last passes (CPT_DEVERR_ITER: a tensor-core barrier wait timed out);
+// reading clears it.
+CPT_EXPORT cpt_status cpt_denoiser_check(cpt_denoiser* d)
+{
+    if (!d) return fail(CPT_ERR_INVALID_ARGUMENT, "cpt_denoiser_check: null");
+    int e = 0;
+    CPT_CUDA(cudaSetDevice(d->net.device));
+    CPT_CUDA(cudaMemcpy(&e, d->net.err, sizeof e, cudaMemcpyDeviceToHost));
+    CPT_CUDA(cudaMemset(d->net.err, 0, sizeof e));
+    if (e) return fail(CPT_ERR_TIMEOUT, "denoiser: a tensor-core barrier wait timed out");
     return CPT_OK;
 }
 

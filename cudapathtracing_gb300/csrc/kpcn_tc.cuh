@@ -1,0 +1,273 @@
+// kpcn_tc.cuh — 3x3 convolution as an implicit GEMM on the 5th-generation tensor cores
+// (tcgen05.mma, BF16 operands from shared memory, FP32 accumulators in tensor memory).
+//
+// One CTA (4 warps) computes a tile of 128 consecutive pixels (the MMA's M) by N output channels
+// (N = cout / tiles along grid.y, a multiple of 16, at most 256).  K = 9 taps x cin runs in chunks
+// of KC = 64 (or 32) channels of one tap: the CTA's threads copy the chunk's A (128 pixel rows, shifted by the
+// tap; cp.async zero-fills rows outside the image) and B (N weight rows, [tap][cout][cin]) into
+// shared memory in the canonical K-major layout without swizzle (8-row x 16-byte core matrices;
+// core matrices adjacent along K are 128 bytes apart, 8-row groups KC * 16 bytes apart); one elected
+// thread issues KC / 16 tcgen05.mma (K = 16 each) per chunk and commits them to the stage's mbarrier.
+// Four stages: the asynchronous copies run two chunks ahead of the MMAs, and a stage is refilled
+// once the MMAs that read it (two chunks earlier) have completed, so the tensor core always has the
+// next chunk queued.  The epilogue reads the accumulator rows back with
+// tcgen05.ld (warp w owns TMEM lanes 32w..32w+31 = pixels), adds the bias, applies ReLU and
+// stores BF16 and/or FP32 views like k_conv3x3.
+//
+// Every wait is bounded: a barrier that does not complete within ~2^31 clock cycles sets
+// CPT_DEVERR_ITER in *err and the CTA stops issuing work (it still frees its tensor memory).
+#pragma once
+
+#include <cuda_bf16.h>
+
+namespace cpt {
+namespace kpcn {
+
+constexpr int TC_M = 128;          // pixels per CTA tile (MMA M)
+constexpr int TC_STAGES = 4;       // shared-memory stages (loads run TC_STAGES - 2 steps ahead)
+constexpr int TC_SM_SMEM = 233472; // shared memory per SM (228 KB)
+
+// KC channels per stage; dynamic shared memory of a launch with N = n_tile:
+// TC_STAGES x (A + B) + 1 KB alignment slack
+__host__ __device__ constexpr int tc_stage_bytes(int kc, int n_tile) { return (TC_M + n_tile) * kc * 2; }
+__host__ __device__ constexpr int tc_smem_bytes(int kc, int n_tile) { return TC_STAGES * tc_stage_bytes(kc, n_tile) + 1024; }
+constexpr int TC_SMEM_MAX = tc_smem_bytes(64, 256);   // largest launch (KC 64, N 256)
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Waits for the barrier phase with the given parity; false (and *err set) on timeout.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err)
+{
+    const long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity)) {
+        if (clock64() - t0 > (1LL << 31)) {
+            if (err) atomicOr(err, CPT_DEVERR_ITER);
+            return false;
+        }
+    }
+    return true;
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// Shared-memory matrix descriptor: start address, leading (K) and stride (M/N) byte offsets,
+// descriptor version 1, no swizzle.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo)
+{
+    return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both K-major, M x N.
+__host__ __device__ constexpr uint32_t idesc_bf16(int m, int n)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accumulate)
+{
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint64_t* bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_addr(bar))
+                 : "memory");
+}
+
+// 16 consecutive FP32 columns of the calling warp's 32 TMEM lanes (one lane per thread).
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
+{
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr)
+        : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// 16-byte asynchronous global -> shared copy; src_bytes = 0 writes zeros without reading.  The
+// activation rows go through L1 (.ca): the three horizontal taps of a row read the same lines in
+// consecutive chunks.
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, uint32_t src_bytes)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+// KC channels per stage (32 or 64; in.C a multiple of KC), cout output channels in grid.y tiles of
+// n_tile (a multiple of 16, <= 256); ncols = tensor-memory columns allocated (power of two >=
+// n_tile).  The launch's shared memory is sized so that at most 512 / ncols CTAs share an SM, so
+// tensor-memory allocations never wait on one another.
+template <int KC>
+__global__ void __launch_bounds__(128, 1) k_conv3x3_tc(Geo g, View in, const __nv_bfloat16* __restrict__ w,
+                                                        const float* __restrict__ bias, int cout, int n_tile,
+                                                        int ncols, bool relu, View out16, View out32, int* err)
+{
+    constexpr uint32_t lbo = 128, sbo = KC * 16;   // core matrices: +128 B along K, +KC*16 B per 8 rows
+    constexpr int A_BYTES = TC_M * KC * 2;
+    extern __shared__ uint8_t tc_smem_raw[];
+    __shared__ uint64_t bar[TC_STAGES];
+    __shared__ uint32_t tmem_slot;
+    __shared__ int abort_flag;
+    uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(tc_smem_raw) + 1023) & ~uintptr_t(1023));
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const long P = (long)g.N * g.H * g.W;
+    const long p_base = (long)blockIdx.x * TC_M;
+    const int n_base = blockIdx.y * n_tile;
+    const int cin = in.C;
+    const int stage_bytes = tc_stage_bytes(KC, n_tile);
+    const __nv_bfloat16* inp = reinterpret_cast<const __nv_bfloat16*>(in.ptr);
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&tmem_slot)),
+                     "r"(ncols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        for (int k = 0; k < TC_STAGES; ++k) mbar_init(&bar[k], 1);
+        abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_slot;
+    const uint32_t idesc = idesc_bf16(TC_M, n_tile);
+    uint32_t phase[TC_STAGES];
+    uint32_t uses[TC_STAGES];
+    for (int k = 0; k < TC_STAGES; ++k) phase[k] = uses[k] = 0u;
+
+    // per-thread rows of A (row-fastest: conflict-free shared stores): row tid, chunks 0..7
+    const long p_row = p_base + tid;
+    const int x_row = (int)(p_row % g.W), y_row = (int)((p_row / g.W) % g.H);
+    const int steps_per_tap = cin / KC;
+    const int total = 9 * steps_per_tap;
+
+    auto issue_loads = [&](int step) {
+        const int st = step % TC_STAGES;
+        const int tap = step / steps_per_tap;
+        const int c0 = (step - tap * steps_per_tap) * KC;
+        const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+        const uint32_t As = smem_addr(smem + st * stage_bytes);
+        const uint32_t Bs = As + A_BYTES;
+        const bool row_ok = p_row < P && (unsigned)(y_row + dy) < (unsigned)g.H && (unsigned)(x_row + dx) < (unsigned)g.W;
+        const __nv_bfloat16* src = row_ok ? inp + (p_row + (long)dy * g.W + dx) * in.cs + in.co + c0 : inp;
+#pragma unroll
+        for (int kc = 0; kc < KC / 8; ++kc)
+            cp_async16(As + (tid >> 3) * sbo + kc * lbo + (tid & 7) * 16, row_ok ? src + kc * 8 : inp,
+                       row_ok ? 16u : 0u);
+        const __nv_bfloat16* wt = w + ((size_t)tap * cout + n_base) * cin + c0;
+        for (int c = tid; c < n_tile * (KC / 8); c += 128) {
+            const int n = c % n_tile, kc = c / n_tile;
+            cp_async16(Bs + (n >> 3) * sbo + kc * lbo + (n & 7) * 16, wt + (size_t)n * cin + kc * 8, 16u);
+        }
+    };
+
+    constexpr int AHEAD = TC_STAGES - 2;
+    for (int k = 0; k < AHEAD; ++k) {
+        if (k < total) issue_loads(k);
+        cp_async_commit();
+    }
+    for (int step = 0; step < total; ++step) {
+        const int kn = step + AHEAD;
+        if (kn < total) {
+            if (kn >= TC_STAGES) {   // the stage's previous chunk (kn - TC_STAGES) must be consumed
+                const int ps = kn % TC_STAGES;
+                if (!mbar_wait(&bar[ps], phase[ps], err)) abort_flag = 1;
+                phase[ps] ^= 1u;
+            }
+            if (!abort_flag) issue_loads(kn);
+        }
+        cp_async_commit();
+        cp_async_wait<AHEAD>();   // this step's copies have landed
+        fence_async_smem();
+        __syncthreads();
+        if (abort_flag) break;
+        const int s = step % TC_STAGES;
+        if (tid == 0) {
+            tc_fence_after();
+            const uint32_t a0 = smem_addr(smem + s * stage_bytes), b0 = a0 + A_BYTES;
+#pragma unroll
+            for (int j = 0; j < KC / 16; ++j)
+                umma_bf16(tmem, smem_desc(a0 + j * 256, lbo, sbo), smem_desc(b0 + j * 256, lbo, sbo), idesc,
+                          (step > 0 || j > 0) ? 1u : 0u);
+            umma_commit(&bar[s]);
+        }
+        uses[s] += 1u;
+    }
+    cp_async_wait<0>();
+    // the last commit covers every MMA issued before it
+    const int sl = (total - 1) % TC_STAGES;
+    bool ok = !abort_flag && mbar_wait(&bar[sl], (uses[sl] - 1u) & 1u, err);
+    tc_fence_after();
+    if (ok) {
+        const long p = p_base + warp * 32 + lane;
+        for (int c = 0; c < n_tile; c += 16) {
+            float v[16];
+            tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, v);
+            if (p >= P) continue;
+#pragma unroll
+            for (int i = 0; i < 16; i += 2) {
+                const int ch = n_base + c + i;
+                float v0 = v[i], v1 = v[i + 1];
+                if (bias) {
+                    v0 += bias[ch];
+                    v1 += bias[ch + 1];
+                }
+                if (out32.ptr) {
+                    float* o = reinterpret_cast<float*>(out32.ptr) + p * out32.cs + out32.co + ch;
+                    o[0] = v0;
+                    o[1] = v1;
+                }
+                if (out16.ptr) {
+                    if (relu) {
+                        v0 = fmaxf(v0, 0.f);
+                        v1 = fmaxf(v1, 0.f);
+                    }
+                    __nv_bfloat16* o = reinterpret_cast<__nv_bfloat16*>(out16.ptr) + p * out16.cs + out16.co + ch;
+                    *reinterpret_cast<unsigned int*>(o) =
+                        pack_bf16(__float2bfloat16_rn(v0), __float2bfloat16_rn(v1));
+                }
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols) : "memory");
+    }
+}
+
+}  // namespace kpcn
+}  // namespace cpt

@@ -69,6 +69,14 @@ class Denoiser:
         check(lib().cpt_denoiser_get_grads(self.h, a.ctypes.data_as(C.c_void_p)), "cpt_denoiser_get_grads")
         return a
 
+    def set_backend(self, backend: int) -> None:
+        """1: tcgen05 convolutions (default), 0: mma.sync convolutions (cpt_denoiser_set_backend)."""
+        check(lib().cpt_denoiser_set_backend(self.h, backend), "cpt_denoiser_set_backend")
+
+    def check(self) -> None:
+        """Raises if a tensor-core barrier wait timed out since the last check."""
+        check(lib().cpt_denoiser_check(self.h), "cpt_denoiser_check")
+
     def export(self, name: str) -> np.ndarray:
         """An internal tensor of the last pass, flattened (see cpt_denoiser_export)."""
         cnt = C.c_uint64()
@@ -130,9 +138,12 @@ def main():
     ap.add_argument("--batch", type=int, default=8)
     ap.add_argument("--crop", type=int, default=256)
     ap.add_argument("--reps", type=int, default=5)
+    ap.add_argument("--backend", type=int, default=None, help="0: mma.sync, 1: tcgen05 (default: the library's)")
     a = ap.parse_args()
     W, H = (int(x) for x in a.size.split("x"))
     net = Denoiser(seed=0)
+    if a.backend is not None:
+        net.set_backend(a.backend)
     rgb = torch.rand(1, H, W, 3, device="cuda")
     gb = torch.rand(1, H, W, 8, device="cuda")
     out = torch.empty_like(rgb)

@@ -49,11 +49,18 @@ def _run(net, rgb, g, tgt):
     return loss, ex, o
 
 
-def test_forward_layers_match_oracle(ctx):
+BACKENDS = pytest.mark.parametrize("backend", [0, 1], ids=["mma_sync", "tcgen05"])
+
+
+@BACKENDS
+def test_forward_layers_match_oracle(ctx, backend):
     from cudapathtracing_gb300 import denoiser as D
     rng = np.random.default_rng(7)
     rgb, g, tgt = _batch(rng, 2, 32, 48)
-    _, ex, o = _run(D.Denoiser(seed=3), rgb, g, tgt)
+    net = D.Denoiser(seed=3)
+    net.set_backend(backend)
+    _, ex, o = _run(net, rgb, g, tgt)
+    net.check()
     skip = {"A0b": ("cat0", 64), "A1b": ("cat1", 96), "A2b": ("cat2", 128), "A3b": ("cat3", 160)}
     for name, (want, _) in o.layer_outputs().items():
         if name in skip:
@@ -68,12 +75,15 @@ def test_forward_layers_match_oracle(ctx):
         assert (got == want).mean() >= 0.99, (name, (got == want).mean())
 
 
-def test_gradients_match_oracle(ctx):
+@BACKENDS
+def test_gradients_match_oracle(ctx, backend):
     from cudapathtracing_gb300 import denoiser as D
     rng = np.random.default_rng(7)
     rgb, g, tgt = _batch(rng, 2, 32, 48)
     net = D.Denoiser(seed=3)
+    net.set_backend(backend)
     loss, ex, o = _run(net, rgb, g, tgt)
+    net.check()
     grads = net.grads()
     lo = o.loss(tgt.astype(np.float64))
     go = o.backward()
@@ -91,13 +101,16 @@ def test_gradients_match_oracle(ctx):
     assert not bad, bad
 
 
-def test_denoise_matches_oracle_forward(ctx):
+@BACKENDS
+def test_denoise_matches_oracle_forward(ctx, backend):
     """Any image size (padded to multiples of 16 inside), batch of 2."""
     from cudapathtracing_gb300 import denoiser as D
     rng = np.random.default_rng(9)
     rgb, g, _ = _batch(rng, 2, 37, 45)
     net = D.Denoiser(seed=5)
+    net.set_backend(backend)
     out = net.denoise(*_cuda(rgb, g)).cpu().numpy()
+    net.check()
     want = K.Net(net.params).forward(rgb, g)
     err = np.abs(out - want) / np.maximum(1.0, np.abs(want))
     assert err.max() < 1e-3, err.max()
