@@ -224,3 +224,21 @@ def test_pick_and_material_edit(ctx):
     s.set_material(pid, pid + 1, 0.3, 0.3, True)
     after = s.render(**prm)["rgb"]
     assert np.isfinite(after).all() and not np.array_equal(before, after)
+
+
+def test_row_bands_of_ranks_reassemble_the_frame(ctx):
+    """The multi-GPU row partition (shard.render_band), run rank by rank on one GPU: the bands
+    together are the single-rank frame (pixels are independent)."""
+    import torch
+    from cudapathtracing_gb300 import shard
+    d = P.cornell_box(width=48)
+    s = api.Scene(ctx, d).init()
+    prm = dict(spp=2, seed=4, estimator=abi.ESTIMATOR_CONFIG, max_depth=8, rr_depth=3, rr_prob=0.8,
+               integrator=abi.INTEGRATOR_WAVEFRONT)
+    full = torch.zeros((s.height, s.width, 3), device="cuda")
+    s.render(rgb=full, **prm)
+    world = 3
+    rgb = torch.zeros_like(full)
+    bands = [shard.render_band(s, r, world, rgb, **prm)[0] for r in range(world)]
+    torch.cuda.synchronize()
+    assert torch.equal(torch.cat(bands, 0), full)
