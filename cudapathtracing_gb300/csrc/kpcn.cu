@@ -10,7 +10,8 @@
 //   pooling / upsampling / concatenation   channel-sliced NHWC views, no copies
 //   kernel apply   softmax over 25 logits, weighted 5x5 gather of the noisy radiance, and its
 //                  gradient
-//   loss           L1 between log(1 + x) of the output and of the target, mean over pixels
+//   loss           L1 between sqrt(x + 1e-3) of the output and of the target (the display
+//                  transform the RMSE is measured in), mean over pixels
 //   optimiser      Adam on FP32 master weights; BF16 weight copies are refreshed each step
 //
 // Activations are NHWC BF16 with an explicit channel stride and offset (a view), so a skip
@@ -464,7 +465,9 @@ __global__ void k_apply_back(Geo g, int Hr, int Wr, const float* __restrict__ wt
     }
 }
 
-// L1 of log(1 + x) over the real pixels; dout = d(mean loss)/d(out); per-block partial sums
+// L1 of sqrt(x + LOSS_EPS) over the real pixels (the display transform of the evaluation, without
+// its clamp); dout = d(mean loss)/d(out); per-block partial sums
+constexpr float LOSS_EPS = 1e-3f;
 __global__ void k_loss(Geo g, int Hr, int Wr, const float* __restrict__ out, const float* __restrict__ target,
                        float* __restrict__ dout, float* __restrict__ partial, float scale)
 {
@@ -479,10 +482,10 @@ __global__ void k_loss(Geo g, int Hr, int Wr, const float* __restrict__ out, con
             if (real) {
                 const float o = out[3 * p + c];
                 const float t = target[(((size_t)b * Hr + y) * Wr + x) * 3 + c];
-                const float lo = log1pf(fmaxf(o, 0.f)), lt = log1pf(fmaxf(t, 0.f));
+                const float lo = sqrtf(fmaxf(o, 0.f) + LOSS_EPS), lt = sqrtf(fmaxf(t, 0.f) + LOSS_EPS);
                 const float d = lo - lt;
                 s += fabsf(d);
-                gr = o > 0.f ? scale * (d > 0.f ? 1.f : (d < 0.f ? -1.f : 0.f)) / (1.f + o) : 0.f;
+                gr = o > 0.f ? scale * (d > 0.f ? 1.f : (d < 0.f ? -1.f : 0.f)) * 0.5f / lo : 0.f;
             }
             dout[3 * p + c] = gr;
         }

@@ -1,13 +1,13 @@
 """Training data, training loop and evaluation for the kernel-predicting denoiser.
 
-Data: seeded random scenes (procedural.random_scene), each rendered by the library at low spp
-(1, 4 and 16, the inputs, with their G-buffers) and at high spp with another seed (the target).
+Data: seeded random scenes (procedural.random_scene), each rendered by the library at 1, 4, 16, 64
+and 256 spp (the inputs, with their G-buffers) and at 2048 spp with another seed (the target).
 Training: Adam on random batches of crops through cpt_denoiser_train_step.  Evaluation: RMSE in
 display space (sqrt, clamped to [0, 1], per channel over all pixels, as pic2RGBW shows images,
 Render.cu:462-481) against a high-spp render of a held-out scene, for the plain render, the
 reference's bilateral filter and the denoiser, and the wall time each needs to reach a target RMSE.
 
-    python -m cudapathtracing_gb300.training --scenes 768 --steps 6000 --out weights.npz
+    python -m cudapathtracing_gb300.training --scenes 1024 --steps 10000 --out weights.npz
 """
 from __future__ import annotations
 
@@ -37,7 +37,7 @@ def render(ctx, scene, spp: int, seed: int, integrator=abi.INTEGRATOR_WAVEFRONT,
     return rgb, gb, r["ms"]
 
 
-def make_dataset(ctx, n_scenes: int, size: int = 256, spp_in=(1, 4, 16, 64), spp_ref: int = 2048,
+def make_dataset(ctx, n_scenes: int, size: int = 256, spp_in=(1, 4, 16, 64, 256), spp_ref: int = 2048,
                  seed0: int = TRAIN_SEED0, log=print):
     """Stacked device tensors noisy [M, S, S, 3], gbuf [M, S, S, 8], target [M, S, S, 3] with
     M = n_scenes * len(spp_in) (one target per scene, shared by its inputs)."""
@@ -88,10 +88,14 @@ def train(net: Denoiser, data, steps: int, batch: int = 8, lr: float = 1e-3, lr_
     return hist
 
 
-def evaluate(ctx, net: Denoiser, desc, ref_spp: int = 8192, plain_spps=(1, 4, 16, 64, 256, 1024, 2048),
-             denoise_spps=(1, 4, 16, 32, 64, 128, 256), target_rmse: float = 0.01, seed: int = 17):
+LADDER = (1, 2, 3, 4, 6, 8, 12, 16, 24, 32, 48, 64, 96, 128, 192, 256, 384, 512, 768, 1024, 1536, 2048)
+
+
+def evaluate(ctx, net: Denoiser, desc, ref_spp: int = 8192, plain_spps=LADDER,
+             denoise_spps=tuple(x for x in LADDER if x <= 512), target_rmse: float = 0.01, seed: int = 17):
     """RMSE and wall time of plain, bilateral-filtered and denoised renders against a high-spp
-    reference (another seed), and the time each needs to reach target_rmse (None if it does not).
+    reference (another seed), and the time each needs to reach target_rmse (None if it does not):
+    the smallest spp of a geometric ladder (ratio ~1.5) at which it does.
     Times are device milliseconds of the render (and of the filter / denoiser) at that spp."""
     import torch
     sc = api.Scene(ctx, desc).init()
@@ -132,10 +136,10 @@ def evaluate(ctx, net: Denoiser, desc, ref_spp: int = 8192, plain_spps=(1, 4, 16
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--scenes", type=int, default=768)
+    ap.add_argument("--scenes", type=int, default=1024)
     ap.add_argument("--size", type=int, default=256)
     ap.add_argument("--spp-ref", type=int, default=2048)
-    ap.add_argument("--steps", type=int, default=6000)
+    ap.add_argument("--steps", type=int, default=10000)
     ap.add_argument("--batch", type=int, default=8)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--seed", type=int, default=0)

@@ -355,7 +355,7 @@ cpt_status cpt_denoiser_get_grads(cpt_denoiser* d, float* host_out);      /* of 
 /* Copies an internal tensor of the last pass (activations "X0", "A0a", "cat0", ..., "logits",
  * "out"; gradients "G_D0b", ...) as floats into host (if capacity suffices); *count = elements. */
 cpt_status cpt_denoiser_export(cpt_denoiser* d, const char* name, float* host, uint64_t capacity, uint64_t* count);
-/* One step: forward, loss = mean |log(1 + out) - log(1 + target)|, backward, and (update != 0)
+/* One step: forward, loss = mean |sqrt(out + 1e-3) - sqrt(target + 1e-3)|, backward, and (update != 0)
  * an Adam step with learning rate lr.  *loss (optional) receives the loss before the update. */
 cpt_status cpt_denoiser_train_step(cpt_denoiser* d, int32_t n, int32_t h, int32_t w, const float* rgb,
                                    const float* gbuf, const float* target, float lr, int32_t update, float* loss,

@@ -12,6 +12,7 @@ import numpy as np
 
 INF = 999999.0
 KS = 5
+LOSS_EPS = 1e-3   # loss: L1 of sqrt(x + LOSS_EPS)
 SPECS = [
     (32, 32, True), (32, 32, True), (32, 64, True), (64, 64, True), (64, 96, True), (96, 96, True),
     (96, 128, True), (128, 128, True), (128, 160, True), (160, 160, True),
@@ -229,10 +230,11 @@ class Net:
     def loss(self, target):
         N, H, W, Hr, Wr = self.dims
         o = self.out[:, :Hr, :Wr]
-        d = np.log1p(np.maximum(o, 0.0)) - np.log1p(np.maximum(target, 0.0))
+        lo = np.sqrt(np.maximum(o, 0.0) + LOSS_EPS)
+        d = lo - np.sqrt(np.maximum(target, 0.0) + LOSS_EPS)
         scale = 1.0 / (N * Hr * Wr * 3)
         dout = np.zeros_like(self.out)
-        dout[:, :Hr, :Wr] = np.where(o > 0, scale * np.sign(d) / (1.0 + o), 0.0)
+        dout[:, :Hr, :Wr] = np.where(o > 0, scale * np.sign(d) * 0.5 / lo, 0.0)
         self.dout = dout
         return np.abs(d).sum() * scale
 
