@@ -556,9 +556,10 @@ struct Net {
     __nv_bfloat16 *wf16 = nullptr, *wd16 = nullptr;
     long step = 0;
     bool copies_fresh = false;
-    // convolution engine: 0 = mma.sync kernel, 1 = tcgen05 kernel (kpcn_tc.cuh); descriptor byte
-    // offsets of the tcgen05 operands (K direction, M/N direction)
+    // convolution engine: 0 = mma.sync kernel, 1 = tcgen05 kernel, 2 = warp-specialised persistent
+    // tcgen05 kernel (both in kpcn_tc.cuh)
     int backend = 1;
+    int sm_count = 152;
     int* err = nullptr;
     // activations / gradients for the current geometry
     int N = 0, H = 0, W = 0;
@@ -628,10 +629,13 @@ cpt_status net_init(Net& n, uint64_t seed)
     CPT_CUDA(cudaMalloc((void**)&n.wf16, o16 * sizeof(__nv_bfloat16)));
     CPT_CUDA(cudaMalloc((void**)&n.wd16, o16 * sizeof(__nv_bfloat16)));
     CPT_CUDA(cudaMemcpy(n.w, h.data(), off * sizeof(float), cudaMemcpyHostToDevice));
+    CPT_CUDA(cudaDeviceGetAttribute(&n.sm_count, cudaDevAttrMultiProcessorCount, n.device));
     CPT_CUDA(cudaMalloc((void**)&n.err, sizeof(int)));
     CPT_CUDA(cudaMemset(n.err, 0, sizeof(int)));
     CPT_CUDA(cudaFuncSetAttribute(k_conv3x3_tc<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM_MAX));
     CPT_CUDA(cudaFuncSetAttribute(k_conv3x3_tc<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM_MAX));
+    CPT_CUDA(cudaFuncSetAttribute(k_conv3x3_ws<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM_MAX));
+    CPT_CUDA(cudaFuncSetAttribute(k_conv3x3_ws<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM_MAX));
     CPT_CUDA(cudaMemset(n.gw, 0, off * sizeof(float)));
     CPT_CUDA(cudaMemset(n.m, 0, off * sizeof(float)));
     CPT_CUDA(cudaMemset(n.v, 0, off * sizeof(float)));
@@ -719,6 +723,21 @@ void conv_tc(Net& n, const __nv_bfloat16* w, const float* bias, int cout, bool r
     int ncols = 32;
     while (ncols < nt) ncols <<= 1;
     const int kc = in.C % 64 == 0 ? 64 : 32;
+    if (n.backend == 2) {   // warp-specialised persistent kernel, two accumulators per CTA
+        const int max_ctas = 512 / (2 * ncols);
+        const int smem = std::max(tc_smem_bytes(kc, nt), TC_SM_SMEM / (max_ctas + 1) + 1024);
+        int per_sm = 1;
+        if (kc == 64) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv3x3_ws<64>, 192, smem);
+        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv3x3_ws<32>, 192, smem);
+        per_sm = std::max(1, std::min(per_sm, max_ctas));
+        const long m_tiles = (P + TC_M - 1) / TC_M;
+        dim3 grid((unsigned)std::min<long>(m_tiles, (long)per_sm * n.sm_count), (unsigned)tiles);
+        if (kc == 64)
+            k_conv3x3_ws<64><<<grid, 192, smem, s>>>(g, in, w, bias, cout, nt, ncols, relu, out16, out32, n.err);
+        else
+            k_conv3x3_ws<32><<<grid, 192, smem, s>>>(g, in, w, bias, cout, nt, ncols, relu, out16, out32, n.err);
+        return;
+    }
     // shared memory large enough that at most 512 / ncols CTAs fit on an SM (tensor memory)
     const int max_ctas = 512 / ncols;
     const int smem = std::max(tc_smem_bytes(kc, nt), TC_SM_SMEM / (max_ctas + 1) + 1024);
@@ -733,7 +752,7 @@ void conv(Net& n, int i, const Geo& g, View in, View out16, View out32, cudaStre
 {
     const ConvSpec& c = SPECS[i];
     in.C = c.cin;
-    if (n.backend == 1) {
+    if (n.backend >= 1) {
         conv_tc(n, n.wf16 + n.w16off[i], n.w + n.boff[i], c.cout, c.relu, g, in, out16, out32, s);
         return;
     }
@@ -748,7 +767,7 @@ void dgrad(Net& n, int i, const Geo& g, View dz, View gin, cudaStream_t s)
 {
     const ConvSpec& c = SPECS[i];
     dz.C = c.cout;
-    if (n.backend == 1) {
+    if (n.backend >= 1) {
         conv_tc(n, n.wd16 + n.w16off[i], nullptr, c.cin, false, g, dz, none(), gin, s);
         return;
     }
@@ -933,10 +952,11 @@ CPT_EXPORT cpt_status cpt_denoiser_create(int device, uint64_t seed, cpt_denoise
     return CPT_OK;
 }
 
-// Convolution engine: 0 = mma.sync kernel, 1 = tcgen05 kernel (the default).
+// Convolution engine: 0 = mma.sync kernel, 1 = tcgen05 kernel (the default), 2 = warp-specialised
+// persistent tcgen05 kernel.
 CPT_EXPORT cpt_status cpt_denoiser_set_backend(cpt_denoiser* d, int32_t backend)
 {
-    if (!d || backend < 0 || backend > 1) return fail(CPT_ERR_INVALID_ARGUMENT, "cpt_denoiser_set_backend: 0 or 1");
+    if (!d || backend < 0 || backend > 2) return fail(CPT_ERR_INVALID_ARGUMENT, "cpt_denoiser_set_backend: 0, 1 or 2");
     d->net.backend = backend;
     return CPT_OK;
 }

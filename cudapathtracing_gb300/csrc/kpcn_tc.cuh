@@ -122,6 +122,15 @@ __device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, uint32
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+// The barrier receives one arrival when all of this thread's earlier cp.async copies have landed.
+__device__ __forceinline__ void cp_async_arrive(uint64_t* bar)
+{
+    asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar)
+{
+    asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.shared::cta.b64 st, [%0];\n}\n" ::"r"(smem_addr(bar)) : "memory");
+}
 
 // KC channels per stage (32 or 64; in.C a multiple of KC), cout output channels in grid.y tiles of
 // n_tile (a multiple of 16, <= 256); ncols = tensor-memory columns allocated (power of two >=
@@ -266,6 +275,182 @@ __global__ void __launch_bounds__(128, 1) k_conv3x3_tc(Geo g, View in, const __n
     if (warp == 0) {
         tc_fence_after();
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols) : "memory");
+    }
+}
+
+// Warp-specialised persistent variant (192 threads): warp 0 copies (cp.async, 32 lanes, each lane's
+// copies arrive on the stage's "full" barrier), lane 0 of warp 1 issues the MMAs (waits "full",
+// commits "empty" per stage and "acc full" per tile), warps 2-5 run the epilogue of the previous
+// tile from the other accumulator (wait "acc full", tcgen05.ld, stores, arrive "acc empty").  The
+// CTA loops over pixel tiles x, x + gridDim.x, ...; two accumulators of ncols columns alternate.
+// Every wait is bounded; a timeout sets CPT_DEVERR_ITER and the role stops.
+template <int KC>
+__global__ void __launch_bounds__(192, 1) k_conv3x3_ws(Geo g, View in, const __nv_bfloat16* __restrict__ w,
+                                                        const float* __restrict__ bias, int cout, int n_tile,
+                                                        int ncols, bool relu, View out16, View out32, int* err)
+{
+    constexpr uint32_t lbo = 128, sbo = KC * 16;
+    constexpr int A_BYTES = TC_M * KC * 2;
+    extern __shared__ uint8_t tc_smem_raw[];
+    __shared__ uint64_t full[TC_STAGES], empty[TC_STAGES], accfull[2], accempty[2];
+    __shared__ uint32_t tmem_slot;
+    __shared__ volatile int ws_abort;   // set by any role whose wait timed out; the others stop
+    uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(tc_smem_raw) + 1023) & ~uintptr_t(1023));
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const long P = (long)g.N * g.H * g.W;
+    const long m_tiles = (P + TC_M - 1) / TC_M;
+    const int my_tiles = m_tiles > (long)blockIdx.x ? (int)((m_tiles - 1 - blockIdx.x) / gridDim.x + 1) : 0;
+    const int n_base = blockIdx.y * n_tile;
+    const int cin = in.C;
+    const int stage_bytes = tc_stage_bytes(KC, n_tile);
+    const int steps_per_tap = cin / KC;
+    const int T = 9 * steps_per_tap;
+    const long total = (long)my_tiles * T;
+    const __nv_bfloat16* inp = reinterpret_cast<const __nv_bfloat16*>(in.ptr);
+
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&tmem_slot)),
+                     "r"(2 * ncols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        for (int k = 0; k < TC_STAGES; ++k) {
+            mbar_init(&full[k], 32);
+            mbar_init(&empty[k], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&accfull[b], 1);
+            mbar_init(&accempty[b], 128);
+        }
+        ws_abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_slot;
+
+    if (warp == 0) {
+        // ---------------- producer: per tile, each lane owns rows lane, lane + 32, lane + 64, lane + 96
+        long gs = 0;
+        for (int i = 0; i < my_tiles && !ws_abort; ++i) {
+            const int p0 = (int)(((long)blockIdx.x + (long)i * gridDim.x) * TC_M);
+            int px[4], py[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int p = p0 + lane + 32 * j;
+                px[j] = p % g.W;
+                py[j] = (p / g.W) % g.H;
+            }
+            for (int k = 0; k < T; ++k, ++gs) {
+                const int st = (int)(gs % TC_STAGES);
+                const long fill = gs / TC_STAGES;
+                if (ws_abort) break;
+                if (fill > 0 && !mbar_wait(&empty[st], (uint32_t)((fill - 1) & 1), err)) {
+                    ws_abort = 1;
+                    break;
+                }
+                const int tap = k / steps_per_tap;
+                const int c0 = (k - tap * steps_per_tap) * KC;
+                const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+                const uint32_t As = smem_addr(smem + st * stage_bytes);
+                const uint32_t Bs = As + A_BYTES;
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const int r = lane + 32 * j;
+                    const int p = p0 + r;
+                    const bool ok = p < P && (unsigned)(py[j] + dy) < (unsigned)g.H && (unsigned)(px[j] + dx) < (unsigned)g.W;
+                    const __nv_bfloat16* src = ok ? inp + ((long)p + dy * g.W + dx) * in.cs + in.co + c0 : inp;
+#pragma unroll
+                    for (int kc = 0; kc < KC / 8; ++kc)
+                        cp_async16(As + (r >> 3) * sbo + kc * lbo + (r & 7) * 16, ok ? src + kc * 8 : inp, ok ? 16u : 0u);
+                }
+                const __nv_bfloat16* wt = w + ((size_t)tap * cout + n_base) * cin + c0;
+                for (int c = lane; c < n_tile * (KC / 8); c += 32) {
+                    const int n = c % n_tile, kc = c / n_tile;
+                    cp_async16(Bs + (n >> 3) * sbo + kc * lbo + (n & 7) * 16, wt + (size_t)n * cin + kc * 8, 16u);
+                }
+                cp_async_arrive(&full[st]);
+            }
+        }
+        cp_async_wait<0>();
+    } else if (warp == 1) {
+        // ---------------- MMA issuer
+        if (lane == 0) {
+            const uint32_t idesc = idesc_bf16(TC_M, n_tile);
+            for (long gs = 0; gs < total; ++gs) {
+                const int st = (int)(gs % TC_STAGES);
+                const int i = (int)(gs / T), k = (int)(gs % T);
+                const int buf = i & 1;
+                if (ws_abort) break;
+                if ((k == 0 && i >= 2 && !mbar_wait(&accempty[buf], (uint32_t)(((i >> 1) - 1) & 1), err)) ||
+                    !mbar_wait(&full[st], (uint32_t)((gs / TC_STAGES) & 1), err)) {
+                    ws_abort = 1;
+                    break;
+                }
+                fence_async_smem();
+                tc_fence_after();
+                const uint32_t a0 = smem_addr(smem + st * stage_bytes), b0 = a0 + A_BYTES;
+                const uint32_t d = tmem + (uint32_t)(buf * ncols);
+#pragma unroll
+                for (int j = 0; j < KC / 16; ++j)
+                    umma_bf16(d, smem_desc(a0 + j * 256, lbo, sbo), smem_desc(b0 + j * 256, lbo, sbo), idesc,
+                              (k > 0 || j > 0) ? 1u : 0u);
+                umma_commit(&empty[st]);
+                if (k == T - 1) umma_commit(&accfull[buf]);
+            }
+        }
+    } else {
+        // ---------------- epilogue (warps 2-5 own TMEM lane quarters 2, 3, 0, 1)
+        const int quarter = warp & 3;
+        for (int i = 0; i < my_tiles; ++i) {
+            const int buf = i & 1;
+            if (ws_abort) break;
+            if (!mbar_wait(&accfull[buf], (uint32_t)((i >> 1) & 1), err)) {
+                ws_abort = 1;
+                break;
+            }
+            tc_fence_after();
+            const long p = ((long)blockIdx.x + (long)i * gridDim.x) * TC_M + quarter * 32 + lane;
+            const uint32_t base = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(buf * ncols);
+            for (int c = 0; c < n_tile; c += 16) {
+                float v[16];
+                tmem_ld16(base + (uint32_t)c, v);
+                if (p >= P) continue;
+#pragma unroll
+                for (int q = 0; q < 16; q += 2) {
+                    const int ch = n_base + c + q;
+                    float v0 = v[q], v1 = v[q + 1];
+                    if (bias) {
+                        v0 += bias[ch];
+                        v1 += bias[ch + 1];
+                    }
+                    if (out32.ptr) {
+                        float* o = reinterpret_cast<float*>(out32.ptr) + p * out32.cs + out32.co + ch;
+                        o[0] = v0;
+                        o[1] = v1;
+                    }
+                    if (out16.ptr) {
+                        if (relu) {
+                            v0 = fmaxf(v0, 0.f);
+                            v1 = fmaxf(v1, 0.f);
+                        }
+                        __nv_bfloat16* o = reinterpret_cast<__nv_bfloat16*>(out16.ptr) + p * out16.cs + out16.co + ch;
+                        *reinterpret_cast<unsigned int*>(o) =
+                            pack_bf16(__float2bfloat16_rn(v0), __float2bfloat16_rn(v1));
+                    }
+                }
+            }
+            tc_fence_before();
+            mbar_arrive(&accempty[buf]);
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * ncols) : "memory");
     }
 }
 

@@ -70,7 +70,8 @@ class Denoiser:
         return a
 
     def set_backend(self, backend: int) -> None:
-        """1: tcgen05 convolutions (default), 0: mma.sync convolutions (cpt_denoiser_set_backend)."""
+        """1: tcgen05 convolutions (default), 0: mma.sync convolutions, 2: warp-specialised persistent
+        tcgen05 convolutions (cpt_denoiser_set_backend)."""
         check(lib().cpt_denoiser_set_backend(self.h, backend), "cpt_denoiser_set_backend")
 
     def check(self) -> None:
@@ -138,7 +139,7 @@ def main():
     ap.add_argument("--batch", type=int, default=8)
     ap.add_argument("--crop", type=int, default=256)
     ap.add_argument("--reps", type=int, default=5)
-    ap.add_argument("--backend", type=int, default=None, help="0: mma.sync, 1: tcgen05 (default: the library's)")
+    ap.add_argument("--backend", type=int, default=None, help="0: mma.sync, 1: tcgen05, 2: tcgen05 warp-specialised (default: the library's)")
     a = ap.parse_args()
     W, H = (int(x) for x in a.size.split("x"))
     net = Denoiser(seed=0)

@@ -363,7 +363,8 @@ cpt_status cpt_denoiser_train_step(cpt_denoiser* d, int32_t n, int32_t h, int32_
 cpt_status cpt_denoise(cpt_denoiser* d, int32_t n, int32_t h, int32_t w, const float* rgb, const float* gbuf,
                        float* out, void* stream);
 /* Convolution engine for the forward and input-gradient convolutions: 1 = tcgen05 kernel
- * (tensor-memory accumulators, the default), 0 = warp-level mma.sync kernel. */
+ * (tensor-memory accumulators, the default), 0 = warp-level mma.sync kernel, 2 = warp-specialised
+ * persistent tcgen05 kernel (copy warp, MMA thread, epilogue warps, two accumulators). */
 cpt_status cpt_denoiser_set_backend(cpt_denoiser* d, int32_t backend);
 /* CPT_ERR_TIMEOUT if a tensor-core barrier wait of the passes since the last check timed out. */
 cpt_status cpt_denoiser_check(cpt_denoiser* d);

@@ -49,7 +49,7 @@ def _run(net, rgb, g, tgt):
     return loss, ex, o
 
 
-BACKENDS = pytest.mark.parametrize("backend", [0, 1], ids=["mma_sync", "tcgen05"])
+BACKENDS = pytest.mark.parametrize("backend", [0, 1, 2], ids=["mma_sync", "tcgen05", "tcgen05_ws"])
 
 
 @BACKENDS
