@@ -23,6 +23,8 @@
 // Input features (10 channels, padded to 32 with zeros): log(1 + radiance) (3), albedo (3),
 // octahedral normal (2), depth / (1 + depth) (1, 1 on a miss), and the 3x3 variance of
 // log(1 + luminance) around the pixel (1).
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -713,6 +715,67 @@ cpt_status ensure_geometry(Net& n, int N, int H, int W)
     return CPT_OK;
 }
 
+// Driver entry points of the tensor-map encoders (resolved once through the runtime, so the
+// library does not link libcuda directly); null when the driver does not provide them.
+struct TmaEncoders {
+    PFN_cuTensorMapEncodeIm2col_v12000 im2col = nullptr;
+    PFN_cuTensorMapEncodeTiled_v12000 tiled = nullptr;
+};
+
+const TmaEncoders& tma_encoders()
+{
+    static const TmaEncoders enc = [] {
+        TmaEncoders e;
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeIm2col", &f, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            e.im2col = reinterpret_cast<PFN_cuTensorMapEncodeIm2col_v12000>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            e.tiled = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+        cudaGetLastError();
+        return e;
+    }();
+    return enc;
+}
+
+// Tensor maps of k_conv3x3_ws: the input view as a {C, W, H, N} im2col tensor (window corners
+// -1 .. -1: base pixel = output pixel - 1, tap offsets 0..2, zero fill outside the image), 128
+// pixels x kc channels per load, and the weights [9 * cout][cin] as a tiled tensor with
+// kc x n_tile boxes; swizzle 128 B (kc 64) or 64 B (kc 32), matching smem_desc_sw.  False when a
+// TMA alignment rule does not hold (16-byte base addresses and strides) or the encoders are
+// missing, and the caller uses the cp.async kernel instead.
+bool tma_maps(const Geo& g, const View& in, const __nv_bfloat16* w, int cout, int kc, int nt, CUtensorMap& ta,
+              CUtensorMap& tb)
+{
+    const TmaEncoders& e = tma_encoders();
+    if (!e.im2col || !e.tiled) return false;
+    const char* a = reinterpret_cast<const char*>(in.ptr) + (size_t)in.co * 2;
+    if ((reinterpret_cast<uintptr_t>(a) & 15) || (in.cs * 2) % 16 || (reinterpret_cast<uintptr_t>(w) & 15) ||
+        (in.C * 2) % 16 || in.C % kc || nt % 16 || nt > 256)
+        return false;
+    const CUtensorMapSwizzle sw = kc == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B;
+    const cuuint64_t rs = (cuuint64_t)in.cs * 2;
+    const cuuint64_t adim[4] = {(cuuint64_t)in.C, (cuuint64_t)g.W, (cuuint64_t)g.H, (cuuint64_t)g.N};
+    const cuuint64_t astr[3] = {rs, rs * g.W, rs * g.W * g.H};
+    const int lo[2] = {-1, -1}, hi[2] = {-1, -1};
+    const cuuint32_t one[4] = {1, 1, 1, 1};
+    if (e.im2col(&ta, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<char*>(a), adim, astr, lo, hi, (cuuint32_t)kc,
+                 (cuuint32_t)TC_M, one, CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return false;
+    const cuuint64_t bdim[2] = {(cuuint64_t)in.C, (cuuint64_t)9 * cout};
+    const cuuint64_t bstr[1] = {(cuuint64_t)in.C * 2};
+    const cuuint32_t box[2] = {(cuuint32_t)kc, (cuuint32_t)nt};
+    return e.tiled(&tb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<__nv_bfloat16*>(w), bdim, bstr, box, one,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 // tcgen05 convolution: cout split into grid.y tiles of at most 256 channels (multiples of 16)
 void conv_tc(Net& n, const __nv_bfloat16* w, const float* bias, int cout, bool relu, const Geo& g, View in, View out16,
              View out32, cudaStream_t s)
@@ -723,7 +786,9 @@ void conv_tc(Net& n, const __nv_bfloat16* w, const float* bias, int cout, bool r
     int ncols = 32;
     while (ncols < nt) ncols <<= 1;
     const int kc = in.C % 64 == 0 ? 64 : 32;
-    if (n.backend == 2) {   // warp-specialised persistent kernel, two accumulators per CTA
+    CUtensorMap ta, tb;
+    if (n.backend == 2 && tma_maps(g, in, w, cout, kc, nt, ta, tb)) {
+        // warp-specialised persistent kernel fed by TMA, two accumulators per CTA
         const int max_ctas = 512 / (2 * ncols);
         const int smem = std::max(tc_smem_bytes(kc, nt), TC_SM_SMEM / (max_ctas + 1) + 1024);
         int per_sm = 1;
@@ -733,9 +798,9 @@ void conv_tc(Net& n, const __nv_bfloat16* w, const float* bias, int cout, bool r
         const long m_tiles = (P + TC_M - 1) / TC_M;
         dim3 grid((unsigned)std::min<long>(m_tiles, (long)per_sm * n.sm_count), (unsigned)tiles);
         if (kc == 64)
-            k_conv3x3_ws<64><<<grid, 192, smem, s>>>(g, in, w, bias, cout, nt, ncols, relu, out16, out32, n.err);
+            k_conv3x3_ws<64><<<grid, 192, smem, s>>>(ta, tb, g, in.C, bias, cout, nt, ncols, relu, out16, out32, n.err);
         else
-            k_conv3x3_ws<32><<<grid, 192, smem, s>>>(g, in, w, bias, cout, nt, ncols, relu, out16, out32, n.err);
+            k_conv3x3_ws<32><<<grid, 192, smem, s>>>(ta, tb, g, in.C, bias, cout, nt, ncols, relu, out16, out32, n.err);
         return;
     }
     // shared memory large enough that at most 512 / ncols CTAs fit on an SM (tensor memory)

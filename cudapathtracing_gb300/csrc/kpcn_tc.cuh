@@ -18,6 +18,7 @@
 // CPT_DEVERR_ITER in *err and the CTA stops issuing work (it still frees its tensor memory).
 #pragma once
 
+#include <cuda.h>
 #include <cuda_bf16.h>
 
 namespace cpt {
@@ -122,11 +123,6 @@ __device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, uint32
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
-// The barrier receives one arrival when all of this thread's earlier cp.async copies have landed.
-__device__ __forceinline__ void cp_async_arrive(uint64_t* bar)
-{
-    asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_addr(bar)) : "memory");
-}
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar)
 {
     asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.shared::cta.b64 st, [%0];\n}\n" ::"r"(smem_addr(bar)) : "memory");
@@ -278,18 +274,62 @@ __global__ void __launch_bounds__(128, 1) k_conv3x3_tc(Geo g, View in, const __n
     }
 }
 
-// Warp-specialised persistent variant (192 threads): warp 0 copies (cp.async, 32 lanes, each lane's
-// copies arrive on the stage's "full" barrier), lane 0 of warp 1 issues the MMAs (waits "full",
-// commits "empty" per stage and "acc full" per tile), warps 2-5 run the epilogue of the previous
-// tile from the other accumulator (wait "acc full", tcgen05.ld, stores, arrive "acc empty").  The
-// CTA loops over pixel tiles x, x + gridDim.x, ...; two accumulators of ncols columns alternate.
-// Every wait is bounded; a timeout sets CPT_DEVERR_ITER and the role stops.
+// ---------------------------------------------------------------- TMA-fed warp-specialised engine
+// Shared-memory descriptor of a K-major operand written by TMA with a 128-byte (KC = 64) or
+// 64-byte (KC = 32) swizzle: rows of KC * 2 bytes, 8-row atoms of 8 * KC * 2 bytes (the stride
+// between 8-row groups), leading offset unused, layout field 2 (128 B) or 4 (64 B) in bits 61-63.
 template <int KC>
-__global__ void __launch_bounds__(192, 1) k_conv3x3_ws(Geo g, View in, const __nv_bfloat16* __restrict__ w,
+__device__ __forceinline__ uint64_t smem_desc_sw(uint32_t addr)
+{
+    constexpr uint64_t layout = KC == 64 ? 2ull : 4ull;
+    constexpr uint32_t sbo = 8 * KC * 2;
+    return (uint64_t)((addr >> 4) & 0x3FFFu) | (1ull << 16) | ((uint64_t)(sbo >> 4) << 32) | (1ull << 46) |
+           (layout << 61);
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+
+// im2col load of 128 pixels x KC channels: coordinates (c, w, h, n) of the first pixel's window
+// corner, tap offsets (w, h) in [0, 2]; pixels outside the image read as zeros.
+__device__ __forceinline__ void tma_im2col4(uint32_t dst, const CUtensorMap* map, int c, int x, int y, int n,
+                                            uint16_t ox, uint16_t oy, uint64_t* bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.im2col.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
+        "%5}], [%6], {%7, %8};" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c), "r"(x), "r"(y), "r"(n), "r"(smem_addr(bar)), "h"(ox), "h"(oy)
+        : "memory");
+}
+
+__device__ __forceinline__ void tma_tile2(uint32_t dst, const CUtensorMap* map, int c, int row, uint64_t* bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
+            "r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c), "r"(row), "r"(smem_addr(bar))
+        : "memory");
+}
+
+// Warp-specialised persistent convolution (192 threads).  Lane 0 of warp 0 is the producer: per
+// K step it arms the stage's "full" barrier with the step's byte count and issues two TMA loads,
+// an im2col load of the 128 pixel rows shifted by the tap (tma_a: the input view as a 4-D
+// {C, W, H, N} tensor, window corners -1..-1, so zero padding comes from TMA's out-of-bounds
+// fill) and a tile load of the N weight rows (tma_b: [9 * cout rows][cin]).  Lane 0 of warp 1
+// issues the MMAs (waits "full", commits "empty" per stage and "acc full" per tile); warps 2-5
+// run the epilogue of the previous tile from the other of two tensor-memory accumulators (wait
+// "acc full", tcgen05.ld, stores, arrive "acc empty").  The CTA loops over pixel tiles x,
+// x + gridDim.x, ...  Every wait is bounded; a timeout sets CPT_DEVERR_ITER, the roles stop, and
+// the producer and MMA thread wait (bounded) for their copies and MMAs in flight before the
+// tensor memory is freed.
+template <int KC>
+__global__ void __launch_bounds__(192, 1) k_conv3x3_ws(const __grid_constant__ CUtensorMap tma_a,
+                                                        const __grid_constant__ CUtensorMap tma_b, Geo g, int cin,
                                                         const float* __restrict__ bias, int cout, int n_tile,
                                                         int ncols, bool relu, View out16, View out32, int* err)
 {
-    constexpr uint32_t lbo = 128, sbo = KC * 16;
     constexpr int A_BYTES = TC_M * KC * 2;
     extern __shared__ uint8_t tc_smem_raw[];
     __shared__ uint64_t full[TC_STAGES], empty[TC_STAGES], accfull[2], accempty[2];
@@ -301,12 +341,10 @@ __global__ void __launch_bounds__(192, 1) k_conv3x3_ws(Geo g, View in, const __n
     const long m_tiles = (P + TC_M - 1) / TC_M;
     const int my_tiles = m_tiles > (long)blockIdx.x ? (int)((m_tiles - 1 - blockIdx.x) / gridDim.x + 1) : 0;
     const int n_base = blockIdx.y * n_tile;
-    const int cin = in.C;
     const int stage_bytes = tc_stage_bytes(KC, n_tile);
     const int steps_per_tap = cin / KC;
     const int T = 9 * steps_per_tap;
     const long total = (long)my_tiles * T;
-    const __nv_bfloat16* inp = reinterpret_cast<const __nv_bfloat16*>(in.ptr);
 
     if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&tmem_slot)),
@@ -316,7 +354,7 @@ __global__ void __launch_bounds__(192, 1) k_conv3x3_ws(Geo g, View in, const __n
     }
     if (tid == 0) {
         for (int k = 0; k < TC_STAGES; ++k) {
-            mbar_init(&full[k], 32);
+            mbar_init(&full[k], 1);
             mbar_init(&empty[k], 1);
         }
         for (int b = 0; b < 2; ++b) {
@@ -325,6 +363,8 @@ __global__ void __launch_bounds__(192, 1) k_conv3x3_ws(Geo g, View in, const __n
         }
         ws_abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tma_a)) : "memory");
+        asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tma_b)) : "memory");
     }
     tc_fence_before();
     __syncthreads();
@@ -332,54 +372,40 @@ __global__ void __launch_bounds__(192, 1) k_conv3x3_ws(Geo g, View in, const __n
     const uint32_t tmem = tmem_slot;
 
     if (warp == 0) {
-        // ---------------- producer: per tile, each lane owns rows lane, lane + 32, lane + 64, lane + 96
-        long gs = 0;
-        for (int i = 0; i < my_tiles && !ws_abort; ++i) {
-            const int p0 = (int)(((long)blockIdx.x + (long)i * gridDim.x) * TC_M);
-            int px[4], py[4];
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                const int p = p0 + lane + 32 * j;
-                px[j] = p % g.W;
-                py[j] = (p / g.W) % g.H;
+        // ---------------- producer
+        if (lane == 0) {
+            long gs = 0;
+            for (int i = 0; i < my_tiles && !ws_abort; ++i) {
+                const long p0 = ((long)blockIdx.x + (long)i * gridDim.x) * TC_M;
+                const int x0 = (int)(p0 % g.W), y0 = (int)((p0 / g.W) % g.H), n0 = (int)(p0 / ((long)g.W * g.H));
+                for (int k = 0; k < T; ++k, ++gs) {
+                    const int st = (int)(gs % TC_STAGES);
+                    const long fill = gs / TC_STAGES;
+                    if (ws_abort) break;
+                    if (fill > 0 && !mbar_wait(&empty[st], (uint32_t)((fill - 1) & 1), err)) {
+                        ws_abort = 1;
+                        break;
+                    }
+                    const int tap = k / steps_per_tap;
+                    const int c0 = (k - tap * steps_per_tap) * KC;
+                    const uint32_t As = smem_addr(smem + st * stage_bytes);
+                    mbar_expect_tx(&full[st], (uint32_t)stage_bytes);
+                    tma_im2col4(As, &tma_a, c0, x0 - 1, y0 - 1, n0, (uint16_t)(tap % 3), (uint16_t)(tap / 3), &full[st]);
+                    tma_tile2(As + A_BYTES, &tma_b, c0, tap * cout + n_base, &full[st]);
+                }
             }
-            for (int k = 0; k < T; ++k, ++gs) {
-                const int st = (int)(gs % TC_STAGES);
-                const long fill = gs / TC_STAGES;
-                if (ws_abort) break;
-                if (fill > 0 && !mbar_wait(&empty[st], (uint32_t)((fill - 1) & 1), err)) {
-                    ws_abort = 1;
-                    break;
-                }
-                const int tap = k / steps_per_tap;
-                const int c0 = (k - tap * steps_per_tap) * KC;
-                const int dy = tap / 3 - 1, dx = tap % 3 - 1;
-                const uint32_t As = smem_addr(smem + st * stage_bytes);
-                const uint32_t Bs = As + A_BYTES;
-#pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    const int r = lane + 32 * j;
-                    const int p = p0 + r;
-                    const bool ok = p < P && (unsigned)(py[j] + dy) < (unsigned)g.H && (unsigned)(px[j] + dx) < (unsigned)g.W;
-                    const __nv_bfloat16* src = ok ? inp + ((long)p + dy * g.W + dx) * in.cs + in.co + c0 : inp;
-#pragma unroll
-                    for (int kc = 0; kc < KC / 8; ++kc)
-                        cp_async16(As + (r >> 3) * sbo + kc * lbo + (r & 7) * 16, ok ? src + kc * 8 : inp, ok ? 16u : 0u);
-                }
-                const __nv_bfloat16* wt = w + ((size_t)tap * cout + n_base) * cin + c0;
-                for (int c = lane; c < n_tile * (KC / 8); c += 32) {
-                    const int n = c % n_tile, kc = c / n_tile;
-                    cp_async16(Bs + (n >> 3) * sbo + kc * lbo + (n & 7) * 16, wt + (size_t)n * cin + kc * 8, 16u);
-                }
-                cp_async_arrive(&full[st]);
+            // copies still in flight land before the CTA leaves (every stage's last fill)
+            for (int st = 0; st < TC_STAGES && st < gs; ++st) {
+                const long last = (gs - 1 - st) / TC_STAGES;   // fills of stage st: 0..last
+                mbar_wait(&full[st], (uint32_t)(last & 1), err);
             }
         }
-        cp_async_wait<0>();
     } else if (warp == 1) {
         // ---------------- MMA issuer
         if (lane == 0) {
             const uint32_t idesc = idesc_bf16(TC_M, n_tile);
-            for (long gs = 0; gs < total; ++gs) {
+            long gs = 0;
+            for (; gs < total; ++gs) {
                 const int st = (int)(gs % TC_STAGES);
                 const int i = (int)(gs / T), k = (int)(gs % T);
                 const int buf = i & 1;
@@ -389,17 +415,18 @@ __global__ void __launch_bounds__(192, 1) k_conv3x3_ws(Geo g, View in, const __n
                     ws_abort = 1;
                     break;
                 }
-                fence_async_smem();
                 tc_fence_after();
                 const uint32_t a0 = smem_addr(smem + st * stage_bytes), b0 = a0 + A_BYTES;
                 const uint32_t d = tmem + (uint32_t)(buf * ncols);
 #pragma unroll
                 for (int j = 0; j < KC / 16; ++j)
-                    umma_bf16(d, smem_desc(a0 + j * 256, lbo, sbo), smem_desc(b0 + j * 256, lbo, sbo), idesc,
+                    umma_bf16(d, smem_desc_sw<KC>(a0 + j * 32), smem_desc_sw<KC>(b0 + j * 32), idesc,
                               (k > 0 || j > 0) ? 1u : 0u);
                 umma_commit(&empty[st]);
                 if (k == T - 1) umma_commit(&accfull[buf]);
             }
+            // the MMAs issued so far finish before the tensor memory is freed
+            if (gs > 0) mbar_wait(&empty[(gs - 1) % TC_STAGES], (uint32_t)(((gs - 1) / TC_STAGES) & 1), err);
         }
     } else {
         // ---------------- epilogue (warps 2-5 own TMEM lane quarters 2, 3, 0, 1)
