@@ -28,6 +28,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -283,65 +284,121 @@ __global__ void k_relu_back(View g32, View act, long P, int C, bool relu, View d
 }
 
 // 2x2 average pooling (fine geometry g) and its gradient (added into the fine gradient view)
+// 2x2 average pooling and nearest 2x upsampling over NHWC views, one coarse pixel x 8 channels
+// (BF16, 16-byte accesses) or x 4 channels (FP32 gradients, 16-byte accesses) per work item; channel
+// counts, strides and offsets of the views are multiples of 8 (BF16) / 4 (FP32).
+__device__ __forceinline__ void coarse_pixel(long q, int Wc, int Hc, int& x, int& y, long& b)
+{
+    x = (int)(q % Wc);
+    const long r = q / Wc;
+    y = (int)(r % Hc);
+    b = r / Hc;
+}
+
 __global__ void k_pool(Geo g, View in, View out)
 {
-    const int Ho = g.H / 2, Wo = g.W / 2, C = in.C;
-    const long n = (long)g.N * Ho * Wo * C;
+    const int Ho = g.H / 2, Wo = g.W / 2, C8 = in.C / 8;
+    const long n = (long)g.N * Ho * Wo * C8;
+    const __nv_bfloat16* ip = reinterpret_cast<const __nv_bfloat16*>(in.ptr);
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-        const int c = (int)(i % C);
-        const long q = i / C;
-        const int x = (int)(q % Wo), y = (int)((q / Wo) % Ho), b = (int)(q / ((long)Wo * Ho));
-        const __nv_bfloat16* ip = reinterpret_cast<const __nv_bfloat16*>(in.ptr);
-        const long p00 = ((long)b * g.H + 2 * y) * g.W + 2 * x;
-        float s = __bfloat162float(ip[p00 * in.cs + in.co + c]) + __bfloat162float(ip[(p00 + 1) * in.cs + in.co + c]) +
-                  __bfloat162float(ip[(p00 + g.W) * in.cs + in.co + c]) +
-                  __bfloat162float(ip[(p00 + g.W + 1) * in.cs + in.co + c]);
-        reinterpret_cast<__nv_bfloat16*>(out.ptr)[q * out.cs + out.co + c] = __float2bfloat16_rn(0.25f * s);
+        const int c = (int)(i % C8) * 8;
+        const long q = i / C8;
+        int x, y;
+        long b;
+        coarse_pixel(q, Wo, Ho, x, y, b);
+        const long p00 = (b * g.H + 2 * y) * g.W + 2 * x;
+        const long src[4] = {p00, p00 + 1, p00 + g.W, p00 + g.W + 1};
+        float s[8] = {};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const uint4 v = *reinterpret_cast<const uint4*>(ip + src[k] * in.cs + in.co + c);
+            const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&v);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const float2 f = __bfloat1622float2(h[j]);
+                s[2 * j] += f.x;
+                s[2 * j + 1] += f.y;
+            }
+        }
+        uint4 o;
+        __nv_bfloat162* oh = reinterpret_cast<__nv_bfloat162*>(&o);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) oh[j] = __floats2bfloat162_rn(0.25f * s[2 * j], 0.25f * s[2 * j + 1]);
+        *reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(out.ptr) + q * out.cs + out.co + c) = o;
     }
 }
 
+// gin (fine, FP32) += gradient of the average pool: a quarter of the coarse gradient on each of the
+// four fine pixels
 __global__ void k_pool_back(Geo g, View gout, View gin)
 {
-    const long n = (long)g.N * g.H * g.W * gin.C;
-    const int C = gin.C;
+    const int Ho = g.H / 2, Wo = g.W / 2, C4 = gin.C / 4;
+    const long n = (long)g.N * Ho * Wo * C4;
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-        const int c = (int)(i % C);
-        const long p = i / C;
-        const int x = (int)(p % g.W), y = (int)((p / g.W) % g.H), b = (int)(p / ((long)g.W * g.H));
-        const long q = ((long)b * (g.H / 2) + y / 2) * (g.W / 2) + x / 2;
-        reinterpret_cast<float*>(gin.ptr)[p * gin.cs + gin.co + c] +=
-            0.25f * reinterpret_cast<const float*>(gout.ptr)[q * gout.cs + gout.co + c];
+        const int c = (int)(i % C4) * 4;
+        const long q = i / C4;
+        int x, y;
+        long b;
+        coarse_pixel(q, Wo, Ho, x, y, b);
+        const float4 gq = *reinterpret_cast<const float4*>(reinterpret_cast<const float*>(gout.ptr) + q * gout.cs + gout.co + c);
+        const long p00 = (b * g.H + 2 * y) * g.W + 2 * x;
+        const long dst[4] = {p00, p00 + 1, p00 + g.W, p00 + g.W + 1};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            float4* d = reinterpret_cast<float4*>(reinterpret_cast<float*>(gin.ptr) + dst[k] * gin.cs + gin.co + c);
+            float4 v = *d;
+            v.x += 0.25f * gq.x;
+            v.y += 0.25f * gq.y;
+            v.z += 0.25f * gq.z;
+            v.w += 0.25f * gq.w;
+            *d = v;
+        }
     }
 }
 
 // nearest 2x upsampling from the coarse geometry gc into the fine view, and its gradient
 __global__ void k_upsample(Geo gc, View in, View out)
 {
-    const int Hf = gc.H * 2, Wf = gc.W * 2, C = in.C;
-    const long n = (long)gc.N * Hf * Wf * C;
+    const int C8 = in.C / 8, Wf = gc.W * 2;
+    const long n = (long)gc.N * gc.H * gc.W * C8;
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-        const int c = (int)(i % C);
-        const long p = i / C;
-        const int x = (int)(p % Wf), y = (int)((p / Wf) % Hf), b = (int)(p / ((long)Wf * Hf));
-        const long q = ((long)b * gc.H + y / 2) * gc.W + x / 2;
-        reinterpret_cast<__nv_bfloat16*>(out.ptr)[p * out.cs + out.co + c] =
-            reinterpret_cast<const __nv_bfloat16*>(in.ptr)[q * in.cs + in.co + c];
+        const int c = (int)(i % C8) * 8;
+        const long q = i / C8;
+        int x, y;
+        long b;
+        coarse_pixel(q, gc.W, gc.H, x, y, b);
+        const uint4 v = *reinterpret_cast<const uint4*>(reinterpret_cast<const __nv_bfloat16*>(in.ptr) + q * in.cs + in.co + c);
+        const long p00 = (b * gc.H * 2 + 2 * y) * Wf + 2 * x;
+        const long dst[4] = {p00, p00 + 1, p00 + Wf, p00 + Wf + 1};
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            *reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(out.ptr) + dst[k] * out.cs + out.co + c) = v;
     }
 }
 
 __global__ void k_upsample_back(Geo gc, View gout, View gin)
 {
-    const long n = (long)gc.N * gc.H * gc.W * gin.C;
-    const int C = gin.C, Wf = gc.W * 2;
+    const int C4 = gin.C / 4, Wf = gc.W * 2;
+    const long n = (long)gc.N * gc.H * gc.W * C4;
+    const float* gp = reinterpret_cast<const float*>(gout.ptr);
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-        const int c = (int)(i % C);
-        const long q = i / C;
-        const int x = (int)(q % gc.W), y = (int)((q / gc.W) % gc.H), b = (int)(q / ((long)gc.W * gc.H));
-        const long p00 = ((long)b * gc.H * 2 + 2 * y) * Wf + 2 * x;
-        const float* gp = reinterpret_cast<const float*>(gout.ptr);
-        float s = gp[p00 * gout.cs + gout.co + c] + gp[(p00 + 1) * gout.cs + gout.co + c] +
-                  gp[(p00 + Wf) * gout.cs + gout.co + c] + gp[(p00 + Wf + 1) * gout.cs + gout.co + c];
-        reinterpret_cast<float*>(gin.ptr)[q * gin.cs + gin.co + c] = s;
+        const int c = (int)(i % C4) * 4;
+        const long q = i / C4;
+        int x, y;
+        long b;
+        coarse_pixel(q, gc.W, gc.H, x, y, b);
+        const long p00 = (b * gc.H * 2 + 2 * y) * Wf + 2 * x;
+        const long src[4] = {p00, p00 + 1, p00 + Wf, p00 + Wf + 1};
+        float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const float4 v = *reinterpret_cast<const float4*>(gp + src[k] * gout.cs + gout.co + c);
+            s.x += v.x;
+            s.y += v.y;
+            s.z += v.z;
+            s.w += v.w;
+        }
+        *reinterpret_cast<float4*>(reinterpret_cast<float*>(gin.ptr) + q * gin.cs + gin.co + c) = s;
     }
 }
 
@@ -351,7 +408,7 @@ __device__ __forceinline__ float log_lum(float3 c) { return log1pf(fmaxf(0.f, 0.
 // Images: rgb [N][Hr][Wr][3] f32, gbuf [N][Hr][Wr][8] f32 (renderer layout) -> features
 // [N][H][W][IN_CH] bf16 and radiance [N][H][W][3] f32 on the padded geometry g.
 __global__ void k_features(Geo g, int Hr, int Wr, const float* __restrict__ rgb, const float* __restrict__ gbuf,
-                           __nv_bfloat16* __restrict__ feat, float* __restrict__ rad)
+                           bool gbuf_aligned, __nv_bfloat16* __restrict__ feat, float* __restrict__ rad)
 {
     const long P = (long)g.N * g.H * g.W;
     for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < P; p += (long)gridDim.x * blockDim.x) {
@@ -363,14 +420,22 @@ __global__ void k_features(Geo g, int Hr, int Wr, const float* __restrict__ rgb,
         if (x < Wr && y < Hr) {
             const size_t o = ((size_t)b * Hr + y) * Wr + x;
             r = f3(fmaxf(rgb[3 * o], 0.f), fmaxf(rgb[3 * o + 1], 0.f), fmaxf(rgb[3 * o + 2], 0.f));
-            const float* gb = gbuf + 8 * o;
+            float4 g0, g1;
+            if (gbuf_aligned) {
+                g0 = __ldg(reinterpret_cast<const float4*>(gbuf + 8 * o));
+                g1 = __ldg(reinterpret_cast<const float4*>(gbuf + 8 * o) + 1);
+            } else {
+                const float* gb = gbuf + 8 * o;
+                g0 = make_float4(gb[0], gb[1], gb[2], gb[3]);
+                g1 = make_float4(gb[4], gb[5], gb[6], gb[7]);
+            }
             f[0] = log1pf(r.x);
             f[1] = log1pf(r.y);
             f[2] = log1pf(r.z);
-            f[3] = gb[4];
-            f[4] = gb[5];
-            f[5] = gb[6];
-            float nx = gb[0], ny = gb[1], nz = gb[2];
+            f[3] = g1.x;
+            f[4] = g1.y;
+            f[5] = g1.z;
+            float nx = g0.x, ny = g0.y, nz = g0.z;
             const float l1 = fabsf(nx) + fabsf(ny) + fabsf(nz);
             if (l1 > 0.f) {
                 nx /= l1;
@@ -384,7 +449,7 @@ __global__ void k_features(Geo g, int Hr, int Wr, const float* __restrict__ rgb,
             }
             f[6] = nx;
             f[7] = ny;
-            const float d = gb[3];
+            const float d = g0.w;
             f[8] = d >= CPT_INF_F ? 1.f : d / (1.f + d);
             // 3x3 variance, two-pass (no cancellation of m2 - m^2 in FP32)
             float l9[9], m = 0.f;
@@ -399,10 +464,13 @@ __global__ void k_features(Geo g, int Hr, int Wr, const float* __restrict__ rgb,
             for (int k = 0; k < 9; ++k) var += (l9[k] - m) * (l9[k] - m);
             f[9] = var / 9.f;
         }
-        __nv_bfloat16* fo = feat + p * IN_CH;
+        uint4* fo = reinterpret_cast<uint4*>(feat + p * IN_CH);
 #pragma unroll
-        for (int c = 0; c < IN_CH; c += 2)
-            *reinterpret_cast<unsigned int*>(fo + c) = pack_bf16(__float2bfloat16_rn(f[c]), __float2bfloat16_rn(f[c + 1]));
+        for (int c = 0; c < IN_CH; c += 8)
+            fo[c / 8] = make_uint4(pack_bf16(__float2bfloat16_rn(f[c]), __float2bfloat16_rn(f[c + 1])),
+                                   pack_bf16(__float2bfloat16_rn(f[c + 2]), __float2bfloat16_rn(f[c + 3])),
+                                   pack_bf16(__float2bfloat16_rn(f[c + 4]), __float2bfloat16_rn(f[c + 5])),
+                                   pack_bf16(__float2bfloat16_rn(f[c + 6]), __float2bfloat16_rn(f[c + 7])));
         rad[3 * p] = r.x;
         rad[3 * p + 1] = r.y;
         rad[3 * p + 2] = r.z;
@@ -416,10 +484,20 @@ __global__ void k_apply(Geo g, int Hr, int Wr, const float* __restrict__ logits,
     const long P = (long)g.N * g.H * g.W;
     for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < P; p += (long)gridDim.x * blockDim.x) {
         const int x = (int)(p % g.W), y = (int)((p / g.W) % g.H), b = (int)(p / ((long)g.W * g.H));
-        const float* lg = logits + p * OUT_CH;
+        float lg[28];
+#pragma unroll
+        for (int i = 0; i < 7; ++i) {
+            const float4 v = __ldg(reinterpret_cast<const float4*>(logits + p * OUT_CH) + i);
+            lg[4 * i] = v.x;
+            lg[4 * i + 1] = v.y;
+            lg[4 * i + 2] = v.z;
+            lg[4 * i + 3] = v.w;
+        }
         float mx = lg[0];
+#pragma unroll
         for (int k = 1; k < KTAPS; ++k) mx = fmaxf(mx, lg[k]);
         float e[KTAPS], s = 0.f;
+#pragma unroll
         for (int k = 0; k < KTAPS; ++k) {
             e[k] = expf(lg[k] - mx);
             s += e[k];
@@ -427,6 +505,7 @@ __global__ void k_apply(Geo g, int Hr, int Wr, const float* __restrict__ logits,
         const float inv = 1.f / s;
         float3 acc = f3(0.f, 0.f, 0.f);
         const int xc = min(x, Wr - 1), yc = min(y, Hr - 1);
+#pragma unroll
         for (int k = 0; k < KTAPS; ++k) {
             const float wk = e[k] * inv;
             if (wts) wts[p * KTAPS + k] = wk;
@@ -558,10 +637,14 @@ struct Net {
     __nv_bfloat16 *wf16 = nullptr, *wd16 = nullptr;
     long step = 0;
     bool copies_fresh = false;
-    // convolution engine: 0 = mma.sync kernel, 1 = tcgen05 kernel, 2 = warp-specialised persistent
-    // tcgen05 kernel (both in kpcn_tc.cuh)
-    int backend = 1;
+    // convolution engine: 0 = mma.sync kernel, 1 = tcgen05 kernel with cp.async copies, 2 = TMA-fed
+    // warp-specialised persistent tcgen05 kernels (row tiles where the width allows, else im2col
+    // tiles; k_conv3x3_tc where a TMA alignment rule fails)
+    int backend = 2;
     int sm_count = 152;
+    int ws_per_sm = 4;        // CTAs of k_conv3x3_ws per SM allowed by its registers and threads
+    int ws_smem_max = 0;      // largest dynamic shared memory of one k_conv3x3_ws / _rows CTA
+    bool rows = true;         // backend 2 uses k_conv3x3_rows where the width allows
     int* err = nullptr;
     // activations / gradients for the current geometry
     int N = 0, H = 0, W = 0;
@@ -636,8 +719,22 @@ cpt_status net_init(Net& n, uint64_t seed)
     CPT_CUDA(cudaMemset(n.err, 0, sizeof(int)));
     CPT_CUDA(cudaFuncSetAttribute(k_conv3x3_tc<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM_MAX));
     CPT_CUDA(cudaFuncSetAttribute(k_conv3x3_tc<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM_MAX));
-    CPT_CUDA(cudaFuncSetAttribute(k_conv3x3_ws<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM_MAX));
-    CPT_CUDA(cudaFuncSetAttribute(k_conv3x3_ws<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM_MAX));
+    {
+        int optin = 0;
+        CPT_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, n.device));
+        cudaFuncAttributes fa;
+        CPT_CUDA(cudaFuncGetAttributes(&fa, k_conv3x3_ws<64>));
+        cudaFuncAttributes fr;
+        CPT_CUDA(cudaFuncGetAttributes(&fr, k_conv3x3_rows<64>));
+        n.ws_smem_max = optin - (int)std::max(fa.sharedSizeBytes, fr.sharedSizeBytes);
+        CPT_CUDA(cudaFuncSetAttribute(k_conv3x3_rows<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, n.ws_smem_max));
+        CPT_CUDA(cudaFuncSetAttribute(k_conv3x3_rows<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, n.ws_smem_max));
+        CPT_CUDA(cudaFuncSetAttribute(k_conv3x3_ws<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, n.ws_smem_max));
+        CPT_CUDA(cudaFuncSetAttribute(k_conv3x3_ws<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, n.ws_smem_max));
+        // registers and threads: 65536 / (192 threads x registers rounded to 8 per thread)
+        const int regs = std::max(1, (std::max(fa.numRegs, fr.numRegs) + 7) / 8 * 8);
+        n.ws_per_sm = std::max(1, std::min(2048 / 192, 65536 / (192 * regs)));
+    }
     CPT_CUDA(cudaMemset(n.gw, 0, off * sizeof(float)));
     CPT_CUDA(cudaMemset(n.m, 0, off * sizeof(float)));
     CPT_CUDA(cudaMemset(n.v, 0, off * sizeof(float)));
@@ -776,6 +873,36 @@ bool tma_maps(const Geo& g, const View& in, const __nv_bfloat16* w, int cout, in
                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// Tensor maps of k_conv3x3_rows: the input view as a tiled {C, W, H, N} tensor with kc x 130 x 3
+// x 1 boxes (a row tile with its halo; pixels outside the image read as zeros) and the weights
+// [9 * cout][cin] with kc x n_tile boxes, both with the kc * 2-byte swizzle.
+bool row_maps(const Geo& g, const View& in, const __nv_bfloat16* w, int cout, int kc, int nt, CUtensorMap& ta,
+              CUtensorMap& tb)
+{
+    const TmaEncoders& e = tma_encoders();
+    if (!e.tiled) return false;
+    const char* a = reinterpret_cast<const char*>(in.ptr) + (size_t)in.co * 2;
+    if ((reinterpret_cast<uintptr_t>(a) & 15) || (in.cs * 2) % 16 || (reinterpret_cast<uintptr_t>(w) & 15) ||
+        in.C % kc || nt % 16 || nt > 256 || g.W % TC_M)
+        return false;
+    const CUtensorMapSwizzle sw = kc == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B;
+    const cuuint64_t rs = (cuuint64_t)in.cs * 2;
+    const cuuint64_t adim[4] = {(cuuint64_t)in.C, (cuuint64_t)g.W, (cuuint64_t)g.H, (cuuint64_t)g.N};
+    const cuuint64_t astr[3] = {rs, rs * g.W, rs * g.W * g.H};
+    const cuuint32_t abox[4] = {(cuuint32_t)kc, (cuuint32_t)ROW_PIX, 3, 1};
+    const cuuint32_t one[4] = {1, 1, 1, 1};
+    if (e.tiled(&ta, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<char*>(a), adim, astr, abox, one,
+                CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return false;
+    const cuuint64_t bdim[2] = {(cuuint64_t)in.C, (cuuint64_t)9 * cout};
+    const cuuint64_t bstr[1] = {(cuuint64_t)in.C * 2};
+    const cuuint32_t bbox[2] = {(cuuint32_t)kc, (cuuint32_t)nt};
+    return e.tiled(&tb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<__nv_bfloat16*>(w), bdim, bstr, bbox, one,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 // tcgen05 convolution: cout split into grid.y tiles of at most 256 channels (multiples of 16)
 void conv_tc(Net& n, const __nv_bfloat16* w, const float* bias, int cout, bool relu, const Geo& g, View in, View out16,
              View out32, cudaStream_t s)
@@ -787,20 +914,45 @@ void conv_tc(Net& n, const __nv_bfloat16* w, const float* bias, int cout, bool r
     while (ncols < nt) ncols <<= 1;
     const int kc = in.C % 64 == 0 ? 64 : 32;
     CUtensorMap ta, tb;
-    if (n.backend == 2 && tma_maps(g, in, w, cout, kc, nt, ta, tb)) {
-        // warp-specialised persistent kernel fed by TMA, two accumulators per CTA
+    const int b_bytes = row_b_bytes(in.C, nt, kc);
+    const int a_stage = row_a_stage(kc);
+    if (n.backend == 2 && n.rows && b_bytes + 2 * a_stage + 1024 <= n.ws_smem_max &&
+        row_maps(g, in, w, cout, kc, nt, ta, tb)) {
+        // row tiles with a resident weight block and halo-reusing activation boxes
         const int max_ctas = 512 / (2 * ncols);
-        const int smem = std::max(tc_smem_bytes(kc, nt), TC_SM_SMEM / (max_ctas + 1) + 1024);
-        int per_sm = 1;
-        if (kc == 64) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv3x3_ws<64>, 192, smem);
-        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv3x3_ws<32>, 192, smem);
-        per_sm = std::max(1, std::min(per_sm, max_ctas));
+        const int per_sm = std::max(1, std::min({max_ctas, n.ws_per_sm, TC_SM_SMEM / (b_bytes + 2 * a_stage + 3072)}));
+        const int share = std::min(TC_SM_SMEM / per_sm - 2048, n.ws_smem_max) - 1024;
+        const int nst = std::max(2, std::min(TC_WS_STAGES, (share - b_bytes) / a_stage));
+        const int smem = std::max(b_bytes + nst * a_stage + 1024, TC_SM_SMEM / (max_ctas + 1) + 1024);
+        const long m_tiles = P / TC_M;
+        dim3 grid((unsigned)std::min<long>(m_tiles, (long)per_sm * n.sm_count), (unsigned)tiles);
+        if (kc == 64)
+            k_conv3x3_rows<64><<<grid, 192, smem, s>>>(ta, tb, g, in.C, bias, cout, nt, ncols, nst, relu, out16, out32,
+                                                       n.err);
+        else
+            k_conv3x3_rows<32><<<grid, 192, smem, s>>>(ta, tb, g, in.C, bias, cout, nt, ncols, nst, relu, out16, out32,
+                                                       n.err);
+        return;
+    }
+    if (n.backend == 2 && tma_maps(g, in, w, cout, kc, nt, ta, tb)) {
+        // warp-specialised persistent kernel fed by TMA, two accumulators per CTA: per_sm CTAs per
+        // SM (tensor memory: 2 * ncols columns each), each with as many stages as its share of the
+        // SM's shared memory holds (2 .. TC_WS_STAGES)
+        const int max_ctas = 512 / (2 * ncols);
+        const int stage = tc_stage_bytes(kc, nt);
+        const int per_sm = std::max(1, std::min({max_ctas, n.ws_per_sm, TC_SM_SMEM / (2 * stage + 3072)}));
+        const int share = std::min(TC_SM_SMEM / per_sm - 2048, n.ws_smem_max) - 1024;
+        const int nst = std::max(2, std::min(TC_WS_STAGES, share / stage));
+        // at most max_ctas CTAs of this launch fit on an SM, whatever the occupancy calculator says
+        const int smem = std::max(nst * stage + 1024, TC_SM_SMEM / (max_ctas + 1) + 1024);
         const long m_tiles = (P + TC_M - 1) / TC_M;
         dim3 grid((unsigned)std::min<long>(m_tiles, (long)per_sm * n.sm_count), (unsigned)tiles);
         if (kc == 64)
-            k_conv3x3_ws<64><<<grid, 192, smem, s>>>(ta, tb, g, in.C, bias, cout, nt, ncols, relu, out16, out32, n.err);
+            k_conv3x3_ws<64><<<grid, 192, smem, s>>>(ta, tb, g, in.C, bias, cout, nt, ncols, nst, relu, out16, out32,
+                                                     n.err);
         else
-            k_conv3x3_ws<32><<<grid, 192, smem, s>>>(ta, tb, g, in.C, bias, cout, nt, ncols, relu, out16, out32, n.err);
+            k_conv3x3_ws<32><<<grid, 192, smem, s>>>(ta, tb, g, in.C, bias, cout, nt, ncols, nst, relu, out16, out32,
+                                                     n.err);
         return;
     }
     // shared memory large enough that at most 512 / ncols CTAs fit on an SM (tensor memory)
@@ -861,7 +1013,7 @@ void relu_back(const Geo& g, View g32, View act, int C, bool relu, View dz, cuda
     k_relu_back<<<grid_for(P * C), 256, 0, s>>>(g32, act, P, C, relu, dz);
 }
 
-void forward(Net& n, int Hr, int Wr, cudaStream_t s)
+void forward(Net& n, int Hr, int Wr, bool train, cudaStream_t s)
 {
     const Geo* G = n.geo;
     conv(n, 0, G[0], vw(n.X0, IN_CH, 0, IN_CH), vw(n.A0a, 32, 0, 32), none(), s);
@@ -891,7 +1043,7 @@ void forward(Net& n, int Hr, int Wr, cudaStream_t s)
     conv(n, 16, G[0], vw(n.cat0, 96, 0, 96), vw(n.D0a, 32, 0, 32), none(), s);
     conv(n, 17, G[0], vw(n.D0a, 32, 0, 32), vw(n.D0b, 32, 0, 32), none(), s);
     conv(n, 18, G[0], vw(n.D0b, 32, 0, 32), none(), vw(n.logits, OUT_CH, 0, OUT_CH), s);
-    k_apply<<<grid_for(n.P[0]), 256, 0, s>>>(G[0], Hr, Wr, n.logits, n.rad, n.wts, n.out);
+    k_apply<<<grid_for(n.P[0]), 256, 0, s>>>(G[0], Hr, Wr, n.logits, n.rad, train ? n.wts : nullptr, n.out);
     add_launches(19 + 4 + 4 + 1);
 }
 
@@ -984,7 +1136,8 @@ cpt_status prepare(Net& n, int N, int Hr, int Wr, const float* rgb, const float*
     if (st != CPT_OK) return st;
     st = refresh_copies(n, s);
     if (st != CPT_OK) return st;
-    k_features<<<grid_for(n.P[0]), 256, 0, s>>>(n.geo[0], Hr, Wr, rgb, gbuf, n.X0, n.rad);
+    const bool aligned = (reinterpret_cast<uintptr_t>(gbuf) & 15) == 0;   // G-buffer rows as float4 pairs
+    k_features<<<grid_for(n.P[0]), 256, 0, s>>>(n.geo[0], Hr, Wr, rgb, gbuf, aligned, n.X0, n.rad);
     add_launches(1);
     return CPT_OK;
 }
@@ -1017,8 +1170,8 @@ CPT_EXPORT cpt_status cpt_denoiser_create(int device, uint64_t seed, cpt_denoise
     return CPT_OK;
 }
 
-// Convolution engine: 0 = mma.sync kernel, 1 = tcgen05 kernel (the default), 2 = warp-specialised
-// persistent tcgen05 kernel.
+// Convolution engine: 0 = mma.sync kernel, 1 = tcgen05 kernel with cp.async copies, 2 = TMA-fed
+// warp-specialised persistent tcgen05 kernels (the default).
 CPT_EXPORT cpt_status cpt_denoiser_set_backend(cpt_denoiser* d, int32_t backend)
 {
     if (!d || backend < 0 || backend > 2) return fail(CPT_ERR_INVALID_ARGUMENT, "cpt_denoiser_set_backend: 0, 1 or 2");
@@ -1140,7 +1293,7 @@ CPT_EXPORT cpt_status cpt_denoiser_train_step(cpt_denoiser* d, int32_t n, int32_
     CPT_CUDA(cudaSetDevice(net.device));
     cpt_status st = kpcn::prepare(net, n, h, w, rgb, gbuf, s);
     if (st != CPT_OK) return st;
-    kpcn::forward(net, h, w, s);
+    kpcn::forward(net, h, w, true, s);
     const int lb = kpcn::grid_for(net.P[0]);
     const float scale = 1.0f / (float)((double)n * h * w * 3.0);
     kpcn::k_loss<<<lb, 256, 0, s>>>(net.geo[0], h, w, net.out, target, net.dout, net.loss_part, scale);
@@ -1177,7 +1330,7 @@ CPT_EXPORT cpt_status cpt_denoise(cpt_denoiser* d, int32_t n, int32_t h, int32_t
     CPT_CUDA(cudaSetDevice(net.device));
     cpt_status st = kpcn::prepare(net, n, h, w, rgb, gbuf, s);
     if (st != CPT_OK) return st;
-    kpcn::forward(net, h, w, s);
+    kpcn::forward(net, h, w, false, s);
     kpcn::k_crop<<<kpcn::grid_for((long)n * h * w), 256, 0, s>>>(net.geo[0], h, w, net.out, out);
     add_launches(1);
     CPT_CUDA(cudaGetLastError());

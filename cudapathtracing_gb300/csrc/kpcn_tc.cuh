@@ -274,6 +274,44 @@ __global__ void __launch_bounds__(128, 1) k_conv3x3_tc(Geo g, View in, const __n
     }
 }
 
+// Epilogue of 16 accumulator columns of one pixel: + bias, FP32 view (stored as is) and/or BF16
+// view (after ReLU), with 16-byte stores.  ch (the first channel) is a multiple of 16; the views'
+// channel strides and offsets are multiples of 8.
+__device__ __forceinline__ void store16(long p, int ch, float (&v)[16], const float* __restrict__ bias, bool relu,
+                                        const View& out16, const View& out32)
+{
+    if (bias) {
+#pragma unroll
+        for (int i = 0; i < 16; i += 4) {
+            const float4 b = __ldg(reinterpret_cast<const float4*>(bias + ch + i));
+            v[i] += b.x;
+            v[i + 1] += b.y;
+            v[i + 2] += b.z;
+            v[i + 3] += b.w;
+        }
+    }
+    if (out32.ptr) {
+        float4* o = reinterpret_cast<float4*>(reinterpret_cast<float*>(out32.ptr) + p * out32.cs + out32.co + ch);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) o[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+    }
+    if (out16.ptr) {
+        uint32_t h[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            float a = v[2 * i], b = v[2 * i + 1];
+            if (relu) {
+                a = fmaxf(a, 0.f);
+                b = fmaxf(b, 0.f);
+            }
+            h[i] = pack_bf16(__float2bfloat16_rn(a), __float2bfloat16_rn(b));
+        }
+        uint4* o = reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(out16.ptr) + p * out16.cs + out16.co + ch);
+        o[0] = make_uint4(h[0], h[1], h[2], h[3]);
+        o[1] = make_uint4(h[4], h[5], h[6], h[7]);
+    }
+}
+
 // ---------------------------------------------------------------- TMA-fed warp-specialised engine
 // Shared-memory descriptor of a K-major operand written by TMA with a 128-byte (KC = 64) or
 // 64-byte (KC = 32) swizzle: rows of KC * 2 bytes, 8-row atoms of 8 * KC * 2 bytes (the stride
@@ -304,6 +342,15 @@ __device__ __forceinline__ void tma_im2col4(uint32_t dst, const CUtensorMap* map
         : "memory");
 }
 
+__device__ __forceinline__ void tma_tile4(uint32_t dst, const CUtensorMap* map, int c, int x, int y, int n, uint64_t* bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+        "[%6];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c), "r"(x), "r"(y), "r"(n), "r"(smem_addr(bar))
+        : "memory");
+}
+
 __device__ __forceinline__ void tma_tile2(uint32_t dst, const CUtensorMap* map, int c, int row, uint64_t* bar)
 {
     asm volatile(
@@ -324,15 +371,18 @@ __device__ __forceinline__ void tma_tile2(uint32_t dst, const CUtensorMap* map, 
 // x + gridDim.x, ...  Every wait is bounded; a timeout sets CPT_DEVERR_ITER, the roles stop, and
 // the producer and MMA thread wait (bounded) for their copies and MMAs in flight before the
 // tensor memory is freed.
+constexpr int TC_WS_STAGES = 8;   // most shared-memory stages of k_conv3x3_ws (the launch picks nst)
+
 template <int KC>
 __global__ void __launch_bounds__(192, 1) k_conv3x3_ws(const __grid_constant__ CUtensorMap tma_a,
                                                         const __grid_constant__ CUtensorMap tma_b, Geo g, int cin,
                                                         const float* __restrict__ bias, int cout, int n_tile,
-                                                        int ncols, bool relu, View out16, View out32, int* err)
+                                                        int ncols, int nst, bool relu, View out16, View out32,
+                                                        int* err)
 {
     constexpr int A_BYTES = TC_M * KC * 2;
     extern __shared__ uint8_t tc_smem_raw[];
-    __shared__ uint64_t full[TC_STAGES], empty[TC_STAGES], accfull[2], accempty[2];
+    __shared__ uint64_t full[TC_WS_STAGES], empty[TC_WS_STAGES], accfull[2], accempty[2];
     __shared__ uint32_t tmem_slot;
     __shared__ volatile int ws_abort;   // set by any role whose wait timed out; the others stop
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(tc_smem_raw) + 1023) & ~uintptr_t(1023));
@@ -353,7 +403,7 @@ __global__ void __launch_bounds__(192, 1) k_conv3x3_ws(const __grid_constant__ C
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     if (tid == 0) {
-        for (int k = 0; k < TC_STAGES; ++k) {
+        for (int k = 0; k < nst; ++k) {
             mbar_init(&full[k], 1);
             mbar_init(&empty[k], 1);
         }
@@ -379,8 +429,8 @@ __global__ void __launch_bounds__(192, 1) k_conv3x3_ws(const __grid_constant__ C
                 const long p0 = ((long)blockIdx.x + (long)i * gridDim.x) * TC_M;
                 const int x0 = (int)(p0 % g.W), y0 = (int)((p0 / g.W) % g.H), n0 = (int)(p0 / ((long)g.W * g.H));
                 for (int k = 0; k < T; ++k, ++gs) {
-                    const int st = (int)(gs % TC_STAGES);
-                    const long fill = gs / TC_STAGES;
+                    const int st = (int)(gs % nst);
+                    const long fill = gs / nst;
                     if (ws_abort) break;
                     if (fill > 0 && !mbar_wait(&empty[st], (uint32_t)((fill - 1) & 1), err)) {
                         ws_abort = 1;
@@ -395,8 +445,8 @@ __global__ void __launch_bounds__(192, 1) k_conv3x3_ws(const __grid_constant__ C
                 }
             }
             // copies still in flight land before the CTA leaves (every stage's last fill)
-            for (int st = 0; st < TC_STAGES && st < gs; ++st) {
-                const long last = (gs - 1 - st) / TC_STAGES;   // fills of stage st: 0..last
+            for (int st = 0; st < nst && st < gs; ++st) {
+                const long last = (gs - 1 - st) / nst;   // fills of stage st: 0..last
                 mbar_wait(&full[st], (uint32_t)(last & 1), err);
             }
         }
@@ -406,12 +456,12 @@ __global__ void __launch_bounds__(192, 1) k_conv3x3_ws(const __grid_constant__ C
             const uint32_t idesc = idesc_bf16(TC_M, n_tile);
             long gs = 0;
             for (; gs < total; ++gs) {
-                const int st = (int)(gs % TC_STAGES);
+                const int st = (int)(gs % nst);
                 const int i = (int)(gs / T), k = (int)(gs % T);
                 const int buf = i & 1;
                 if (ws_abort) break;
                 if ((k == 0 && i >= 2 && !mbar_wait(&accempty[buf], (uint32_t)(((i >> 1) - 1) & 1), err)) ||
-                    !mbar_wait(&full[st], (uint32_t)((gs / TC_STAGES) & 1), err)) {
+                    !mbar_wait(&full[st], (uint32_t)((gs / nst) & 1), err)) {
                     ws_abort = 1;
                     break;
                 }
@@ -426,7 +476,7 @@ __global__ void __launch_bounds__(192, 1) k_conv3x3_ws(const __grid_constant__ C
                 if (k == T - 1) umma_commit(&accfull[buf]);
             }
             // the MMAs issued so far finish before the tensor memory is freed
-            if (gs > 0) mbar_wait(&empty[(gs - 1) % TC_STAGES], (uint32_t)(((gs - 1) / TC_STAGES) & 1), err);
+            if (gs > 0) mbar_wait(&empty[(gs - 1) % nst], (uint32_t)(((gs - 1) / nst) & 1), err);
         }
     } else {
         // ---------------- epilogue (warps 2-5 own TMEM lane quarters 2, 3, 0, 1)
@@ -444,30 +494,165 @@ __global__ void __launch_bounds__(192, 1) k_conv3x3_ws(const __grid_constant__ C
             for (int c = 0; c < n_tile; c += 16) {
                 float v[16];
                 tmem_ld16(base + (uint32_t)c, v);
-                if (p >= P) continue;
-#pragma unroll
-                for (int q = 0; q < 16; q += 2) {
-                    const int ch = n_base + c + q;
-                    float v0 = v[q], v1 = v[q + 1];
-                    if (bias) {
-                        v0 += bias[ch];
-                        v1 += bias[ch + 1];
+                if (p < P) store16(p, n_base + c, v, bias, relu, out16, out32);
+            }
+            tc_fence_before();
+            mbar_arrive(&accempty[buf]);
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * ncols) : "memory");
+    }
+}
+
+// ---------------------------------------------------------------- row-tile engine (W % 128 == 0)
+// A tile is 128 pixels of one image row (x0 .. x0 + 127 of row y).  Per KC-channel chunk the
+// producer loads one TMA box of 3 rows x 130 pixels (x0 - 1 .. x0 + 128 of rows y - 1 .. y + 1;
+// zeros outside the image from the out-of-bounds fill) with the KC * 2-byte swizzle, and the nine
+// taps read it through descriptors whose start row is dy * 130 + dx: each input pixel crosses
+// L2 -> SM once per chunk instead of nine times.  The tensor core applies the swizzle to absolute
+// shared-memory address bits (as TMA does), so a start row off the 1024-byte pattern boundary
+// needs no matrix base offset (with the base-offset field set to (address >> 7) & 7 the products
+// are wrong; with 0 they match the oracle bit for bit).  All weights of the CTA's output channels
+// stay resident in shared memory (loaded once, 9 x cin / KC tiles of n_tile x KC); the streamed
+// stages hold only activations.  Roles and waits as in k_conv3x3_ws.
+constexpr int ROW_PIX = TC_M + 2;   // pixels per box row (with halo)
+// bytes of one activation box, and the stage pitch (1024-byte aligned)
+__host__ __device__ constexpr int row_a_tx(int kc) { return 3 * ROW_PIX * kc * 2; }
+__host__ __device__ constexpr int row_a_stage(int kc) { return (row_a_tx(kc) + 1023) / 1024 * 1024; }
+__host__ __device__ constexpr int row_b_bytes(int cin, int n_tile, int kc) { return 9 * (cin / kc) * n_tile * kc * 2; }
+
+template <int KC>
+__global__ void __launch_bounds__(192, 1) k_conv3x3_rows(const __grid_constant__ CUtensorMap tma_a,
+                                                          const __grid_constant__ CUtensorMap tma_b, Geo g, int cin,
+                                                          const float* __restrict__ bias, int cout, int n_tile,
+                                                          int ncols, int nst, bool relu, View out16, View out32,
+                                                          int* err)
+{
+    extern __shared__ uint8_t tc_smem_raw[];
+    __shared__ uint64_t full[TC_WS_STAGES], empty[TC_WS_STAGES], accfull[2], accempty[2], bfull;
+    __shared__ uint32_t tmem_slot;
+    __shared__ volatile int ws_abort;
+    uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(tc_smem_raw) + 1023) & ~uintptr_t(1023));
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const long P = (long)g.N * g.H * g.W;
+    const long m_tiles = P / TC_M;
+    const int my_tiles = m_tiles > (long)blockIdx.x ? (int)((m_tiles - 1 - blockIdx.x) / gridDim.x + 1) : 0;
+    const int n_base = blockIdx.y * n_tile;
+    constexpr int A_STAGE = row_a_stage(KC);
+    const int chunks = cin / KC;
+    const int b_tile = n_tile * KC * 2;                    // one weight tile: n_tile rows x KC channels
+    const int b_bytes = 9 * chunks * b_tile;
+    const uint32_t Bs = smem_addr(smem);
+    const uint32_t As0 = Bs + (uint32_t)b_bytes;            // b_bytes is a multiple of 1024
+    const long total = (long)my_tiles * chunks;
+
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&tmem_slot)),
+                     "r"(2 * ncols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        for (int k = 0; k < nst; ++k) {
+            mbar_init(&full[k], 1);
+            mbar_init(&empty[k], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&accfull[b], 1);
+            mbar_init(&accempty[b], 128);
+        }
+        mbar_init(&bfull, 1);
+        ws_abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tma_a)) : "memory");
+        asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tma_b)) : "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_slot;
+
+    if (warp == 0) {
+        // ---------------- producer: resident weights once, then one activation box per (tile, chunk)
+        if (lane == 0) {
+            mbar_expect_tx(&bfull, (uint32_t)b_bytes);
+            for (int t = 0; t < 9; ++t)
+                for (int c = 0; c < chunks; ++c)
+                    tma_tile2(Bs + (uint32_t)((t * chunks + c) * b_tile), &tma_b, c * KC, t * cout + n_base, &bfull);
+            long gs = 0;
+            for (int i = 0; i < my_tiles && !ws_abort; ++i) {
+                const long p0 = ((long)blockIdx.x + (long)i * gridDim.x) * TC_M;
+                const int x0 = (int)(p0 % g.W), y0 = (int)((p0 / g.W) % g.H), n0 = (int)(p0 / ((long)g.W * g.H));
+                for (int c = 0; c < chunks; ++c, ++gs) {
+                    const int st = (int)(gs % nst);
+                    const long fill = gs / nst;
+                    if (ws_abort) break;
+                    if (fill > 0 && !mbar_wait(&empty[st], (uint32_t)((fill - 1) & 1), err)) {
+                        ws_abort = 1;
+                        break;
                     }
-                    if (out32.ptr) {
-                        float* o = reinterpret_cast<float*>(out32.ptr) + p * out32.cs + out32.co + ch;
-                        o[0] = v0;
-                        o[1] = v1;
-                    }
-                    if (out16.ptr) {
-                        if (relu) {
-                            v0 = fmaxf(v0, 0.f);
-                            v1 = fmaxf(v1, 0.f);
-                        }
-                        __nv_bfloat16* o = reinterpret_cast<__nv_bfloat16*>(out16.ptr) + p * out16.cs + out16.co + ch;
-                        *reinterpret_cast<unsigned int*>(o) =
-                            pack_bf16(__float2bfloat16_rn(v0), __float2bfloat16_rn(v1));
-                    }
+                    mbar_expect_tx(&full[st], (uint32_t)row_a_tx(KC));
+                    tma_tile4(As0 + (uint32_t)(st * A_STAGE), &tma_a, c * KC, x0 - 1, y0 - 1, n0, &full[st]);
                 }
+            }
+            for (int st = 0; st < nst && st < gs; ++st) {
+                const long last = (gs - 1 - st) / nst;
+                mbar_wait(&full[st], (uint32_t)(last & 1), err);
+            }
+            mbar_wait(&bfull, 0u, err);
+        }
+    } else if (warp == 1) {
+        // ---------------- MMA issuer
+        if (lane == 0) {
+            const uint32_t idesc = idesc_bf16(TC_M, n_tile);
+            long gs = 0;
+            if (total > 0 && !mbar_wait(&bfull, 0u, err)) ws_abort = 1;
+            for (; gs < total && !ws_abort; ++gs) {
+                const int st = (int)(gs % nst);
+                const int i = (int)(gs / chunks), c = (int)(gs % chunks);
+                const int buf = i & 1;
+                if ((c == 0 && i >= 2 && !mbar_wait(&accempty[buf], (uint32_t)(((i >> 1) - 1) & 1), err)) ||
+                    !mbar_wait(&full[st], (uint32_t)((gs / nst) & 1), err)) {
+                    ws_abort = 1;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t a0 = As0 + (uint32_t)(st * A_STAGE);
+                const uint32_t d = tmem + (uint32_t)(buf * ncols);
+                for (int t = 0; t < 9; ++t) {
+                    const uint32_t at = a0 + (uint32_t)(((t / 3) * ROW_PIX + (t % 3)) * KC * 2);
+                    const uint32_t bt = Bs + (uint32_t)((t * chunks + c) * b_tile);
+#pragma unroll
+                    for (int j = 0; j < KC / 16; ++j)
+                        umma_bf16(d, smem_desc_sw<KC>(at + j * 32), smem_desc_sw<KC>(bt + j * 32), idesc,
+                                  (c > 0 || t > 0 || j > 0) ? 1u : 0u);
+                }
+                umma_commit(&empty[st]);
+                if (c == chunks - 1) umma_commit(&accfull[buf]);
+            }
+            if (gs > 0) mbar_wait(&empty[(gs - 1) % nst], (uint32_t)(((gs - 1) / nst) & 1), err);
+        }
+    } else {
+        // ---------------- epilogue (warps 2-5 own TMEM lane quarters 2, 3, 0, 1)
+        const int quarter = warp & 3;
+        for (int i = 0; i < my_tiles; ++i) {
+            const int buf = i & 1;
+            if (ws_abort) break;
+            if (!mbar_wait(&accfull[buf], (uint32_t)((i >> 1) & 1), err)) {
+                ws_abort = 1;
+                break;
+            }
+            tc_fence_after();
+            const long p = ((long)blockIdx.x + (long)i * gridDim.x) * TC_M + quarter * 32 + lane;
+            const uint32_t base = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(buf * ncols);
+            for (int c = 0; c < n_tile; c += 16) {
+                float v[16];
+                tmem_ld16(base + (uint32_t)c, v);
+                store16(p, n_base + c, v, bias, relu, out16, out32);
             }
             tc_fence_before();
             mbar_arrive(&accempty[buf]);

@@ -70,8 +70,8 @@ class Denoiser:
         return a
 
     def set_backend(self, backend: int) -> None:
-        """1: tcgen05 convolutions (default), 0: mma.sync convolutions, 2: warp-specialised persistent
-        tcgen05 convolutions (cpt_denoiser_set_backend)."""
+        """2: TMA-fed warp-specialised tcgen05 convolutions (default), 1: tcgen05 convolutions with
+        cp.async copies, 0: mma.sync convolutions (cpt_denoiser_set_backend)."""
         check(lib().cpt_denoiser_set_backend(self.h, backend), "cpt_denoiser_set_backend")
 
     def check(self) -> None:

@@ -362,9 +362,10 @@ cpt_status cpt_denoiser_train_step(cpt_denoiser* d, int32_t n, int32_t h, int32_
                                    void* stream);
 cpt_status cpt_denoise(cpt_denoiser* d, int32_t n, int32_t h, int32_t w, const float* rgb, const float* gbuf,
                        float* out, void* stream);
-/* Convolution engine for the forward and input-gradient convolutions: 1 = tcgen05 kernel
- * (tensor-memory accumulators, the default), 0 = warp-level mma.sync kernel, 2 = warp-specialised
- * persistent tcgen05 kernel (copy warp, MMA thread, epilogue warps, two accumulators). */
+/* Convolution engine for the forward and input-gradient convolutions: 2 = TMA-fed warp-specialised
+ * persistent tcgen05 kernels (the default: row tiles with halo reuse where the padded width is a
+ * multiple of 128, im2col tiles elsewhere), 1 = tcgen05 kernel with cp.async copies, 0 = warp-level
+ * mma.sync kernel. */
 cpt_status cpt_denoiser_set_backend(cpt_denoiser* d, int32_t backend);
 /* CPT_ERR_TIMEOUT if a tensor-core barrier wait of the passes since the last check timed out. */
 cpt_status cpt_denoiser_check(cpt_denoiser* d);

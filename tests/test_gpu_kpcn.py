@@ -52,11 +52,24 @@ def _run(net, rgb, g, tgt):
 BACKENDS = pytest.mark.parametrize("backend", [0, 1, 2], ids=["mma_sync", "tcgen05", "tcgen05_ws"])
 
 
+# Engine 2 switches to row tiles (k_conv3x3_rows) where the padded width is a multiple of 128:
+# a 256-wide batch runs levels 0-1 on row tiles and levels 2-4 on im2col tiles.
+ROW_SHAPE = (1, 32, 256)
+
+
 @BACKENDS
 def test_forward_layers_match_oracle(ctx, backend):
+    _forward_layers(backend, (2, 32, 48))
+
+
+def test_forward_layers_match_oracle_row_tiles(ctx):
+    _forward_layers(2, ROW_SHAPE)
+
+
+def _forward_layers(backend, shape):
     from cudapathtracing_gb300 import denoiser as D
     rng = np.random.default_rng(7)
-    rgb, g, tgt = _batch(rng, 2, 32, 48)
+    rgb, g, tgt = _batch(rng, *shape)
     net = D.Denoiser(seed=3)
     net.set_backend(backend)
     _, ex, o = _run(net, rgb, g, tgt)
@@ -77,9 +90,17 @@ def test_forward_layers_match_oracle(ctx, backend):
 
 @BACKENDS
 def test_gradients_match_oracle(ctx, backend):
+    _gradients(backend, (2, 32, 48))
+
+
+def test_gradients_match_oracle_row_tiles(ctx):
+    _gradients(2, ROW_SHAPE)
+
+
+def _gradients(backend, shape):
     from cudapathtracing_gb300 import denoiser as D
     rng = np.random.default_rng(7)
-    rgb, g, tgt = _batch(rng, 2, 32, 48)
+    rgb, g, tgt = _batch(rng, *shape)
     net = D.Denoiser(seed=3)
     net.set_backend(backend)
     loss, ex, o = _run(net, rgb, g, tgt)
@@ -104,9 +125,18 @@ def test_gradients_match_oracle(ctx, backend):
 @BACKENDS
 def test_denoise_matches_oracle_forward(ctx, backend):
     """Any image size (padded to multiples of 16 inside), batch of 2."""
+    _denoise(backend, (2, 37, 45))
+
+
+def test_denoise_matches_oracle_forward_row_tiles(ctx):
+    """Padded to 32 x 256: row tiles with zero rows and columns of padding."""
+    _denoise(2, (1, 21, 250))
+
+
+def _denoise(backend, shape):
     from cudapathtracing_gb300 import denoiser as D
     rng = np.random.default_rng(9)
-    rgb, g, _ = _batch(rng, 2, 37, 45)
+    rgb, g, _ = _batch(rng, *shape)
     net = D.Denoiser(seed=5)
     net.set_backend(backend)
     out = net.denoise(*_cuda(rgb, g)).cpu().numpy()
