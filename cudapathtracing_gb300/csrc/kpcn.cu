@@ -729,6 +729,7 @@ cpt_status net_init(Net& n, uint64_t seed)
         n.ws_smem_max = optin - (int)std::max(fa.sharedSizeBytes, fr.sharedSizeBytes);
         CPT_CUDA(cudaFuncSetAttribute(k_conv3x3_rows<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, n.ws_smem_max));
         CPT_CUDA(cudaFuncSetAttribute(k_conv3x3_rows<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, n.ws_smem_max));
+        CPT_CUDA(cudaFuncSetAttribute(k_wgrad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, WT_SMEM));
         CPT_CUDA(cudaFuncSetAttribute(k_conv3x3_ws<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, n.ws_smem_max));
         CPT_CUDA(cudaFuncSetAttribute(k_conv3x3_ws<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, n.ws_smem_max));
         // registers and threads: 65536 / (192 threads x registers rounded to 8 per thread)
@@ -993,10 +994,58 @@ void dgrad(Net& n, int i, const Geo& g, View dz, View gin, cudaStream_t s)
     k_conv3x3<4><<<grid, 128, 0, s>>>(g, dz, n.wd16 + n.w16off[i], nullptr, c.cin, false, none(), gin, false);
 }
 
+// Tensor maps of k_wgrad_tc: X as an im2col {cin, W, H, N} tensor (64 channels x 64 pixels per
+// load, window corners -1 .. -1) and dZ as a 2D {cout, P} tensor (64 x 64 boxes), 128-byte swizzle.
+bool wgrad_maps(const Geo& g, const View& x, const View& dz, CUtensorMap& tx, CUtensorMap& tz)
+{
+    const TmaEncoders& e = tma_encoders();
+    if (!e.im2col || !e.tiled) return false;
+    const char* xa = reinterpret_cast<const char*>(x.ptr) + (size_t)x.co * 2;
+    const char* za = reinterpret_cast<const char*>(dz.ptr) + (size_t)dz.co * 2;
+    if ((reinterpret_cast<uintptr_t>(xa) & 15) || (reinterpret_cast<uintptr_t>(za) & 15) || (x.cs * 2) % 16 ||
+        (dz.cs * 2) % 16 || x.C % 32 || dz.C % 32)
+        return false;
+    const cuuint64_t rs = (cuuint64_t)x.cs * 2;
+    const cuuint64_t xdim[4] = {(cuuint64_t)x.C, (cuuint64_t)g.W, (cuuint64_t)g.H, (cuuint64_t)g.N};
+    const cuuint64_t xstr[3] = {rs, rs * g.W, rs * g.W * g.H};
+    const int lo[2] = {-1, -1}, hi[2] = {-1, -1};
+    const cuuint32_t one[4] = {1, 1, 1, 1};
+    if (e.im2col(&tx, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<char*>(xa), xdim, xstr, lo, hi, 64,
+                 (cuuint32_t)WT_PIX, one, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                 CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return false;
+    const cuuint64_t zdim[2] = {(cuuint64_t)dz.C, (cuuint64_t)g.N * g.H * g.W};
+    const cuuint64_t zstr[1] = {(cuuint64_t)dz.cs * 2};
+    const cuuint32_t zbox[2] = {64, (cuuint32_t)WT_PIX};
+    return e.tiled(&tz, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<char*>(za), zdim, zstr, zbox, one,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 void wgrad(Net& n, int i, const Geo& g, View x, View dz, cudaStream_t s)
 {
     const ConvSpec& c = SPECS[i];
     const long P = (long)g.N * g.H * g.W;
+    x.C = c.cin;
+    dz.C = c.cout;
+    CUtensorMap tx, tz;
+    if (n.backend == 2 && wgrad_maps(g, x, dz, tx, tz)) {
+        // tcgen05: grid = pixel chunks x (3 tap rows x 64-channel ci slices x 128-channel co slices),
+        // at least two CTAs per SM, at least two tiles per chunk
+        const int ns = (c.cin + 63) / 64, ms = (c.cout + 127) / 128;
+        const long tiles = (P + WT_PIX - 1) / WT_PIX;
+        long chunks = std::max(1L, std::min<long>({(2L * n.sm_count + 3 * ns * ms - 1) / (3 * ns * ms),
+                                                   (long)WG_CHUNKS, std::max(1L, tiles / 2)}));
+        const int tpc = (int)((tiles + chunks - 1) / chunks);
+        chunks = (tiles + tpc - 1) / tpc;
+        dim3 grid((unsigned)chunks, (unsigned)(3 * ns * ms));
+        k_wgrad_tc<<<grid, 192, WT_SMEM, s>>>(tx, tz, g, c.cin, c.cout, ns, tpc, n.wpart, n.err);
+        k_bgrad<<<(unsigned)chunks, 256, 0, s>>>(dz, P, c.cout, (long)tpc * WT_PIX, n.bpart);
+        const size_t cnt = (size_t)9 * c.cin * c.cout;
+        k_wgrad_reduce<<<grid_for((long)cnt), 256, 0, s>>>(n.wpart, (int)chunks, cnt, n.gw + n.woff[i]);
+        k_wgrad_reduce<<<1, 256, 0, s>>>(n.bpart, (int)chunks, (size_t)c.cout, n.gw + n.boff[i]);
+        return;
+    }
     // chunk = ceil(P / WG_CHUNKS) rounded up to WG_PIX, so there are at most WG_CHUNKS chunks
     const long cp = std::max<long>(WG_PIX, ((P + WG_CHUNKS - 1) / WG_CHUNKS + WG_PIX - 1) / WG_PIX * WG_PIX);
     const int chunks = (int)((P + cp - 1) / cp);

@@ -666,5 +666,169 @@ __global__ void __launch_bounds__(192, 1) k_conv3x3_rows(const __grid_constant__
     }
 }
 
+// ---------------------------------------------------------------- weight gradient on tcgen05
+// dW[tap][ci][co] = sum_p X[p + off(tap), ci] dZ[p, co] as GEMMs with K = pixels.  A CTA owns one
+// tap row dy (three taps), 128 output-gradient channels co (M; dZ channels beyond cout read as zeros)
+// and up to 64 input channels ci (N), and a contiguous chunk of 64-pixel tiles.  Per tile the
+// producer loads dZ (2D map over {cout, P}: two 64-channel boxes of 64 pixels) and, per tap, X
+// through an im2col map (64 channels x 64 pixels shifted by the tap, zeros outside the image);
+// both land in the 128-byte-swizzled MN-major layout (pixel rows of 128 bytes, 8-row groups
+// 1024 bytes apart = SBO, 64-channel atoms 8 KB apart = LBO).  The MMA thread accumulates the three
+// taps' M x N products in tensor memory over the whole chunk (12 MMAs per tile); at the end the
+// epilogue warps write the chunk's partial sums part[chunk][tap][ci][co] (lane = co: coalesced),
+// which a fixed-order reduction over chunks turns into the gradient.
+constexpr int WT_PIX = 64;                       // pixels (K) per tile
+constexpr int WT_ATOM = WT_PIX * 128;            // one 64-channel x 64-pixel box (8 KB)
+constexpr int WT_STAGE = 5 * WT_ATOM;            // dZ (2 atoms) + X for three taps
+constexpr int WT_STAGES = 4;
+constexpr int WT_SMEM = WT_STAGES * WT_STAGE + 1024 + 16384;   // + alignment and slack
+
+// MN-major operand descriptor (128-byte swizzle): LBO = stride of 64-element MN atoms, SBO = stride
+// of 8-row K groups.
+__device__ __forceinline__ uint64_t smem_desc_mn128(uint32_t addr, uint32_t lbo, uint32_t sbo)
+{
+    return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46) | (2ull << 61);
+}
+
+// Instruction descriptor of kind::f16 with both operands MN-major (transpose bits 15, 16).
+__host__ __device__ constexpr uint32_t idesc_bf16_mn(int m, int n) { return idesc_bf16(m, n) | (1u << 15) | (1u << 16); }
+
+__global__ void __launch_bounds__(192, 1) k_wgrad_tc(const __grid_constant__ CUtensorMap tma_x,
+                                                      const __grid_constant__ CUtensorMap tma_z, Geo g, int cin,
+                                                      int cout, int n_slices, int tiles_per_chunk,
+                                                      float* __restrict__ part, int* err)
+{
+    extern __shared__ uint8_t tc_smem_raw[];
+    __shared__ uint64_t full[WT_STAGES], empty[WT_STAGES], done;
+    __shared__ uint32_t tmem_slot;
+    __shared__ volatile int ws_abort;
+    uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(tc_smem_raw) + 1023) & ~uintptr_t(1023));
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const long P = (long)g.N * g.H * g.W;
+    const long n_tiles = (P + WT_PIX - 1) / WT_PIX;
+    const long t0 = (long)blockIdx.x * tiles_per_chunk;
+    const long left = n_tiles - t0;
+    const int my_tiles = left <= 0 ? 0 : (left < tiles_per_chunk ? (int)left : tiles_per_chunk);
+    const int dy_row = blockIdx.y % 3;                       // taps 3 dy_row .. 3 dy_row + 2
+    const int n_base = (blockIdx.y / 3 % n_slices) * 64;     // ci
+    const int m_base = (blockIdx.y / (3 * n_slices)) * 128;  // co
+    const int nn = cin - n_base < 64 ? cin - n_base : 64;  // 32 or 64
+    const uint32_t S0 = smem_addr(smem);
+
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&tmem_slot)),
+                     "r"(256)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        for (int k = 0; k < WT_STAGES; ++k) {
+            mbar_init(&full[k], 1);
+            mbar_init(&empty[k], 1);
+        }
+        mbar_init(&done, 1);
+        ws_abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tma_x)) : "memory");
+        asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tma_z)) : "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            int i = 0;
+            for (; i < my_tiles && !ws_abort; ++i) {
+                const int st = i % WT_STAGES;
+                if (i >= WT_STAGES && !mbar_wait(&empty[st], (uint32_t)(((i / WT_STAGES) - 1) & 1), err)) {
+                    ws_abort = 1;
+                    break;
+                }
+                const long p0 = (t0 + i) * WT_PIX;
+                const int x0 = (int)(p0 % g.W), y0 = (int)((p0 / g.W) % g.H), n0 = (int)(p0 / ((long)g.W * g.H));
+                const uint32_t a = S0 + (uint32_t)(st * WT_STAGE);
+                mbar_expect_tx(&full[st], (uint32_t)WT_STAGE);
+                tma_tile2(a, &tma_z, m_base, (int)p0, &full[st]);
+                tma_tile2(a + WT_ATOM, &tma_z, m_base + 64, (int)p0, &full[st]);
+                for (int t = 0; t < 3; ++t)
+                    tma_im2col4(a + (uint32_t)((2 + t) * WT_ATOM), &tma_x, n_base, x0 - 1, y0 - 1, n0, (uint16_t)t,
+                                (uint16_t)dy_row, &full[st]);
+            }
+            for (int st = 0; st < WT_STAGES && st < i; ++st)
+                mbar_wait(&full[st], (uint32_t)(((i - 1 - st) / WT_STAGES) & 1), err);
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            const uint32_t idesc = idesc_bf16_mn(128, nn);
+            int i = 0;
+            for (; i < my_tiles && !ws_abort; ++i) {
+                const int st = i % WT_STAGES;
+                if (!mbar_wait(&full[st], (uint32_t)((i / WT_STAGES) & 1), err)) {
+                    ws_abort = 1;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t a = S0 + (uint32_t)(st * WT_STAGE);
+                for (int t = 0; t < 3; ++t)
+#pragma unroll
+                    for (int k = 0; k < WT_PIX / 16; ++k)
+                        umma_bf16(tmem + (uint32_t)(t * 64), smem_desc_mn128(a + k * 2048, WT_ATOM, 1024),
+                                  smem_desc_mn128(a + (uint32_t)((2 + t) * WT_ATOM) + k * 2048, WT_ATOM, 1024), idesc,
+                                  (i > 0 || k > 0) ? 1u : 0u);
+                umma_commit(&empty[st]);
+            }
+            if (i > 0) umma_commit(&done);   // completes when every MMA issued above has finished
+            else mbar_arrive(&done);
+        }
+    } else {
+        // ---------------- epilogue: warps 2-5 own TMEM lanes (co) 32 * (warp & 3) ..
+        const int quarter = warp & 3;
+        const bool ok = mbar_wait(&done, 0u, err) && !ws_abort;
+        tc_fence_after();
+        const int co = m_base + quarter * 32 + lane;
+        for (int t = 0; t < 3 && ok; ++t) {
+            float* out = part + ((size_t)blockIdx.x * 9 + dy_row * 3 + t) * cin * cout;
+            for (int c = 0; c < nn; c += 16) {
+                float v[16];
+                tmem_ld16(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(t * 64 + c), v);
+                if (co < cout) {
+#pragma unroll
+                    for (int q = 0; q < 16; ++q) out[(size_t)(n_base + c + q) * cout + co] = v[q];
+                }
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(256) : "memory");
+    }
+}
+
+// Bias gradient partial sums: bpart[chunk][co] = sum of dZ[p, co] over the chunk's pixels, in a fixed
+// order (thread (co, lane8) sums every 8th pixel, then the 8 lanes are added in order).
+__global__ void k_bgrad(View dz, long P, int cout, long chunk_pixels, float* __restrict__ bpart)
+{
+    const long pbeg = (long)blockIdx.x * chunk_pixels, pend = P < pbeg + chunk_pixels ? P : pbeg + chunk_pixels;
+    __shared__ float red[8][160];
+    const __nv_bfloat16* zp = reinterpret_cast<const __nv_bfloat16*>(dz.ptr);
+    const int sub = threadIdx.x / 32, c0 = threadIdx.x % 32;   // 256 threads: 8 pixel lanes x 32 channels
+    for (int c = c0; c < cout; c += 32) {
+        float s = 0.f;
+        for (long p = pbeg + sub; p < pend; p += 8) s += __bfloat162float(zp[p * dz.cs + dz.co + c]);
+        red[sub][c] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x < cout) {
+        float s = 0.f;
+        for (int k = 0; k < 8; ++k) s += red[k][threadIdx.x];
+        bpart[(size_t)blockIdx.x * cout + threadIdx.x] = s;
+    }
+}
+
 }  // namespace kpcn
 }  // namespace cpt
