@@ -260,26 +260,57 @@ __global__ void __launch_bounds__(128) k_wgrad(Geo g, View x, View dz, int cin, 
     }
 }
 
+// grad[i] = sum over chunks of part[chunk][i] in a fixed order: a block of 256 threads covers 32
+// consecutive i; its 8 warps sum chunks w, w + 8, ... and the 8 partial sums are added in order.
 __global__ void k_wgrad_reduce(const float* __restrict__ part, int chunks, size_t n, float* __restrict__ grad)
 {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    __shared__ float red[8][32];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (size_t i0 = (size_t)blockIdx.x * 32; i0 < n; i0 += (size_t)gridDim.x * 32) {
+        const size_t i = i0 + lane;
         float s = 0.f;
-        for (int c = 0; c < chunks; ++c) s += part[(size_t)c * n + i];
-        grad[i] = s;
+        if (i < n)
+            for (int c = w; c < chunks; c += 8) s += part[(size_t)c * n + i];
+        red[w][lane] = s;
+        __syncthreads();
+        if (w == 0 && i < n) {
+            float t = 0.f;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) t += red[k][lane];
+            grad[i] = t;
+        }
+        __syncthreads();
     }
 }
 
 // dZ = dA * (A > 0) (ReLU backward) as BF16; without relu the gradient is converted only
+// dZ (BF16) = FP32 gradient, zeroed where the ReLU's output was not positive; 8 channels per item
+// (16- and 32-byte accesses; channel counts, strides and offsets are multiples of 8).
 __global__ void k_relu_back(View g32, View act, long P, int C, bool relu, View dz)
 {
-    const long n = P * C;
+    const int C8 = C / 8;
+    const long n = P * C8;
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-        const long p = i / C;
-        const int c = (int)(i - p * C);
-        float v = reinterpret_cast<const float*>(g32.ptr)[p * g32.cs + g32.co + c];
-        if (relu && __bfloat162float(reinterpret_cast<const __nv_bfloat16*>(act.ptr)[p * act.cs + act.co + c]) <= 0.f)
-            v = 0.f;
-        reinterpret_cast<__nv_bfloat16*>(dz.ptr)[p * dz.cs + dz.co + c] = __float2bfloat16_rn(v);
+        const long p = i / C8;
+        const int c = (int)(i - p * C8) * 8;
+        const float4* gp = reinterpret_cast<const float4*>(reinterpret_cast<const float*>(g32.ptr) + p * g32.cs + g32.co + c);
+        const float4 u = gp[0], w = gp[1];
+        float v[8] = {u.x, u.y, u.z, u.w, w.x, w.y, w.z, w.w};
+        if (relu) {
+            const uint4 a = *reinterpret_cast<const uint4*>(reinterpret_cast<const __nv_bfloat16*>(act.ptr) + p * act.cs + act.co + c);
+            const __nv_bfloat162* ah = reinterpret_cast<const __nv_bfloat162*>(&a);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const float2 f = __bfloat1622float2(ah[j]);
+                if (f.x <= 0.f) v[2 * j] = 0.f;
+                if (f.y <= 0.f) v[2 * j + 1] = 0.f;
+            }
+        }
+        uint4 o;
+        __nv_bfloat162* oh = reinterpret_cast<__nv_bfloat162*>(&o);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) oh[j] = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
+        *reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(dz.ptr) + p * dz.cs + dz.co + c) = o;
     }
 }
 
@@ -1040,10 +1071,13 @@ void wgrad(Net& n, int i, const Geo& g, View x, View dz, cudaStream_t s)
         chunks = (tiles + tpc - 1) / tpc;
         dim3 grid((unsigned)chunks, (unsigned)(3 * ns * ms));
         k_wgrad_tc<<<grid, 192, WT_SMEM, s>>>(tx, tz, g, c.cin, c.cout, ns, tpc, n.wpart, n.err);
-        k_bgrad<<<(unsigned)chunks, 256, 0, s>>>(dz, P, c.cout, (long)tpc * WT_PIX, n.bpart);
+        // bias partial sums over their own (finer) pixel chunks, 8 channels per thread
+        const long bcp = std::max<long>(256, (P + WG_CHUNKS - 1) / WG_CHUNKS);
+        const int bchunks = (int)((P + bcp - 1) / bcp);
+        k_bgrad<<<(unsigned)bchunks, 256, 0, s>>>(dz, P, c.cout, bcp, n.bpart);
         const size_t cnt = (size_t)9 * c.cin * c.cout;
-        k_wgrad_reduce<<<grid_for((long)cnt), 256, 0, s>>>(n.wpart, (int)chunks, cnt, n.gw + n.woff[i]);
-        k_wgrad_reduce<<<1, 256, 0, s>>>(n.bpart, (int)chunks, (size_t)c.cout, n.gw + n.boff[i]);
+        k_wgrad_reduce<<<grid_for((long)cnt, 32), 256, 0, s>>>(n.wpart, (int)chunks, cnt, n.gw + n.woff[i]);
+        k_wgrad_reduce<<<grid_for((long)c.cout, 32), 256, 0, s>>>(n.bpart, bchunks, (size_t)c.cout, n.gw + n.boff[i]);
         return;
     }
     // chunk = ceil(P / WG_CHUNKS) rounded up to WG_PIX, so there are at most WG_CHUNKS chunks
@@ -1052,8 +1086,8 @@ void wgrad(Net& n, int i, const Geo& g, View x, View dz, cudaStream_t s)
     dim3 grid((unsigned)((c.cin + 31) / 32), (unsigned)(9 * ((c.cout + 31) / 32)), (unsigned)chunks);
     k_wgrad<<<grid, 128, 0, s>>>(g, x, dz, c.cin, c.cout, cp, n.wpart, n.bpart);
     const size_t cnt = (size_t)9 * c.cin * c.cout;
-    k_wgrad_reduce<<<grid_for((long)cnt), 256, 0, s>>>(n.wpart, chunks, cnt, n.gw + n.woff[i]);
-    k_wgrad_reduce<<<1, 256, 0, s>>>(n.bpart, chunks, (size_t)c.cout, n.gw + n.boff[i]);
+    k_wgrad_reduce<<<grid_for((long)cnt, 32), 256, 0, s>>>(n.wpart, chunks, cnt, n.gw + n.woff[i]);
+    k_wgrad_reduce<<<grid_for((long)c.cout, 32), 256, 0, s>>>(n.bpart, chunks, (size_t)c.cout, n.gw + n.boff[i]);
 }
 
 void relu_back(const Geo& g, View g32, View act, int C, bool relu, View dz, cudaStream_t s)

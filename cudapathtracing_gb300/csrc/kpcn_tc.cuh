@@ -809,23 +809,35 @@ __global__ void __launch_bounds__(192, 1) k_wgrad_tc(const __grid_constant__ CUt
     }
 }
 
-// Bias gradient partial sums: bpart[chunk][co] = sum of dZ[p, co] over the chunk's pixels, in a fixed
-// order (thread (co, lane8) sums every 8th pixel, then the 8 lanes are added in order).
+// Bias gradient partial sums: bpart[chunk][co] = sum of dZ[p, co] over the chunk's pixels in a fixed
+// order.  Thread t owns channels 8 (t % C8) .. + 7 (one 16-byte load per pixel) and pixel lane
+// t / C8 of L = 256 / C8 lanes (every L-th pixel); the lanes are then added in order.
 __global__ void k_bgrad(View dz, long P, int cout, long chunk_pixels, float* __restrict__ bpart)
 {
     const long pbeg = (long)blockIdx.x * chunk_pixels, pend = P < pbeg + chunk_pixels ? P : pbeg + chunk_pixels;
-    __shared__ float red[8][160];
+    __shared__ float red[256][8];
     const __nv_bfloat16* zp = reinterpret_cast<const __nv_bfloat16*>(dz.ptr);
-    const int sub = threadIdx.x / 32, c0 = threadIdx.x % 32;   // 256 threads: 8 pixel lanes x 32 channels
-    for (int c = c0; c < cout; c += 32) {
-        float s = 0.f;
-        for (long p = pbeg + sub; p < pend; p += 8) s += __bfloat162float(zp[p * dz.cs + dz.co + c]);
-        red[sub][c] = s;
-    }
+    const int C8 = cout / 8, L = 256 / C8;   // cout <= 160: C8 <= 20, L >= 12
+    const int cg = threadIdx.x % C8, lane = threadIdx.x / C8;
+    float acc[8] = {};
+    if (lane < L)
+        for (long p = pbeg + lane; p < pend; p += L) {
+            const uint4 v = *reinterpret_cast<const uint4*>(zp + p * dz.cs + dz.co + cg * 8);
+            const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&v);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const float2 f = __bfloat1622float2(h[j]);
+                acc[2 * j] += f.x;
+                acc[2 * j + 1] += f.y;
+            }
+        }
+#pragma unroll
+    for (int j = 0; j < 8; ++j) red[threadIdx.x][j] = acc[j];
     __syncthreads();
     if (threadIdx.x < cout) {
+        const int g8 = threadIdx.x / 8, j = threadIdx.x % 8;
         float s = 0.f;
-        for (int k = 0; k < 8; ++k) s += red[k][threadIdx.x];
+        for (int k = 0; k < L; ++k) s += red[k * C8 + g8][j];
         bpart[(size_t)blockIdx.x * cout + threadIdx.x] = s;
     }
 }
