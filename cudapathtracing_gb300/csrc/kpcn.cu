@@ -1062,11 +1062,11 @@ void wgrad(Net& n, int i, const Geo& g, View x, View dz, cudaStream_t s)
     CUtensorMap tx, tz;
     if (n.backend == 2 && wgrad_maps(g, x, dz, tx, tz)) {
         // tcgen05: grid = pixel chunks x (3 tap rows x 64-channel ci slices x 128-channel co slices),
-        // at least two CTAs per SM, at least two tiles per chunk
+        // at most two waves of one CTA per SM (no partial third wave), at least two tiles per chunk
         const int ns = (c.cin + 63) / 64, ms = (c.cout + 127) / 128;
         const long tiles = (P + WT_PIX - 1) / WT_PIX;
-        long chunks = std::max(1L, std::min<long>({(2L * n.sm_count + 3 * ns * ms - 1) / (3 * ns * ms),
-                                                   (long)WG_CHUNKS, std::max(1L, tiles / 2)}));
+        long chunks = std::max(1L, std::min<long>({2L * n.sm_count / (3 * ns * ms), (long)WG_CHUNKS,
+                                                   std::max(1L, tiles / 2)}));
         const int tpc = (int)((tiles + chunks - 1) / chunks);
         chunks = (tiles + tpc - 1) / tpc;
         dim3 grid((unsigned)chunks, (unsigned)(3 * ns * ms));

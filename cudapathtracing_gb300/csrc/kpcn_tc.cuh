@@ -714,6 +714,7 @@ __global__ void __launch_bounds__(192, 1) k_wgrad_tc(const __grid_constant__ CUt
     const int n_base = (blockIdx.y / 3 % n_slices) * 64;     // ci
     const int m_base = (blockIdx.y / (3 * n_slices)) * 128;  // co
     const int nn = cin - n_base < 64 ? cin - n_base : 64;  // 32 or 64
+    const bool two_z = m_base + 64 < cout;
     const uint32_t S0 = smem_addr(smem);
 
     if (warp == 1) {
@@ -750,9 +751,10 @@ __global__ void __launch_bounds__(192, 1) k_wgrad_tc(const __grid_constant__ CUt
                 const long p0 = (t0 + i) * WT_PIX;
                 const int x0 = (int)(p0 % g.W), y0 = (int)((p0 / g.W) % g.H), n0 = (int)(p0 / ((long)g.W * g.H));
                 const uint32_t a = S0 + (uint32_t)(st * WT_STAGE);
-                mbar_expect_tx(&full[st], (uint32_t)WT_STAGE);
+                // the second dZ atom only when it holds channels (otherwise its D rows are never read)
+                mbar_expect_tx(&full[st], (uint32_t)(two_z ? WT_STAGE : WT_STAGE - WT_ATOM));
                 tma_tile2(a, &tma_z, m_base, (int)p0, &full[st]);
-                tma_tile2(a + WT_ATOM, &tma_z, m_base + 64, (int)p0, &full[st]);
+                if (two_z) tma_tile2(a + WT_ATOM, &tma_z, m_base + 64, (int)p0, &full[st]);
                 for (int t = 0; t < 3; ++t)
                     tma_im2col4(a + (uint32_t)((2 + t) * WT_ATOM), &tma_x, n_base, x0 - 1, y0 - 1, n0, (uint16_t)t,
                                 (uint16_t)dy_row, &full[st]);
