@@ -1062,7 +1062,7 @@ void wgrad(Net& n, int i, const Geo& g, View x, View dz, cudaStream_t s)
     CUtensorMap tx, tz;
     if (n.backend == 2 && wgrad_maps(g, x, dz, tx, tz)) {
         // tcgen05: grid = pixel chunks x (3 tap rows x 64-channel ci slices x 128-channel co slices),
-        // at most two waves of one CTA per SM (no partial third wave), at least two tiles per chunk
+        // at most one wave of two CTAs per SM (no partial second wave), at least two tiles per chunk
         const int ns = (c.cin + 63) / 64, ms = (c.cout + 127) / 128;
         const long tiles = (P + WT_PIX - 1) / WT_PIX;
         long chunks = std::max(1L, std::min<long>({2L * n.sm_count / (3 * ns * ms), (long)WG_CHUNKS,

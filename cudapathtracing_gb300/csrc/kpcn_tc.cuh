@@ -673,14 +673,16 @@ __global__ void __launch_bounds__(192, 1) k_conv3x3_rows(const __grid_constant__
 // producer loads dZ (2D map over {cout, P}: two 64-channel boxes of 64 pixels) and, per tap, X
 // through an im2col map (64 channels x 64 pixels shifted by the tap, zeros outside the image);
 // both land in the 128-byte-swizzled MN-major layout (pixel rows of 128 bytes, 8-row groups
-// 1024 bytes apart = SBO, 64-channel atoms 8 KB apart = LBO).  The MMA thread accumulates the three
-// taps' M x N products in tensor memory over the whole chunk (12 MMAs per tile); at the end the
+// 1024 bytes apart = SBO, 64-channel atoms 8 KB apart = LBO).  The three taps' X tiles sit in
+// consecutive atoms, so one MMA with N = 3 x 64 covers all three taps (columns 64 t + ci; channels
+// beyond the slice are zeros); the MMA thread accumulates over the whole chunk (4 MMAs per tile) in
+// tensor memory; at the end the
 // epilogue warps write the chunk's partial sums part[chunk][tap][ci][co] (lane = co: coalesced),
 // which a fixed-order reduction over chunks turns into the gradient.
 constexpr int WT_PIX = 64;                       // pixels (K) per tile
 constexpr int WT_ATOM = WT_PIX * 128;            // one 64-channel x 64-pixel box (8 KB)
 constexpr int WT_STAGE = 5 * WT_ATOM;            // dZ (2 atoms) + X for three taps
-constexpr int WT_STAGES = 4;
+constexpr int WT_STAGES = 2;   // two CTAs per SM fit (shared and tensor memory); faster than one CTA with 4-5 stages
 constexpr int WT_SMEM = WT_STAGES * WT_STAGE + 1024 + 16384;   // + alignment and slack
 
 // MN-major operand descriptor (128-byte swizzle): LBO = stride of 64-element MN atoms, SBO = stride
@@ -764,7 +766,7 @@ __global__ void __launch_bounds__(192, 1) k_wgrad_tc(const __grid_constant__ CUt
         }
     } else if (warp == 1) {
         if (lane == 0) {
-            const uint32_t idesc = idesc_bf16_mn(128, nn);
+            const uint32_t idesc = idesc_bf16_mn(128, 192);
             int i = 0;
             for (; i < my_tiles && !ws_abort; ++i) {
                 const int st = i % WT_STAGES;
@@ -774,12 +776,12 @@ __global__ void __launch_bounds__(192, 1) k_wgrad_tc(const __grid_constant__ CUt
                 }
                 tc_fence_after();
                 const uint32_t a = S0 + (uint32_t)(st * WT_STAGE);
-                for (int t = 0; t < 3; ++t)
+                // the three taps' X tiles are consecutive 64-channel atoms: one N = 192 operand
 #pragma unroll
-                    for (int k = 0; k < WT_PIX / 16; ++k)
-                        umma_bf16(tmem + (uint32_t)(t * 64), smem_desc_mn128(a + k * 2048, WT_ATOM, 1024),
-                                  smem_desc_mn128(a + (uint32_t)((2 + t) * WT_ATOM) + k * 2048, WT_ATOM, 1024), idesc,
-                                  (i > 0 || k > 0) ? 1u : 0u);
+                for (int k = 0; k < WT_PIX / 16; ++k)
+                    umma_bf16(tmem, smem_desc_mn128(a + k * 2048, WT_ATOM, 1024),
+                              smem_desc_mn128(a + (uint32_t)(2 * WT_ATOM) + k * 2048, WT_ATOM, 1024), idesc,
+                              (i > 0 || k > 0) ? 1u : 0u);
                 umma_commit(&empty[st]);
             }
             if (i > 0) umma_commit(&done);   // completes when every MMA issued above has finished
