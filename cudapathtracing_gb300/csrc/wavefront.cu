@@ -202,8 +202,10 @@ __global__ void k_wf_finish(Wf w, RenderArgs a, int groups)
     if (a.rgba8) reinterpret_cast<uchar4*>(a.rgba8)[off] = make_uchar4(to_u8(v.x), to_u8(v.y), to_u8(v.z), 255);
 }
 
+// At most 48 registers (5 blocks of 256 per SM): 62 % occupancy instead of 50 % for a few spilled
+// values, +5.7 % on the 1080p spheres render (the shadow kernel is faster uncapped).
 template <bool WIDE, int SHORT>
-__global__ void __launch_bounds__(256) k_wf_trace(SceneView s, Wf w, int par)
+__global__ void __launch_bounds__(256, 5) k_wf_trace(SceneView s, Wf w, int par)
 {
     const int n = w.cnt[par];
     const int nq = par ^ 1;
