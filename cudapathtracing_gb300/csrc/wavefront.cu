@@ -300,7 +300,9 @@ __global__ void __launch_bounds__(256) k_wf_resolve(SceneView s, Wf w, RenderArg
     }
 }
 
-__global__ void __launch_bounds__(256) k_wf_shade(SceneView s, Wf w, RenderArgs a, int par)
+// At most 64 registers (4 blocks of 256 per SM, 50 % occupancy instead of 37 % at 79 registers):
+// +4.4 % on the 1080p spheres render; 48 registers: +3.7 %.
+__global__ void __launch_bounds__(256, 4) k_wf_shade(SceneView s, Wf w, RenderArgs a, int par)
 {
     const int n = w.cnt[par];
     const int nq = par ^ 1;
