@@ -192,3 +192,22 @@ def test_trained_denoiser_gain(ctx):
     e_plain, e_bil, e_den = T.rmse(rgb, ref), T.rmse(bil, ref), T.rmse(den, ref)
     print(f"RMSE plain {e_plain:.4f} bilateral {e_bil:.4f} denoised {e_den:.4f}")
     assert e_den < 0.5 * e_plain and e_den < e_bil, (e_plain, e_bil, e_den)
+
+
+def test_denoise_unaligned_gbuffer(ctx):
+    """A G-buffer that does not start on a 16-byte boundary (read with scalar loads) gives the
+    same output as an aligned copy (read as float4 pairs)."""
+    import torch
+    from cudapathtracing_gb300 import denoiser as D
+    rng = np.random.default_rng(11)
+    rgb, g, _ = _batch(rng, 1, 32, 48)
+    net = D.Denoiser(seed=5)
+    r_t, g_t = _cuda(rgb, g)
+    want = net.denoise(r_t, g_t)
+    buf = torch.empty(g_t.numel() + 1, device="cuda")
+    buf[1:] = g_t.flatten()
+    g_u = buf[1:].view(g_t.shape)
+    assert g_u.data_ptr() % 16 != 0
+    got = net.denoise(r_t, g_u)
+    net.check()
+    assert torch.equal(got, want)
