@@ -1,10 +1,17 @@
-// kpcn_tc.cuh — 3x3 convolution as an implicit GEMM on the 5th-generation tensor cores
-// (tcgen05.mma, BF16 operands from shared memory, FP32 accumulators in tensor memory).
+// kpcn_tc.cuh — the denoiser's convolutions on the 5th-generation tensor cores (tcgen05.mma,
+// BF16 operands from shared memory, FP32 accumulators in tensor memory).  Four kernels:
+//   k_conv3x3_tc    one output tile per CTA, operands copied by cp.async (engine 1; described
+//                   below)
+//   k_conv3x3_ws    warp-specialised persistent kernel fed by TMA im2col loads (engine 2)
+//   k_conv3x3_rows  as k_conv3x3_ws for widths that are multiples of 128: one halo box per
+//                   channel chunk read by nine row-shifted descriptors, weights resident (engine 2)
+//   k_wgrad_tc      weight gradient with MN-major TMA operands (engine 2), plus k_bgrad
 //
-// One CTA (4 warps) computes a tile of 128 consecutive pixels (the MMA's M) by N output channels
+// k_conv3x3_tc: one CTA (4 warps) computes a tile of 128 consecutive pixels (the MMA's M) by N output channels
 // (N = cout / tiles along grid.y, a multiple of 16, at most 256).  K = 9 taps x cin runs in chunks
-// of KC = 64 (or 32) channels of one tap: the CTA's threads copy the chunk's A (128 pixel rows, shifted by the
-// tap; cp.async zero-fills rows outside the image) and B (N weight rows, [tap][cout][cin]) into
+// of KC = 64 (or 32) channels of one tap: the CTA's threads copy the chunk's A (128 pixel rows,
+// shifted by the tap; cp.async zero-fills rows outside the image) and B (N weight rows,
+// [tap][cout][cin]) into
 // shared memory in the canonical K-major layout without swizzle (8-row x 16-byte core matrices;
 // core matrices adjacent along K are 128 bytes apart, 8-row groups KC * 16 bytes apart); one elected
 // thread issues KC / 16 tcgen05.mma (K = 16 each) per chunk and commits them to the stage's mbarrier.
