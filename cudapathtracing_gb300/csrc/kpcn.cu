@@ -675,7 +675,6 @@ struct Net {
     int sm_count = 152;
     int ws_per_sm = 4;        // CTAs of k_conv3x3_ws per SM allowed by its registers and threads
     int ws_smem_max = 0;      // largest dynamic shared memory of one k_conv3x3_ws / _rows CTA
-    bool rows = true;         // backend 2 uses k_conv3x3_rows where the width allows
     int* err = nullptr;
     // activations / gradients for the current geometry
     int N = 0, H = 0, W = 0;
@@ -948,7 +947,7 @@ void conv_tc(Net& n, const __nv_bfloat16* w, const float* bias, int cout, bool r
     CUtensorMap ta, tb;
     const int b_bytes = row_b_bytes(in.C, nt, kc);
     const int a_stage = row_a_stage(kc);
-    if (n.backend == 2 && n.rows && b_bytes + 2 * a_stage + 1024 <= n.ws_smem_max &&
+    if (n.backend == 2 && b_bytes + 2 * a_stage + 1024 <= n.ws_smem_max &&
         row_maps(g, in, w, cout, kc, nt, ta, tb)) {
         // row tiles with a resident weight block and halo-reusing activation boxes
         const int max_ctas = 512 / (2 * ncols);
