@@ -907,14 +907,14 @@ bool tma_maps(const Geo& g, const View& in, const __nv_bfloat16* w, int cout, in
 // Tensor maps of k_conv3x3_rows: the input view as a tiled {C, W, H, N} tensor with kc x 130 x 3
 // x 1 boxes (a row tile with its halo; pixels outside the image read as zeros) and the weights
 // [9 * cout][cin] with kc x n_tile boxes, both with the kc * 2-byte swizzle.
-bool row_maps(const Geo& g, const View& in, const __nv_bfloat16* w, int cout, int kc, int nt, CUtensorMap& ta,
-              CUtensorMap& tb)
+bool row_maps(const Geo& g, const View& in, const __nv_bfloat16* w, int cout, int kc, int nt, bool pitched,
+              CUtensorMap& ta, CUtensorMap& tb)
 {
     const TmaEncoders& e = tma_encoders();
-    if (!e.tiled) return false;
+    if (!e.tiled || !e.im2col) return false;
     const char* a = reinterpret_cast<const char*>(in.ptr) + (size_t)in.co * 2;
     if ((reinterpret_cast<uintptr_t>(a) & 15) || (in.cs * 2) % 16 || (reinterpret_cast<uintptr_t>(w) & 15) ||
-        in.C % kc || nt % 16 || nt > 256 || g.W % TC_M)
+        in.C % kc || nt % 16 || nt > 256 || (!pitched && g.W % TC_M))
         return false;
     const CUtensorMapSwizzle sw = kc == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B;
     const cuuint64_t rs = (cuuint64_t)in.cs * 2;
@@ -922,10 +922,17 @@ bool row_maps(const Geo& g, const View& in, const __nv_bfloat16* w, int cout, in
     const cuuint64_t astr[3] = {rs, rs * g.W, rs * g.W * g.H};
     const cuuint32_t abox[4] = {(cuuint32_t)kc, (cuuint32_t)ROW_PIX, 3, 1};
     const cuuint32_t one[4] = {1, 1, 1, 1};
-    if (e.tiled(&ta, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<char*>(a), adim, astr, abox, one,
-                CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-        return false;
+    // pitched: base positions x in [-1, W - 1] (W + 1 per row: lower corner -1, upper corner 0),
+    // y in [-1, H - 2]; corners listed W first, like the dimensions
+    const int lo[2] = {-1, -1}, hi[2] = {0, -1};
+    const CUresult ra =
+        pitched ? e.im2col(&ta, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<char*>(a), adim, astr, lo, hi,
+                           (cuuint32_t)kc, (cuuint32_t)ROW_PIX, one, CU_TENSOR_MAP_INTERLEAVE_NONE, sw,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE)
+                : e.tiled(&ta, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<char*>(a), adim, astr, abox, one,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (ra != CUDA_SUCCESS) return false;
     const cuuint64_t bdim[2] = {(cuuint64_t)in.C, (cuuint64_t)9 * cout};
     const cuuint64_t bstr[1] = {(cuuint64_t)in.C * 2};
     const cuuint32_t bbox[2] = {(cuuint32_t)kc, (cuuint32_t)nt};
@@ -945,24 +952,32 @@ void conv_tc(Net& n, const __nv_bfloat16* w, const float* bias, int cout, bool r
     while (ncols < nt) ncols <<= 1;
     const int kc = in.C % 64 == 0 ? 64 : 32;
     CUtensorMap ta, tb;
-    const int b_bytes = row_b_bytes(in.C, nt, kc);
-    const int a_stage = row_a_stage(kc);
-    if (n.backend == 2 && b_bytes + 2 * a_stage + 1024 <= n.ws_smem_max &&
-        row_maps(g, in, w, cout, kc, nt, ta, tb)) {
-        // row tiles with a resident weight block and halo-reusing activation boxes
+    // row tiles: halo-reusing activation boxes (tiled when W % 128 == 0, else im2col over the W + 1
+    // pitch), weights resident when they fit next to two stages, else streamed with each stage
+    RowPlan rp;
+    rp.pitched = g.W % TC_M != 0;
+    rp.a_seg = rp.pitched ? (ROW_PIX * kc * 2 + 1023) / 1024 * 1024 : ROW_PIX * kc * 2;
+    rp.a_region = (3 * rp.a_seg + 1023) / 1024 * 1024;
+    const int b_all = row_b_bytes(in.C, nt, kc), b_stage = 9 * nt * kc * 2;
+    rp.resident = b_all + 2 * rp.a_region + 1024 <= n.ws_smem_max;
+    rp.stage = rp.a_region + (rp.resident ? 0 : b_stage);
+    const int b_bytes = rp.resident ? b_all : 0;
+    if (n.backend == 2 && b_bytes + 2 * rp.stage + 1024 <= n.ws_smem_max &&
+        row_maps(g, in, w, cout, kc, nt, rp.pitched, ta, tb)) {
         const int max_ctas = 512 / (2 * ncols);
-        const int per_sm = std::max(1, std::min({max_ctas, n.ws_per_sm, TC_SM_SMEM / (b_bytes + 2 * a_stage + 3072)}));
+        const int per_sm = std::max(1, std::min({max_ctas, n.ws_per_sm, TC_SM_SMEM / (b_bytes + 2 * rp.stage + 3072)}));
         const int share = std::min(TC_SM_SMEM / per_sm - 2048, n.ws_smem_max) - 1024;
-        const int nst = std::max(2, std::min(TC_WS_STAGES, (share - b_bytes) / a_stage));
-        const int smem = std::max(b_bytes + nst * a_stage + 1024, TC_SM_SMEM / (max_ctas + 1) + 1024);
-        const long m_tiles = P / TC_M;
+        const int nst = std::max(2, std::min(TC_WS_STAGES, (share - b_bytes) / rp.stage));
+        const int smem = std::max(b_bytes + nst * rp.stage + 1024, TC_SM_SMEM / (max_ctas + 1) + 1024);
+        const long q = (long)g.N * g.H * (rp.pitched ? g.W + 1 : g.W);
+        const long m_tiles = (q + TC_M - 1) / TC_M;
         dim3 grid((unsigned)std::min<long>(m_tiles, (long)per_sm * n.sm_count), (unsigned)tiles);
         if (kc == 64)
-            k_conv3x3_rows<64><<<grid, 192, smem, s>>>(ta, tb, g, in.C, bias, cout, nt, ncols, nst, relu, out16, out32,
-                                                       n.err);
+            k_conv3x3_rows<64><<<grid, 192, smem, s>>>(ta, tb, g, in.C, bias, cout, nt, ncols, nst, rp, relu, out16,
+                                                       out32, n.err);
         else
-            k_conv3x3_rows<32><<<grid, 192, smem, s>>>(ta, tb, g, in.C, bias, cout, nt, ncols, nst, relu, out16, out32,
-                                                       n.err);
+            k_conv3x3_rows<32><<<grid, 192, smem, s>>>(ta, tb, g, in.C, bias, cout, nt, ncols, nst, rp, relu, out16,
+                                                       out32, n.err);
         return;
     }
     if (n.backend == 2 && tma_maps(g, in, w, cout, kc, nt, ta, tb)) {

@@ -515,29 +515,44 @@ __global__ void __launch_bounds__(192, 1) k_conv3x3_ws(const __grid_constant__ C
     }
 }
 
-// ---------------------------------------------------------------- row-tile engine (W % 128 == 0)
-// A tile is 128 pixels of one image row (x0 .. x0 + 127 of row y).  Per KC-channel chunk the
-// producer loads one TMA box of 3 rows x 130 pixels (x0 - 1 .. x0 + 128 of rows y - 1 .. y + 1;
-// zeros outside the image from the out-of-bounds fill) with the KC * 2-byte swizzle, and the nine
-// taps read it through descriptors whose start row is dy * 130 + dx: each input pixel crosses
-// L2 -> SM once per chunk instead of nine times.  The tensor core applies the swizzle to absolute
+// ---------------------------------------------------------------- row-tile engine
+// A tile is 128 consecutive positions.  When W % 128 == 0 they are 128 pixels of one image row
+// (x0 .. x0 + 127 of row y) and per KC-channel chunk the producer loads one TMA box of 3 rows x 130
+// pixels (x0 - 1 .. x0 + 128 of rows y - 1 .. y + 1; zeros outside the image from the
+// out-of-bounds fill) with the KC * 2-byte swizzle.  Other widths use positions of pitch W + 1:
+// three im2col boxes of 130 positions (one per dy) whose bounding box has one extra column per row
+// that reads as zeros, so position q + dx is still the left/centre/right neighbour of position q
+// (across a row end it lands on the zero column); the position W of each row is a padding output
+// the epilogue skips.  Either way the nine taps read the rows through descriptors whose start row
+// is dy * (segment) + dx: each input pixel crosses L2 -> SM once per chunk instead of nine times.  The tensor core applies the swizzle to absolute
 // shared-memory address bits (as TMA does), so a start row off the 1024-byte pattern boundary
 // needs no matrix base offset (with the base-offset field set to (address >> 7) & 7 the products
-// are wrong; with 0 they match the oracle bit for bit).  All weights of the CTA's output channels
-// stay resident in shared memory (loaded once, 9 x cin / KC tiles of n_tile x KC); the streamed
-// stages hold only activations.  Roles and waits as in k_conv3x3_ws.
+// are wrong; with 0 they match the oracle bit for bit).  The weights of the CTA's output channels
+// stay resident in shared memory (loaded once, 9 x cin / KC tiles of n_tile x KC) when they fit,
+// else each stage also carries its chunk's nine weight tiles.  Roles and waits as in
+// k_conv3x3_ws.
 constexpr int ROW_PIX = TC_M + 2;   // pixels per box row (with halo)
-// bytes of one activation box, and the stage pitch (1024-byte aligned)
+// bytes of the activation rows of one stage (3 rows of 130 pixels x kc channels)
 __host__ __device__ constexpr int row_a_tx(int kc) { return 3 * ROW_PIX * kc * 2; }
-__host__ __device__ constexpr int row_a_stage(int kc) { return (row_a_tx(kc) + 1023) / 1024 * 1024; }
 __host__ __device__ constexpr int row_b_bytes(int cin, int n_tile, int kc) { return 9 * (cin / kc) * n_tile * kc * 2; }
+
+// Shared-memory plan of a k_conv3x3_rows launch.  pitched: the activation rows come from three
+// im2col boxes (one per dy, each at a 1024-byte aligned segment a_seg apart) over positions of
+// pitch W + 1 (the bounding box's extra column per row reads as zeros, so the horizontal taps stay
+// row shifts whatever the width); else from one tiled box of 3 contiguous segments (W % 128 == 0).
+// resident: all weights loaded once before the stages; else each stage carries its chunk's nine
+// weight tiles after the activation region (a_region bytes).
+struct RowPlan {
+    int a_seg, a_region, stage;
+    bool pitched, resident;
+};
 
 template <int KC>
 __global__ void __launch_bounds__(192, 1) k_conv3x3_rows(const __grid_constant__ CUtensorMap tma_a,
                                                           const __grid_constant__ CUtensorMap tma_b, Geo g, int cin,
                                                           const float* __restrict__ bias, int cout, int n_tile,
-                                                          int ncols, int nst, bool relu, View out16, View out32,
-                                                          int* err)
+                                                          int ncols, int nst, RowPlan rp, bool relu, View out16,
+                                                          View out32, int* err)
 {
     extern __shared__ uint8_t tc_smem_raw[];
     __shared__ uint64_t full[TC_WS_STAGES], empty[TC_WS_STAGES], accfull[2], accempty[2], bfull;
@@ -545,14 +560,16 @@ __global__ void __launch_bounds__(192, 1) k_conv3x3_rows(const __grid_constant__
     __shared__ volatile int ws_abort;
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(tc_smem_raw) + 1023) & ~uintptr_t(1023));
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const long P = (long)g.N * g.H * g.W;
-    const long m_tiles = P / TC_M;
+    // tile positions: pixels (tiled boxes) or positions of the W + 1 pitch (im2col boxes, whose
+    // position W of a row is a padding output that the epilogue skips)
+    const int Wq = rp.pitched ? g.W + 1 : g.W;
+    const long Q = (long)g.N * g.H * Wq;
+    const long m_tiles = (Q + TC_M - 1) / TC_M;
     const int my_tiles = m_tiles > (long)blockIdx.x ? (int)((m_tiles - 1 - blockIdx.x) / gridDim.x + 1) : 0;
     const int n_base = blockIdx.y * n_tile;
-    constexpr int A_STAGE = row_a_stage(KC);
     const int chunks = cin / KC;
     const int b_tile = n_tile * KC * 2;                    // one weight tile: n_tile rows x KC channels
-    const int b_bytes = 9 * chunks * b_tile;
+    const int b_bytes = rp.resident ? 9 * chunks * b_tile : 0;
     const uint32_t Bs = smem_addr(smem);
     const uint32_t As0 = Bs + (uint32_t)b_bytes;            // b_bytes is a multiple of 1024
     const long total = (long)my_tiles * chunks;
@@ -584,16 +601,22 @@ __global__ void __launch_bounds__(192, 1) k_conv3x3_rows(const __grid_constant__
     const uint32_t tmem = tmem_slot;
 
     if (warp == 0) {
-        // ---------------- producer: resident weights once, then one activation box per (tile, chunk)
+        // ---------------- producer: resident weights once, then per (tile, chunk) the activation
+        // rows (one tiled box, or three im2col boxes, one per dy) and, when not resident, the
+        // chunk's nine weight tiles
         if (lane == 0) {
-            mbar_expect_tx(&bfull, (uint32_t)b_bytes);
-            for (int t = 0; t < 9; ++t)
-                for (int c = 0; c < chunks; ++c)
-                    tma_tile2(Bs + (uint32_t)((t * chunks + c) * b_tile), &tma_b, c * KC, t * cout + n_base, &bfull);
+            if (rp.resident) {
+                mbar_expect_tx(&bfull, (uint32_t)b_bytes);
+                for (int t = 0; t < 9; ++t)
+                    for (int c = 0; c < chunks; ++c)
+                        tma_tile2(Bs + (uint32_t)((t * chunks + c) * b_tile), &tma_b, c * KC, t * cout + n_base,
+                                  &bfull);
+            }
+            const uint32_t tx = (uint32_t)(row_a_tx(KC) + (rp.resident ? 0 : 9 * b_tile));
             long gs = 0;
             for (int i = 0; i < my_tiles && !ws_abort; ++i) {
                 const long p0 = ((long)blockIdx.x + (long)i * gridDim.x) * TC_M;
-                const int x0 = (int)(p0 % g.W), y0 = (int)((p0 / g.W) % g.H), n0 = (int)(p0 / ((long)g.W * g.H));
+                const int x0 = (int)(p0 % Wq), y0 = (int)((p0 / Wq) % g.H), n0 = (int)(p0 / ((long)Wq * g.H));
                 for (int c = 0; c < chunks; ++c, ++gs) {
                     const int st = (int)(gs % nst);
                     const long fill = gs / nst;
@@ -602,22 +625,33 @@ __global__ void __launch_bounds__(192, 1) k_conv3x3_rows(const __grid_constant__
                         ws_abort = 1;
                         break;
                     }
-                    mbar_expect_tx(&full[st], (uint32_t)row_a_tx(KC));
-                    tma_tile4(As0 + (uint32_t)(st * A_STAGE), &tma_a, c * KC, x0 - 1, y0 - 1, n0, &full[st]);
+                    const uint32_t a = As0 + (uint32_t)(st * rp.stage);
+                    mbar_expect_tx(&full[st], tx);
+                    if (rp.pitched) {
+                        for (int dy = 0; dy < 3; ++dy)
+                            tma_im2col4(a + (uint32_t)(dy * rp.a_seg), &tma_a, c * KC, x0 - 1, y0 - 1, n0, (uint16_t)0,
+                                        (uint16_t)dy, &full[st]);
+                    } else {
+                        tma_tile4(a, &tma_a, c * KC, x0 - 1, y0 - 1, n0, &full[st]);
+                    }
+                    if (!rp.resident)
+                        for (int t = 0; t < 9; ++t)
+                            tma_tile2(a + (uint32_t)(rp.a_region + t * b_tile), &tma_b, c * KC, t * cout + n_base,
+                                      &full[st]);
                 }
             }
             for (int st = 0; st < nst && st < gs; ++st) {
                 const long last = (gs - 1 - st) / nst;
                 mbar_wait(&full[st], (uint32_t)(last & 1), err);
             }
-            mbar_wait(&bfull, 0u, err);
+            if (rp.resident) mbar_wait(&bfull, 0u, err);
         }
     } else if (warp == 1) {
         // ---------------- MMA issuer
         if (lane == 0) {
             const uint32_t idesc = idesc_bf16(TC_M, n_tile);
             long gs = 0;
-            if (total > 0 && !mbar_wait(&bfull, 0u, err)) ws_abort = 1;
+            if (rp.resident && total > 0 && !mbar_wait(&bfull, 0u, err)) ws_abort = 1;
             for (; gs < total && !ws_abort; ++gs) {
                 const int st = (int)(gs % nst);
                 const int i = (int)(gs / chunks), c = (int)(gs % chunks);
@@ -628,11 +662,12 @@ __global__ void __launch_bounds__(192, 1) k_conv3x3_rows(const __grid_constant__
                     break;
                 }
                 tc_fence_after();
-                const uint32_t a0 = As0 + (uint32_t)(st * A_STAGE);
+                const uint32_t a0 = As0 + (uint32_t)(st * rp.stage);
                 const uint32_t d = tmem + (uint32_t)(buf * ncols);
                 for (int t = 0; t < 9; ++t) {
-                    const uint32_t at = a0 + (uint32_t)(((t / 3) * ROW_PIX + (t % 3)) * KC * 2);
-                    const uint32_t bt = Bs + (uint32_t)((t * chunks + c) * b_tile);
+                    const uint32_t at = a0 + (uint32_t)((t / 3) * rp.a_seg + (t % 3) * KC * 2);
+                    const uint32_t bt = rp.resident ? Bs + (uint32_t)((t * chunks + c) * b_tile)
+                                                    : a0 + (uint32_t)(rp.a_region + t * b_tile);
 #pragma unroll
                     for (int j = 0; j < KC / 16; ++j)
                         umma_bf16(d, smem_desc_sw<KC>(at + j * 32), smem_desc_sw<KC>(bt + j * 32), idesc,
@@ -654,12 +689,15 @@ __global__ void __launch_bounds__(192, 1) k_conv3x3_rows(const __grid_constant__
                 break;
             }
             tc_fence_after();
-            const long p = ((long)blockIdx.x + (long)i * gridDim.x) * TC_M + quarter * 32 + lane;
+            const long q = ((long)blockIdx.x + (long)i * gridDim.x) * TC_M + quarter * 32 + lane;
+            const int qx = (int)(q % Wq);
+            const bool valid = q < Q && qx < g.W;
+            const long p = (q / Wq) * g.W + qx;
             const uint32_t base = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(buf * ncols);
             for (int c = 0; c < n_tile; c += 16) {
                 float v[16];
                 tmem_ld16(base + (uint32_t)c, v);
-                store16(p, n_base + c, v, bias, relu, out16, out32);
+                if (valid) store16(p, n_base + c, v, bias, relu, out16, out32);
             }
             tc_fence_before();
             mbar_arrive(&accempty[buf]);
