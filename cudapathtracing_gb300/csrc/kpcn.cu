@@ -675,6 +675,7 @@ struct Net {
     int sm_count = 152;
     int ws_per_sm = 4;        // CTAs of k_conv3x3_ws per SM allowed by its registers and threads
     int ws_smem_max = 0;      // largest dynamic shared memory of one k_conv3x3_ws / _rows CTA
+    int rows_apply_per_sm = 2;   // CTAs per SM of the row-tile kernel with the fused apply epilogue
     int* err = nullptr;
     // activations / gradients for the current geometry
     int N = 0, H = 0, W = 0;
@@ -755,10 +756,18 @@ cpt_status net_init(Net& n, uint64_t seed)
         cudaFuncAttributes fa;
         CPT_CUDA(cudaFuncGetAttributes(&fa, k_conv3x3_ws<64>));
         cudaFuncAttributes fr;
-        CPT_CUDA(cudaFuncGetAttributes(&fr, k_conv3x3_rows<64>));
+        CPT_CUDA(cudaFuncGetAttributes(&fr, k_conv3x3_rows<64, false>));
         n.ws_smem_max = optin - (int)std::max(fa.sharedSizeBytes, fr.sharedSizeBytes);
-        CPT_CUDA(cudaFuncSetAttribute(k_conv3x3_rows<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, n.ws_smem_max));
-        CPT_CUDA(cudaFuncSetAttribute(k_conv3x3_rows<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, n.ws_smem_max));
+        cudaFuncAttributes fapply;
+        CPT_CUDA(cudaFuncGetAttributes(&fapply, k_conv3x3_rows<32, true>));
+        n.ws_smem_max = std::min(n.ws_smem_max, optin - (int)fapply.sharedSizeBytes);
+        CPT_CUDA(cudaFuncSetAttribute(k_conv3x3_rows<32, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      n.ws_smem_max));
+        CPT_CUDA(cudaFuncSetAttribute(k_conv3x3_rows<64, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      n.ws_smem_max));
+        CPT_CUDA(cudaFuncSetAttribute(k_conv3x3_rows<32, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      n.ws_smem_max));
+        n.rows_apply_per_sm = std::max(1, std::min(2048 / 192, 65536 / (192 * std::max(1, (fapply.numRegs + 7) / 8 * 8))));
         CPT_CUDA(cudaFuncSetAttribute(k_wgrad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, WT_SMEM));
         CPT_CUDA(cudaFuncSetAttribute(k_conv3x3_ws<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, n.ws_smem_max));
         CPT_CUDA(cudaFuncSetAttribute(k_conv3x3_ws<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, n.ws_smem_max));
@@ -941,9 +950,11 @@ bool row_maps(const Geo& g, const View& in, const __nv_bfloat16* w, int cout, in
                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-// tcgen05 convolution: cout split into grid.y tiles of at most 256 channels (multiples of 16)
-void conv_tc(Net& n, const __nv_bfloat16* w, const float* bias, int cout, bool relu, const Geo& g, View in, View out16,
-             View out32, cudaStream_t s)
+// tcgen05 convolution: cout split into grid.y tiles of at most 256 channels (multiples of 16).
+// With ap (the logits layer at inference, cout == 32) the row-tile kernel applies the predicted
+// kernels in its epilogue instead of storing the logits; returns whether it did.
+bool conv_tc(Net& n, const __nv_bfloat16* w, const float* bias, int cout, bool relu, const Geo& g, View in, View out16,
+             View out32, cudaStream_t s, const ApplyArgs* ap = nullptr)
 {
     const long P = (long)g.N * g.H * g.W;
     const int tiles = (cout + 255) / 256;
@@ -972,13 +983,22 @@ void conv_tc(Net& n, const __nv_bfloat16* w, const float* bias, int cout, bool r
         const long q = (long)g.N * g.H * (rp.pitched ? g.W + 1 : g.W);
         const long m_tiles = (q + TC_M - 1) / TC_M;
         dim3 grid((unsigned)std::min<long>(m_tiles, (long)per_sm * n.sm_count), (unsigned)tiles);
+        if (ap && cout == 32 && bias && kc == 32) {
+            // the apply epilogue needs more registers: its own CTAs-per-SM limit
+            const int ps = std::max(1, std::min(per_sm, n.rows_apply_per_sm));
+            dim3 ga((unsigned)std::min<long>(m_tiles, (long)ps * n.sm_count), 1u);
+            k_conv3x3_rows<32, true><<<ga, 192, smem, s>>>(ta, tb, g, in.C, bias, cout, nt, ncols, nst, rp, *ap, relu,
+                                                          out16, out32, n.err);
+            return true;
+        }
+        const ApplyArgs none_ap{nullptr, nullptr, 0, 0, 0};
         if (kc == 64)
-            k_conv3x3_rows<64><<<grid, 192, smem, s>>>(ta, tb, g, in.C, bias, cout, nt, ncols, nst, rp, relu, out16,
-                                                       out32, n.err);
+            k_conv3x3_rows<64, false><<<grid, 192, smem, s>>>(ta, tb, g, in.C, bias, cout, nt, ncols, nst, rp, none_ap,
+                                                              relu, out16, out32, n.err);
         else
-            k_conv3x3_rows<32><<<grid, 192, smem, s>>>(ta, tb, g, in.C, bias, cout, nt, ncols, nst, rp, relu, out16,
-                                                       out32, n.err);
-        return;
+            k_conv3x3_rows<32, false><<<grid, 192, smem, s>>>(ta, tb, g, in.C, bias, cout, nt, ncols, nst, rp, none_ap,
+                                                              relu, out16, out32, n.err);
+        return false;
     }
     if (n.backend == 2 && tma_maps(g, in, w, cout, kc, nt, ta, tb)) {
         // warp-specialised persistent kernel fed by TMA, two accumulators per CTA: per_sm CTAs per
@@ -999,7 +1019,7 @@ void conv_tc(Net& n, const __nv_bfloat16* w, const float* bias, int cout, bool r
         else
             k_conv3x3_ws<32><<<grid, 192, smem, s>>>(ta, tb, g, in.C, bias, cout, nt, ncols, nst, relu, out16, out32,
                                                      n.err);
-        return;
+        return false;
     }
     // shared memory large enough that at most 512 / ncols CTAs fit on an SM (tensor memory)
     const int max_ctas = 512 / ncols;
@@ -1009,20 +1029,21 @@ void conv_tc(Net& n, const __nv_bfloat16* w, const float* bias, int cout, bool r
         k_conv3x3_tc<64><<<grid, 128, smem, s>>>(g, in, w, bias, cout, nt, ncols, relu, out16, out32, n.err);
     else
         k_conv3x3_tc<32><<<grid, 128, smem, s>>>(g, in, w, bias, cout, nt, ncols, relu, out16, out32, n.err);
+    return false;
 }
 
-void conv(Net& n, int i, const Geo& g, View in, View out16, View out32, cudaStream_t s)
+// Forward convolution of layer i; with ap, returns true when the kernel apply was fused into it
+// (conv_tc), false when the caller still has to run k_apply.
+bool conv(Net& n, int i, const Geo& g, View in, View out16, View out32, cudaStream_t s, const ApplyArgs* ap = nullptr)
 {
     const ConvSpec& c = SPECS[i];
     in.C = c.cin;
-    if (n.backend >= 1) {
-        conv_tc(n, n.wf16 + n.w16off[i], n.w + n.boff[i], c.cout, c.relu, g, in, out16, out32, s);
-        return;
-    }
+    if (n.backend >= 1) return conv_tc(n, n.wf16 + n.w16off[i], n.w + n.boff[i], c.cout, c.relu, g, in, out16, out32, s, ap);
     const long P = (long)g.N * g.H * g.W;
     dim3 grid((unsigned)(((P + 15) / 16 + 3) / 4), (unsigned)(c.cout / 32));
     k_conv3x3<4><<<grid, 128, 0, s>>>(g, in, n.wf16 + n.w16off[i], n.w + n.boff[i], c.cout, c.relu, out16, out32,
                                       false);
+    return false;
 }
 
 // input gradient: G (FP32, stored or added) = conv(dZ, flipped weights)
@@ -1139,9 +1160,13 @@ void forward(Net& n, int Hr, int Wr, bool train, cudaStream_t s)
     k_upsample<<<grid_for(n.P[0] * 64), 256, 0, s>>>(G[1], vw(n.D1b, 64, 0, 64), vw(n.cat0, 96, 0, 64));
     conv(n, 16, G[0], vw(n.cat0, 96, 0, 96), vw(n.D0a, 32, 0, 32), none(), s);
     conv(n, 17, G[0], vw(n.D0a, 32, 0, 32), vw(n.D0b, 32, 0, 32), none(), s);
-    conv(n, 18, G[0], vw(n.D0b, 32, 0, 32), none(), vw(n.logits, OUT_CH, 0, OUT_CH), s);
-    k_apply<<<grid_for(n.P[0]), 256, 0, s>>>(G[0], Hr, Wr, n.logits, n.rad, train ? n.wts : nullptr, n.out);
-    add_launches(19 + 4 + 4 + 1);
+    // at inference the row-tile kernel applies the predicted kernels in its epilogue (no logits
+    // stored); training keeps the logits and the softmax weights for the backward pass
+    const ApplyArgs ap{n.rad, n.out, Hr, Wr, 1};
+    const bool fused = conv(n, 18, G[0], vw(n.D0b, 32, 0, 32), none(), vw(n.logits, OUT_CH, 0, OUT_CH), s,
+                            train ? nullptr : &ap);
+    if (!fused) k_apply<<<grid_for(n.P[0]), 256, 0, s>>>(G[0], Hr, Wr, n.logits, n.rad, train ? n.wts : nullptr, n.out);
+    add_launches(19 + 4 + 4 + (fused ? 0 : 1));
 }
 
 void backward(Net& n, int Hr, int Wr, cudaStream_t s)

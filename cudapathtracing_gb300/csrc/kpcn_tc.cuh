@@ -547,12 +547,57 @@ struct RowPlan {
     bool pitched, resident;
 };
 
-template <int KC>
+// Kernel apply fused into the logits convolution's epilogue (inference): the 32 accumulator
+// columns of a pixel are its logits (25 used); softmax, then the weighted 5x5 gather of the
+// noisy radiance rad [N][H][W][3] (clamped to the real Hr x Wr image) into out, as k_apply.
+struct ApplyArgs {
+    const float* rad;
+    float* out;
+    int Hr, Wr, on;
+};
+
+__device__ __forceinline__ void apply_pixel(long p, const Geo& g, const float (&l0)[16], const float (&l1)[16],
+                                            const float* __restrict__ bias, const ApplyArgs& ap)
+{
+    float lg[KTAPS];
+    float mx = -3.0e38f;
+#pragma unroll
+    for (int k = 0; k < KTAPS; ++k) {
+        lg[k] = (k < 16 ? l0[k & 15] : l1[k & 15]) + __ldg(bias + k);
+        mx = fmaxf(mx, lg[k]);
+    }
+    float sum = 0.f;
+#pragma unroll
+    for (int k = 0; k < KTAPS; ++k) {
+        lg[k] = expf(lg[k] - mx);
+        sum += lg[k];
+    }
+    const float inv = 1.f / sum;
+    const int x = (int)(p % g.W), y = (int)((p / g.W) % g.H);
+    const long b = p / ((long)g.W * g.H);
+    const int xc = min(x, ap.Wr - 1), yc = min(y, ap.Hr - 1);
+    float ax = 0.f, ay = 0.f, az = 0.f;
+#pragma unroll
+    for (int k = 0; k < KTAPS; ++k) {
+        const float wk = lg[k] * inv;
+        const int xx = min(max(xc + k % KSIZE - KSIZE / 2, 0), ap.Wr - 1);
+        const int yy = min(max(yc + k / KSIZE - KSIZE / 2, 0), ap.Hr - 1);
+        const float* r = ap.rad + 3 * ((b * g.H + yy) * g.W + xx);
+        ax += wk * __ldg(r);
+        ay += wk * __ldg(r + 1);
+        az += wk * __ldg(r + 2);
+    }
+    ap.out[3 * p] = ax;
+    ap.out[3 * p + 1] = ay;
+    ap.out[3 * p + 2] = az;
+}
+
+template <int KC, bool APPLY>
 __global__ void __launch_bounds__(192, 1) k_conv3x3_rows(const __grid_constant__ CUtensorMap tma_a,
                                                           const __grid_constant__ CUtensorMap tma_b, Geo g, int cin,
                                                           const float* __restrict__ bias, int cout, int n_tile,
-                                                          int ncols, int nst, RowPlan rp, bool relu, View out16,
-                                                          View out32, int* err)
+                                                          int ncols, int nst, RowPlan rp, ApplyArgs ap, bool relu,
+                                                          View out16, View out32, int* err)
 {
     extern __shared__ uint8_t tc_smem_raw[];
     __shared__ uint64_t full[TC_WS_STAGES], empty[TC_WS_STAGES], accfull[2], accempty[2], bfull;
@@ -694,10 +739,17 @@ __global__ void __launch_bounds__(192, 1) k_conv3x3_rows(const __grid_constant__
             const bool valid = q < Q && qx < g.W;
             const long p = (q / Wq) * g.W + qx;
             const uint32_t base = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(buf * ncols);
-            for (int c = 0; c < n_tile; c += 16) {
-                float v[16];
-                tmem_ld16(base + (uint32_t)c, v);
-                if (valid) store16(p, n_base + c, v, bias, relu, out16, out32);
+            if (APPLY) {   // n_tile == 32: the pixel's logits
+                float l0[16], l1[16];
+                tmem_ld16(base, l0);
+                tmem_ld16(base + 16u, l1);
+                if (valid) apply_pixel(p, g, l0, l1, bias, ap);
+            } else {
+                for (int c = 0; c < n_tile; c += 16) {
+                    float v[16];
+                    tmem_ld16(base + (uint32_t)c, v);
+                    if (valid) store16(p, n_base + c, v, bias, relu, out16, out32);
+                }
             }
             tc_fence_before();
             mbar_arrive(&accempty[buf]);

@@ -353,7 +353,9 @@ cpt_status cpt_denoiser_get_params(cpt_denoiser* d, float* host_out);
 cpt_status cpt_denoiser_set_params(cpt_denoiser* d, const float* host_in); /* also resets Adam */
 cpt_status cpt_denoiser_get_grads(cpt_denoiser* d, float* host_out);      /* of the last train step */
 /* Copies an internal tensor of the last pass (activations "X0", "A0a", "cat0", ..., "logits",
- * "out"; gradients "G_D0b", ...) as floats into host (if capacity suffices); *count = elements. */
+ * "out"; gradients "G_D0b", ...) as floats into host (if capacity suffices); *count = elements.
+ * cpt_denoise on the default engine applies the predicted kernels inside the last convolution and
+ * does not store "logits"; cpt_denoiser_train_step stores every tensor. */
 cpt_status cpt_denoiser_export(cpt_denoiser* d, const char* name, float* host, uint64_t capacity, uint64_t* count);
 /* One step: forward, loss = mean |sqrt(out + 1e-3) - sqrt(target + 1e-3)|, backward, and (update != 0)
  * an Adam step with learning rate lr.  *loss (optional) receives the loss before the update. */
