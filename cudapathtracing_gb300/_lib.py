@@ -42,6 +42,7 @@ def lib():
             "cpt_context_set_wavefront": (S, [P, C.c_int, C.c_int, C.c_int, C.c_int]),
             "cpt_context_set_bvh_width": (S, [P, C.c_int]),
             "cpt_context_set_short_stack": (S, [P, C.c_int]),
+            "cpt_context_set_loop_limits": (S, [P, C.c_int32, C.c_int32]),
             "cpt_filter_bilateral": (S, [P, P, P, P, C.c_int32, C.c_int32, C.POINTER(abi.cpt_filter_params), P]),
             "cpt_pick": (S, [P, C.c_int32, C.c_int32, C.POINTER(C.c_int32)]),
             "cpt_scene_set_material": (S, [P, C.c_uint32, C.c_uint32, C.c_double, C.c_double, C.c_int32]),
@@ -57,6 +58,7 @@ def lib():
             "cpt_denoise": (S, [P, C.c_int32, C.c_int32, C.c_int32, P, P, P, P]),
             "cpt_denoiser_set_backend": (S, [P, C.c_int32]),
             "cpt_denoiser_check": (S, [P]),
+            "cpt_denoiser_wait_selftest": (S, [P]),
             "cpt_filter_temporal": (S, [P, P, P, P, C.POINTER(abi.cpt_camera), C.POINTER(abi.cpt_camera), C.c_float, P]),
             "cpt_ini_load": (S, [C.c_char_p, C.POINTER(P)]),
             "cpt_ini_describe": (S, [P, C.POINTER(abi.cpt_scene_desc)]),

@@ -51,6 +51,10 @@ class Context:
         check(lib().cpt_context_set_wavefront(self.h, slots, block_trace, block_shade, use_graph),
               "cpt_context_set_wavefront")
 
+    def set_loop_limits(self, max_trips: int = 1 << 16, max_replays: int = 1 << 20) -> None:
+        """Device loop bounds (cpt_context_set_loop_limits); the defaults are the maxima."""
+        check(lib().cpt_context_set_loop_limits(self.h, max_trips, max_replays), "cpt_context_set_loop_limits")
+
     def set_short_stack(self, entries: int) -> None:
         check(lib().cpt_context_set_short_stack(self.h, entries), "cpt_context_set_short_stack")
 

@@ -49,6 +49,7 @@ struct cpt_context {
     WavefrontTuning wf;        // grids are filled on first use
     bool wf_grids_ready;
     int bvh_width;             // traversal layout built by cpt_lbvh_build: 8 (compressed wide) or 2
+    int iter_limit;            // loop trips per sample of the render loops (cpt_context_set_loop_limits)
 };
 
 namespace cpt {
@@ -140,10 +141,15 @@ inline float3 tof(D3 v) { return make_float3((float)v.x, (float)v.y, (float)v.z)
 inline float rd(double x) { float f = (float)x; return (double)f > x ? std::nextafter(f, -INFINITY) : f; }
 inline float ru(double x) { float f = (float)x; return (double)f < x ? std::nextafter(f, INFINITY) : f; }
 
-// Camera ctor (Camera.cu:5-40) in double, then rounded to FP32.
-DevCamera make_camera(const cpt_camera& c)
+// Camera ctor (Camera.cu:5-40) in double: eye, centre of pixel (0, 0) and the per-pixel steps.
+struct CameraFrame {
+    D3 from, pixel_center, dh, dv;
+    int width, height;
+};
+
+CameraFrame camera_frame(const cpt_camera& c)
 {
-    DevCamera k;
+    CameraFrame f;
     int width = c.width;
     double hh = width / c.aspect_ratio;
     int height = hh < 1 ? 1 : (int)hh;
@@ -159,14 +165,27 @@ DevCamera make_camera(const cpt_camera& c)
     D3 hor = u * vw, ver = v * vh;
     D3 dh = hor / width, dv = ver / height;
     D3 ul = from - hor / 2 - ver / 2 - w * focal;
-    D3 pc = ul + dh / 2 + dv / 2;
-    k.look_from = tof(from);
-    k.pixel_center = tof(pc);
-    k.delta_h = tof(dh);
-    k.delta_v = tof(dv);
+    f.from = from;
+    f.pixel_center = ul + dh / 2 + dv / 2;
+    f.dh = dh;
+    f.dv = dv;
+    f.width = width;
+    f.height = height;
+    return f;
+}
+
+// The frame rounded to FP32 for the kernels.
+DevCamera make_camera(const cpt_camera& c)
+{
+    const CameraFrame f = camera_frame(c);
+    DevCamera k;
+    k.look_from = tof(f.from);
+    k.pixel_center = tof(f.pixel_center);
+    k.delta_h = tof(f.dh);
+    k.delta_v = tof(f.dv);
     k.background = tof(d3(c.background));
-    k.width = width;
-    k.height = height;
+    k.width = f.width;
+    k.height = f.height;
     return k;
 }
 
@@ -450,6 +469,8 @@ CPT_EXPORT cpt_status cpt_context_create(int device, cpt_context** out)
     c->wf.use_graph = true;
     c->wf_grids_ready = false;
     c->bvh_width = 2;   // the faster of the two layouts as measured on GB300
+    c->iter_limit = CPT_ITER_LIMIT;
+    c->wf.max_replays = CPT_MAX_REPLAYS;
     CPT_CUDA(cudaStreamCreateWithFlags(&c->wf.capture_stream, cudaStreamNonBlocking));
     CPT_CUDA(cudaStreamCreateWithFlags(&c->wf.side_stream, cudaStreamNonBlocking));
     CPT_CUDA(cudaEventCreateWithFlags(&c->wf.fork, cudaEventDisableTiming));
@@ -480,6 +501,15 @@ CPT_EXPORT cpt_status cpt_context_set_wavefront(cpt_context* ctx, int slots, int
     ctx->wf.block_shade = block_shade;
     ctx->wf.use_graph = use_graph != 0;
     ctx->wf_grids_ready = false;
+    return CPT_OK;
+}
+
+CPT_EXPORT cpt_status cpt_context_set_loop_limits(cpt_context* ctx, int32_t max_trips, int32_t max_replays)
+{
+    if (!ctx || max_trips < 1 || max_trips > CPT_ITER_LIMIT || max_replays < 1 || max_replays > CPT_MAX_REPLAYS)
+        return fail(CPT_ERR_INVALID_ARGUMENT, "loop limits: trips in [1, 65536], replays in [1, 1048576]");
+    ctx->iter_limit = max_trips;
+    ctx->wf.max_replays = max_replays;
     return CPT_OK;
 }
 
@@ -705,16 +735,18 @@ CPT_EXPORT cpt_status cpt_lbvh_export(const cpt_scene* s, uint64_t* keys, uint32
 }
 
 namespace {
-__global__ void k_fill_u32(uint32_t* p, uint32_t n, uint32_t v)
+// mat[i] = remap[mat[i]] for i < n (material indices of a primitive range)
+__global__ void k_remap_u32(uint32_t* mat, uint32_t n, const uint32_t* __restrict__ remap)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) p[i] = v;
+    if (i < n) mat[i] = remap[mat[i]];
 }
 }  // namespace
 
 // getObject (Render.cu:485-496): one ray through the centre of pixel (x, y) (row 0 at the bottom,
-// Camera::getSampleRay, Camera.cuh:44-48); the closest primitive in the reference's numbering, or
-// -1 on a miss or a light (lights carry no material).
+// Camera::getSampleRay, Camera.cuh:44-48), built in double like the reference's and rounded to
+// FP32; the closest primitive in the reference's numbering (a light included: every primitive's
+// hit sets a material, so getObject's material test never rejects one), or -1 on a miss.
 CPT_EXPORT cpt_status cpt_pick(cpt_scene* s, int32_t x, int32_t y, int32_t* prim)
 {
     if (!s || !prim) return fail(CPT_ERR_INVALID_ARGUMENT, "cpt_pick: null argument");
@@ -722,29 +754,31 @@ CPT_EXPORT cpt_status cpt_pick(cpt_scene* s, int32_t x, int32_t y, int32_t* prim
     *prim = -1;
     if (x < 0 || y < 0 || x >= s->cam.width || y >= s->cam.height) return CPT_OK;
     CPT_CUDA(cudaSetDevice(s->ctx->device));
-    const DevCamera& c = s->cam;
-    float3 p = c.pixel_center + (float)x * c.delta_h + (float)y * c.delta_v;
+    const CameraFrame f = camera_frame(s->camera);
+    const D3 px = f.pixel_center + f.dh * (double)x + f.dv * (double)y;
+    const D3 dir = px - f.from;
     cpt_ray r;
     std::memset(&r, 0, sizeof r);
-    r.origin[0] = c.look_from.x;
-    r.origin[1] = c.look_from.y;
-    r.origin[2] = c.look_from.z;
-    r.direction[0] = p.x - c.look_from.x;
-    r.direction[1] = p.y - c.look_from.y;
-    r.direction[2] = p.z - c.look_from.z;
+    r.origin[0] = (float)f.from.x;
+    r.origin[1] = (float)f.from.y;
+    r.origin[2] = (float)f.from.z;
+    r.direction[0] = (float)dir.x;
+    r.direction[1] = (float)dir.y;
+    r.direction[2] = (float)dir.z;
     r.tmin = 0.001f;
     r.tmax = CPT_INF_F;
     cpt_hit h;
     cpt_status st = cpt_trace_closest(s, &r, 1, &h, 0, nullptr);
     if (st != CPT_OK) return st;
-    if (h.prim >= (int32_t)s->n_lights) *prim = h.prim;
+    *prim = h.prim;
     return CPT_OK;
 }
 
-// changeMaterial (Render.cu:498-522): primitives [first, end) get roughness (alpha_x, alpha_y) and
-// the Opaque type, or SpecularDielectric when glass != 0; lights are left alone.  The range gets a
-// new material (a copy of its first primitive's, edited), so other primitives sharing the old one
-// are unchanged, as with the reference's per-object material copies.
+// changeMaterial (Render.cu:498-522): every primitive in [first, end) keeps its colour and takes
+// roughness (alpha_x, alpha_y) and the Opaque type, or SpecularDielectric when glass != 0; lights
+// are left alone.  The reference edits each object's own material copy; here primitives share
+// material records, so each distinct material of the range gets an edited copy appended and the
+// range's indices are remapped to the copies (primitives outside the range keep the originals).
 CPT_EXPORT cpt_status cpt_scene_set_material(cpt_scene* s, uint32_t first, uint32_t end, double alpha_x,
                                              double alpha_y, int32_t glass)
 {
@@ -754,33 +788,61 @@ CPT_EXPORT cpt_status cpt_scene_set_material(cpt_scene* s, uint32_t first, uint3
     if (first >= end) return CPT_OK;
     CPT_CUDA(cudaSetDevice(s->ctx->device));
     const uint32_t sph0 = s->n_lights, tri0 = s->n_lights + s->n_spheres;
-    uint32_t old_mi = 0;
-    if (first < tri0) CPT_CUDA(cudaMemcpy(&old_mi, s->sphere_mat + (first - sph0), 4, cudaMemcpyDeviceToHost));
-    else CPT_CUDA(cudaMemcpy(&old_mi, s->tri_mat + (first - tri0), 4, cudaMemcpyDeviceToHost));
-    DevMaterial m;
-    CPT_CUDA(cudaMemcpy(&m, s->mats + old_mi, sizeof m, cudaMemcpyDeviceToHost));
-    m.ax = (float)alpha_x;
-    m.ay = (float)alpha_y;
-    m.type = glass ? CPT_M_SPECULAR_DIELECTRIC : CPT_M_OPAQUE;
+    struct Part {
+        uint32_t* mat;
+        uint32_t count;
+    } parts[2] = {{nullptr, 0}, {nullptr, 0}};
+    if (first < tri0) parts[0] = {s->sphere_mat + (first - sph0), std::min(end, tri0) - first};
+    if (end > tri0) {
+        const uint32_t a = std::max(first, tri0);
+        parts[1] = {s->tri_mat + (a - tri0), end - a};
+    }
+    // distinct materials of the range
+    const uint32_t n_old = s->n_mats;
+    std::vector<uint32_t> remap(n_old);
+    for (uint32_t i = 0; i < n_old; ++i) remap[i] = i;
+    std::vector<char> used(n_old, 0);
+    for (const Part& pt : parts) {
+        if (!pt.count) continue;
+        std::vector<uint32_t> idx(pt.count);
+        CPT_CUDA(cudaMemcpy(idx.data(), pt.mat, pt.count * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+        for (uint32_t m : idx)
+            if (m < n_old) used[m] = 1;
+    }
+    std::vector<DevMaterial> mats(n_old);
+    CPT_CUDA(cudaMemcpy(mats.data(), s->mats, n_old * sizeof(DevMaterial), cudaMemcpyDeviceToHost));
+    for (uint32_t m = 0; m < n_old; ++m) {
+        if (!used[m]) continue;
+        DevMaterial e = mats[m];
+        e.ax = (float)alpha_x;
+        e.ay = (float)alpha_y;
+        e.type = glass ? CPT_M_SPECULAR_DIELECTRIC : CPT_M_OPAQUE;
+        remap[m] = (uint32_t)mats.size();
+        mats.push_back(e);
+    }
     DevMaterial* grown = nullptr;
-    CPT_CUDA(cudaMalloc((void**)&grown, (s->n_mats + 1) * sizeof(DevMaterial)));
-    CPT_CUDA(cudaMemcpy(grown, s->mats, s->n_mats * sizeof(DevMaterial), cudaMemcpyDeviceToDevice));
-    CPT_CUDA(cudaMemcpy(grown + s->n_mats, &m, sizeof m, cudaMemcpyHostToDevice));
+    uint32_t* d_remap = nullptr;
+    CPT_CUDA(cudaMalloc((void**)&grown, mats.size() * sizeof(DevMaterial)));
+    cudaError_t e = cudaMalloc((void**)&d_remap, n_old * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemcpy(grown, mats.data(), mats.size() * sizeof(DevMaterial), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d_remap, remap.data(), n_old * sizeof(uint32_t), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        for (const Part& pt : parts) {
+            if (!pt.count) continue;
+            k_remap_u32<<<(pt.count + 255) / 256, 256>>>(pt.mat, pt.count, d_remap);
+            add_launches(1);
+        }
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    cudaFree(d_remap);
+    if (e != cudaSuccess) {
+        cudaFree(grown);
+        return cuda_fail(e, "cpt_scene_set_material");
+    }
     CPT_CUDA(cudaFree(s->mats));
     s->mats = grown;
-    const uint32_t mi = s->n_mats++;
-    if (first < tri0) {
-        const uint32_t a = first - sph0, b = std::min(end, tri0) - sph0;
-        k_fill_u32<<<(b - a + 255) / 256, 256>>>(s->sphere_mat + a, b - a, mi);
-        add_launches(1);
-    }
-    if (end > tri0) {
-        const uint32_t a = std::max(first, tri0) - tri0, b = end - tri0;
-        k_fill_u32<<<(b - a + 255) / 256, 256>>>(s->tri_mat + a, b - a, mi);
-        add_launches(1);
-    }
-    CPT_CUDA(cudaGetLastError());
-    CPT_CUDA(cudaDeviceSynchronize());
+    s->n_mats = (uint32_t)mats.size();
     return CPT_OK;
 }
 
@@ -858,6 +920,7 @@ CPT_EXPORT cpt_status cpt_render(cpt_scene* s, const cpt_render_params* p, const
     a.gbuf = gbuf;
     a.ray_counter = s->ray_counter;
     a.err = s->err;
+    a.iter_limit = s->ctx->iter_limit;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (stats) {
         CPT_CUDA(cudaEventCreate(&e0));

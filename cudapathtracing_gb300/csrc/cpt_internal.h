@@ -82,7 +82,13 @@ struct RenderArgs {
     float* gbuf;
     unsigned long long* ray_counter;
     int* err;
+    int iter_limit;   // loop trips per sample before the error word is set (CPT_ITER_LIMIT by default)
 };
+
+// Default bounds of the device loops: trips per sample of a path loop, and wavefront graph
+// replays per render (cpt_context_set_loop_limits lowers them).
+constexpr int CPT_ITER_LIMIT = 1 << 16;
+constexpr int CPT_MAX_REPLAYS = 1 << 20;
 
 cpt_status launch_render_megakernel(const SceneView& view, const RenderArgs& args, cudaStream_t stream, int block_x,
                                     int block_y);
@@ -94,6 +100,7 @@ struct WavefrontTuning {
     int grid_shade, block_shade;
     int short_stack;             // traversal stack entries kept in shared memory (8, 16, 24, 32)
     bool use_graph;
+    int max_replays;             // iteration chunks replayed before the render gives up (CPT_ERR_TIMEOUT)
     cudaStream_t capture_stream; // non-default stream used only to capture the iteration graph
     cudaStream_t side_stream;    // second capture stream: shadow rays traced beside extension rays
     cudaEvent_t fork, join;      // capture-time dependencies between the two streams

@@ -138,7 +138,7 @@ __device__ __forceinline__ uint32_t word_of(const float4& f, int w)
 }
 
 // Closest hit through the compressed 8-wide BVH (layout in wide.cu).  A visit decodes the 8
-// 16-bit quantised child boxes and tests them; hit children are recorded in a byte mask at bit
+// 8-bit quantised child boxes and tests them; hit children are recorded in a byte mask at bit
 // positions slot ^ (7 ^ octant), which orders them roughly front to back for this ray (the slots
 // were assigned by direction at build time).  Leaf children are tested at once, nearest bit
 // first (the reference tests leaves as it reaches them); the traversal continues with the first

@@ -668,6 +668,7 @@ struct Net {
     __nv_bfloat16 *wf16 = nullptr, *wd16 = nullptr;
     long step = 0;
     bool copies_fresh = false;
+    bool logits_stored = false;   // the last forward pass wrote n.logits (not the fused apply)
     // convolution engine: 0 = mma.sync kernel, 1 = tcgen05 kernel with cp.async copies, 2 = TMA-fed
     // warp-specialised persistent tcgen05 kernels (row tiles where the width allows, else im2col
     // tiles; k_conv3x3_tc where a TMA alignment rule fails)
@@ -991,7 +992,7 @@ bool conv_tc(Net& n, const __nv_bfloat16* w, const float* bias, int cout, bool r
                                                           out16, out32, n.err);
             return true;
         }
-        const ApplyArgs none_ap{nullptr, nullptr, 0, 0, 0};
+        const ApplyArgs none_ap{nullptr, nullptr, 0, 0};
         if (kc == 64)
             k_conv3x3_rows<64, false><<<grid, 192, smem, s>>>(ta, tb, g, in.C, bias, cout, nt, ncols, nst, rp, none_ap,
                                                               relu, out16, out32, n.err);
@@ -1162,10 +1163,11 @@ void forward(Net& n, int Hr, int Wr, bool train, cudaStream_t s)
     conv(n, 17, G[0], vw(n.D0a, 32, 0, 32), vw(n.D0b, 32, 0, 32), none(), s);
     // at inference the row-tile kernel applies the predicted kernels in its epilogue (no logits
     // stored); training keeps the logits and the softmax weights for the backward pass
-    const ApplyArgs ap{n.rad, n.out, Hr, Wr, 1};
+    const ApplyArgs ap{n.rad, n.out, Hr, Wr};
     const bool fused = conv(n, 18, G[0], vw(n.D0b, 32, 0, 32), none(), vw(n.logits, OUT_CH, 0, OUT_CH), s,
                             train ? nullptr : &ap);
     if (!fused) k_apply<<<grid_for(n.P[0]), 256, 0, s>>>(G[0], Hr, Wr, n.logits, n.rad, train ? n.wts : nullptr, n.out);
+    n.logits_stored = !fused;
     add_launches(19 + 4 + 4 + (fused ? 0 : 1));
 }
 
@@ -1314,6 +1316,33 @@ CPT_EXPORT cpt_status cpt_denoiser_check(cpt_denoiser* d)
     return CPT_OK;
 }
 
+namespace {
+// Self-test of the bounded barrier wait that every tensor-core kernel uses: a barrier that
+// nothing arrives on (no copy or MMA is issued, so nothing is in flight when the wait gives up).
+// mbar_wait returns false after its cycle budget (about 1 s) and sets the error word, which
+// cpt_denoiser_check reports as CPT_ERR_TIMEOUT; the context stays usable.
+__global__ void k_wait_selftest(int* err)
+{
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        cpt::kpcn::mbar_init(&bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        cpt::kpcn::mbar_wait(&bar, 0u, err);
+    }
+}
+}  // namespace
+
+CPT_EXPORT cpt_status cpt_denoiser_wait_selftest(cpt_denoiser* d)
+{
+    if (!d) return fail(CPT_ERR_INVALID_ARGUMENT, "cpt_denoiser_wait_selftest: null");
+    CPT_CUDA(cudaSetDevice(d->net.device));
+    k_wait_selftest<<<1, 32>>>(d->net.err);
+    add_launches(1);
+    CPT_CUDA(cudaGetLastError());
+    CPT_CUDA(cudaDeviceSynchronize());
+    return CPT_OK;
+}
+
 CPT_EXPORT cpt_status cpt_denoiser_destroy(cpt_denoiser* d)
 {
     delete d;
@@ -1384,6 +1413,9 @@ CPT_EXPORT cpt_status cpt_denoiser_export(cpt_denoiser* d, const char* name, flo
     };
     for (const T& t : table) {
         if (std::strcmp(t.name, name) != 0) continue;
+        if (t.ptr == n.logits && !n.logits_stored)
+            return fail(CPT_ERR_UNSUPPORTED, "cpt_denoiser_export: the last pass did not store \"logits\" (cpt_denoise "
+                                             "applies the predicted kernels inside the last convolution)");
         *count = (uint64_t)t.elems;
         if (!host || capacity < (uint64_t)t.elems) return CPT_OK;
         CPT_CUDA(cudaSetDevice(n.device));

@@ -553,7 +553,7 @@ struct RowPlan {
 struct ApplyArgs {
     const float* rad;
     float* out;
-    int Hr, Wr, on;
+    int Hr, Wr;
 };
 
 __device__ __forceinline__ void apply_pixel(long p, const Geo& g, const float (&l0)[16], const float (&l1)[16],

@@ -12,6 +12,8 @@
 // The scratch is g_lbvh_scratch below: 3 MiB of device memory that every GPU which loads this
 // library keeps until the process exits.  It holds the scratch of builds of up to
 // CPT_LBVH_STATIC_MAX_PRIMS (65,536) primitives; larger builds are rejected.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -23,28 +25,80 @@ namespace {
 constexpr size_t kStaticScratchBytes = 3u << 20;
 
 // File-scope device array.  In host code this name is only a stand-in for the symbol, not a
-// device address; its address is obtained per device with cudaGetSymbolAddress.
+// device address; its address is obtained per context with cudaGetSymbolAddress.
 __device__ __align__(256) unsigned char g_lbvh_scratch[kStaticScratchBytes];
 
-constexpr int kMaxDevices = 64;
+// The device address of g_lbvh_scratch belongs to the CUDA context it was looked up in: after
+// cudaDeviceReset, or from another context on the same device, the array lives elsewhere.  The
+// cache is therefore keyed on the context's process-unique ID (cuCtxGetId: an ID is never
+// reused, so an entry of a destroyed context can never match a later one).
+constexpr int kCacheSlots = 64;
+struct ScratchAddr {
+    unsigned long long ctx_id;
+    void* addr;
+};
 std::mutex g_mu;
-void* g_scratch_addr[kMaxDevices] = {};
+ScratchAddr g_cache[kCacheSlots] = {};
+int g_cache_next = 0;
 
-// Address of g_lbvh_scratch on the current device, looked up once per device (the first call
-// on a device does this set-up; make that first call before any stream capture begins).
+// Driver entry points resolved through the runtime (the library does not link libcuda).
+struct CtxQueries {
+    PFN_cuCtxGetCurrent_v4000 current = nullptr;
+    PFN_cuCtxGetId_v12000 id = nullptr;
+};
+
+const CtxQueries& ctx_queries()
+{
+    static const CtxQueries q = [] {
+        CtxQueries r;
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult res;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 4000, cudaEnableDefault, &res) == cudaSuccess &&
+            res == cudaDriverEntryPointSuccess)
+            r.current = reinterpret_cast<PFN_cuCtxGetCurrent_v4000>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &res) == cudaSuccess &&
+            res == cudaDriverEntryPointSuccess)
+            r.id = reinterpret_cast<PFN_cuCtxGetId_v12000>(f);
+        cudaGetLastError();
+        return r;
+    }();
+    return q;
+}
+
+// Address of g_lbvh_scratch in the calling thread's current context (the device selected with
+// cudaSetDevice).  The first call in a context looks the address up with cudaGetSymbolAddress,
+// which also creates the device's primary context if none is current yet; make that first call
+// before any stream capture begins.  Later calls in the same context reuse the cached address.
 cpt_status static_scratch(void** out)
 {
-    int dev = 0;
-    CPT_CUDA(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= kMaxDevices) return cpt::fail(CPT_ERR_UNSUPPORTED, "device index out of range");
+    const CtxQueries& q = ctx_queries();
+    if (!q.current || !q.id) return cpt::fail(CPT_ERR_UNSUPPORTED, "driver lacks cuCtxGetCurrent / cuCtxGetId");
+    CUcontext c = nullptr;
+    if (q.current(&c) != CUDA_SUCCESS) return cpt::fail(CPT_ERR_CUDA, "cuCtxGetCurrent failed");
     std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_scratch_addr[dev]) {
+    if (!c) {
+        // No context is current on this thread yet: the runtime's first device call makes the
+        // primary context current.
         void* p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_lbvh_scratch);
         if (e != cudaSuccess) return cpt::cuda_fail(e, "cudaGetSymbolAddress(g_lbvh_scratch)");
-        g_scratch_addr[dev] = p;
+        if (q.current(&c) != CUDA_SUCCESS || !c) return cpt::fail(CPT_ERR_CUDA, "no current CUDA context");
     }
-    *out = g_scratch_addr[dev];
+    unsigned long long id = 0;
+    if (q.id(c, &id) != CUDA_SUCCESS) return cpt::fail(CPT_ERR_CUDA, "cuCtxGetId failed");
+    for (const ScratchAddr& a : g_cache) {
+        if (a.addr && a.ctx_id == id) {
+            *out = a.addr;
+            return CPT_OK;
+        }
+    }
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_lbvh_scratch);
+    if (e != cudaSuccess) return cpt::cuda_fail(e, "cudaGetSymbolAddress(g_lbvh_scratch)");
+    g_cache[g_cache_next] = {id, p};
+    g_cache_next = (g_cache_next + 1) % kCacheSlots;
+    *out = p;
     return CPT_OK;
 }
 

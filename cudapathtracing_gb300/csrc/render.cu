@@ -18,8 +18,6 @@ namespace cpt {
 
 namespace {
 
-constexpr int ITER_LIMIT = 1 << 16;   // bound on loop trips per sample (error word on overflow)
-
 // Traversal stack of the megakernel: local memory.  (A shared-memory short stack made this
 // 122-register kernel slower on GB300; the wavefront's trace kernels use one.)
 using MkStack = LocalStack;
@@ -64,7 +62,7 @@ __device__ PixelResult pixel_reference(const SceneView& s, int i, int j, const R
         out.galb = f3(0.f, 0.f, 0.f);
         bool has_sample_light = false;
         for (int guard = 0;; ++guard) {
-            if (guard >= ITER_LIMIT) {
+            if (guard >= a.iter_limit) {
                 atomicOr(a.err, CPT_DEVERR_ITER);
                 break;
             }
@@ -85,7 +83,7 @@ __device__ PixelResult pixel_reference(const SceneView& s, int i, int j, const R
                 float3 pos = sf.pos + t * d;
                 o = pos;
                 for (int vguard = 0; t < dmax; ++vguard) {
-                    if (vguard >= ITER_LIMIT) {
+                    if (vguard >= a.iter_limit) {
                         atomicOr(a.err, CPT_DEVERR_ITER);
                         break;
                     }
@@ -181,7 +179,7 @@ __device__ PixelResult pixel_config(const SceneView& s, int i, int j, const Rend
         float m_sigma = 0.f, m_albedo = 0.f;
         int depth = 0;
         for (int guard = 0;; ++guard) {
-            if (guard >= ITER_LIMIT) {
+            if (guard >= a.iter_limit) {
                 atomicOr(a.err, CPT_DEVERR_ITER);
                 break;
             }

@@ -35,7 +35,6 @@ namespace cpt {
 
 namespace {
 
-constexpr int ITER_LIMIT = 1 << 16;   // loop trips per sample, as in the megakernel
 constexpr int CHUNK = 8;              // iterations per graph replay (even: parities repeat)
 
 enum : uint32_t {
@@ -340,7 +339,7 @@ __global__ void __launch_bounds__(256, 4) k_wf_shade(SceneView s, Wf w, RenderAr
         const bool hit = h.leaf >= 0;
         int nee = 0;
         bool cont = false;   // path continues with (o, d)
-        if (guard >= ITER_LIMIT) {
+        if (guard >= a.iter_limit) {
             atomicOr(w.err, CPT_DEVERR_ITER);
         } else {
             bool done_vertex = false;
@@ -618,7 +617,7 @@ cpt_status launch_render_wavefront(const SceneView& view, const RenderArgs& args
         }
     }
     int host_cnt[6];
-    const int max_chunks = 1 << 20;
+    const int max_chunks = tune.max_replays;
     bool drained = false;
     for (int chunk = 0; chunk < max_chunks; ++chunk) {
         if (use_graph) {

@@ -229,6 +229,12 @@ cpt_status cpt_context_set_short_stack(cpt_context* ctx, int entries);
  * both child boxes per 64-byte node (the default), 8 = the compressed 8-wide BVH (96-byte nodes,
  * 8-bit quantised child boxes, direction-ordered slots). */
 cpt_status cpt_context_set_bvh_width(cpt_context* ctx, int width);
+/* Bounds of the device loops that replace the reference's unbounded `while (true)` bounce loop
+ * (Render.cu:58) and its exit(99) on failure (Device.cuh:9-19): max_trips = loop trips per sample
+ * (bounces plus volume steps) after which a path is stopped and the render returns
+ * CPT_ERR_TIMEOUT; max_replays = wavefront iteration chunks (8 iterations each) replayed before a
+ * render that has not drained returns CPT_ERR_TIMEOUT.  Defaults and maxima: 65536 and 1048576. */
+cpt_status cpt_context_set_loop_limits(cpt_context* ctx, int32_t max_trips, int32_t max_replays);
 
 /* ---- scene files (host only, no GPU needed) ------------------------------------------ */
 /* Parses an INI scene (IniParser::Parse, IniParser.cpp:3-96) and assembles it in the
@@ -298,8 +304,10 @@ cpt_status cpt_lbvh_build_device(uint32_t num_extra, const double* extra_centroi
  * scratch is a 3 MiB array compiled into this library, which every GPU that loads it keeps
  * until the process exits.  At most CPT_LBVH_STATIC_MAX_PRIMS primitives; more is rejected with
  * CPT_ERR_INVALID_ARGUMENT.  The call allocates nothing.  Its first call on a device looks up the
- * array's device address (do that first call before any stream capture).  All calls share the
- * one array: calls whose work overlaps on the GPU (other streams, other host threads) race. */
+ * array's device address in the current CUDA context (do that first call before any stream
+ * capture); the address is cached per context, so after cudaDeviceReset the next call looks it up
+ * again.  All calls share the one array: calls whose work overlaps on the GPU (other streams,
+ * other host threads) race. */
 #define CPT_LBVH_STATIC_MAX_PRIMS 65536u
 cpt_status cpt_lbvh_build_device_static(uint32_t num_extra, const double* extra_centroids, const float* extra_boxes,
                                         uint32_t num_tri, const float* tri_vertices, const double scene_min[3],
@@ -330,10 +338,11 @@ cpt_status cpt_filter_temporal(cpt_context* ctx, float* rgb, const float* prev_r
                                const cpt_camera* camera, const cpt_camera* prev_camera, float alpha, void* stream);
 
 /* Picking and live material edit (getObject / changeMaterial, Render.cu:485-522, driven by
- * Window.cu:313-346).  cpt_pick: the primitive (reference numbering) hit by the ray through the
- * centre of pixel (x, y), row 0 at the bottom; -1 on a miss or a light.
- * cpt_scene_set_material: primitives [first, end) take roughness (alpha_x, alpha_y) and the
- * Opaque type, or SpecularDielectric when glass != 0 (lights are skipped). */
+ * Window.cu:313-346).  cpt_pick: the primitive (reference numbering, a light included) hit by the
+ * ray through the centre of pixel (x, y), row 0 at the bottom; -1 on a miss or outside the image.
+ * cpt_scene_set_material: primitives [first, end) keep their colours and take roughness
+ * (alpha_x, alpha_y) and the Opaque type, or SpecularDielectric when glass != 0 (lights are
+ * skipped); primitives outside the range are unchanged. */
 cpt_status cpt_pick(cpt_scene* scene, int32_t x, int32_t y, int32_t* prim);
 cpt_status cpt_scene_set_material(cpt_scene* scene, uint32_t first, uint32_t end, double alpha_x, double alpha_y,
                                   int32_t glass);
@@ -355,7 +364,8 @@ cpt_status cpt_denoiser_get_grads(cpt_denoiser* d, float* host_out);      /* of 
 /* Copies an internal tensor of the last pass (activations "X0", "A0a", "cat0", ..., "logits",
  * "out"; gradients "G_D0b", ...) as floats into host (if capacity suffices); *count = elements.
  * cpt_denoise on the default engine applies the predicted kernels inside the last convolution and
- * does not store "logits"; cpt_denoiser_train_step stores every tensor. */
+ * does not store "logits" (asking for them then fails with CPT_ERR_UNSUPPORTED);
+ * cpt_denoiser_train_step stores every tensor. */
 cpt_status cpt_denoiser_export(cpt_denoiser* d, const char* name, float* host, uint64_t capacity, uint64_t* count);
 /* One step: forward, loss = mean |sqrt(out + 1e-3) - sqrt(target + 1e-3)|, backward, and (update != 0)
  * an Adam step with learning rate lr.  *loss (optional) receives the loss before the update. */
@@ -371,6 +381,11 @@ cpt_status cpt_denoise(cpt_denoiser* d, int32_t n, int32_t h, int32_t w, const f
 cpt_status cpt_denoiser_set_backend(cpt_denoiser* d, int32_t backend);
 /* CPT_ERR_TIMEOUT if a tensor-core barrier wait of the passes since the last check timed out. */
 cpt_status cpt_denoiser_check(cpt_denoiser* d);
+/* Diagnostic: runs the bounded barrier wait of the tensor-core kernels on a barrier that nothing
+ * arrives on, so that it gives up (after about one second) and sets the error word; the next
+ * cpt_denoiser_check returns CPT_ERR_TIMEOUT and the denoiser stays usable.  Nothing is copied or
+ * computed while it waits. */
+cpt_status cpt_denoiser_wait_selftest(cpt_denoiser* d);
 
 /* Renders the scene's camera view (render, Render.cu:16-261, STATIC mode). */
 cpt_status cpt_render(cpt_scene* scene, const cpt_render_params* params, const cpt_render_output* out,

@@ -1300,6 +1300,38 @@ ORC_API uint64_t orc_render(void* p, const cpt_render_params* prm, double* rgb, 
     return total.load();
 }
 
+// getObject (Render.cu:485-496): the primitive hit by the ray through the centre of pixel (x, y)
+// (Camera::getSampleRay, Camera.cuh:44-48) with traverseIterative's default interval, or -1.
+ORC_API int orc_pick(void* p, int x, int y)
+{
+    Handle* h = (Handle*)p;
+    const Scene& s = h->ref;
+    V3 px = s.pixelCenter + (double)x * s.dh + (double)y * s.dv;
+    Ray ray = {s.lookFrom, px - s.lookFrom};
+    HitRecord rec;
+    int id = traverse(s, ray, rec);
+    return (id >= 0 && rec.material != nullptr) ? id : -1;
+}
+
+// changeMaterial (Render.cu:498-522) over primitives [first, end) of both estimators' copies:
+// spheres and triangles take (alphaX, alphaY) and Opaque, or SpecularDielectric when glass;
+// lights are skipped.
+ORC_API void orc_set_material(void* p, int first, int end, double alphaX, double alphaY, int glass)
+{
+    Handle* h = (Handle*)p;
+    Scene* both[2] = {&h->ref, &h->cfg};
+    for (Scene* s : both) {
+        const int n = (int)s->prims.size();
+        for (int i = first < 0 ? 0 : first; i < end && i < n; ++i) {
+            Prim& q = s->prims[i];
+            if (q.kind == K_LIGHT) continue;
+            q.mat.ax = alphaX;
+            q.mat.ay = alphaY;
+            q.mat.type = glass ? M_SPEC : M_OPAQUE;
+        }
+    }
+}
+
 // Renders like orc_render (rgb only) while counting, for every closest-hit query the render
 // makes, the internal-node visits and primitive tests of the ordered, pruned traversal of the
 // binary LBVH.  out[0] = queries, out[1] = internal visits, out[2] = primitive tests.

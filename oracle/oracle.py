@@ -28,6 +28,13 @@ def build(ref: bool = True) -> None:
     subprocess.check_call(["make", "-s", "-C", HERE, "all" if ref else "oracle"])
 
 
+def reference_dir() -> str | None:
+    """The reference's source folder as oracle/Makefile names it, or None where it is absent."""
+    r = subprocess.run(["make", "-s", "-C", HERE, "print-ref"], capture_output=True, text=True)
+    d = r.stdout.strip()
+    return d if r.returncode == 0 and d and os.path.isdir(d) else None
+
+
 def _sig(lib):
     P = C.c_void_p
     lib.orc_scene_create.restype = P
@@ -43,6 +50,9 @@ def _sig(lib):
     lib.orc_render.restype = C.c_uint64
     lib.orc_render.argtypes = [P, C.POINTER(abi.cpt_render_params), P, P, P, C.c_int]
     lib.orc_render_visit_counts.argtypes = [P, C.POINTER(abi.cpt_render_params), C.c_int, P]
+    lib.orc_pick.restype = C.c_int
+    lib.orc_pick.argtypes = [P, C.c_int, C.c_int]
+    lib.orc_set_material.argtypes = [P, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int]
 
 
 def oracle_lib():
@@ -73,6 +83,10 @@ def ref_lib():
         lib.ref_render.argtypes = [P, C.c_int, C.c_uint64, C.c_int, C.c_int, P, P, C.c_int]
         lib.ref_ini_dump.restype = C.c_int
         lib.ref_ini_dump.argtypes = [C.c_char_p, P, C.c_int]
+        if hasattr(lib, "ref_pick"):
+            lib.ref_pick.restype = C.c_int
+            lib.ref_pick.argtypes = [P, C.c_int, C.c_int]
+            lib.ref_change_material.argtypes = [P, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int]
         if hasattr(lib, "ref_gaussian_separate"):
             D = C.c_double
             lib.ref_gaussian_separate.argtypes = [P, P, P, D, D, D, D, C.c_int, C.c_int, C.c_int]
@@ -148,6 +162,14 @@ class OracleScene(_SceneBase):
         self.lib.orc_render_visit_counts(self.h, C.byref(params), threads, _p(out))
         return tuple(int(x) for x in out)
 
+    def pick(self, x: int, y: int) -> int:
+        """getObject (Render.cu:485-496) at pixel (x, y)."""
+        return int(self.lib.orc_pick(self.h, int(x), int(y)))
+
+    def set_material(self, first: int, end: int, alpha_x: float, alpha_y: float, glass: bool) -> None:
+        """changeMaterial (Render.cu:498-522) over primitives [first, end)."""
+        self.lib.orc_set_material(self.h, int(first), int(end), float(alpha_x), float(alpha_y), 1 if glass else 0)
+
     def render(self, params: abi.cpt_render_params, threads: int = 0, gbuffer: bool = False):
         rgb = np.zeros((self.height, self.width, 3))
         rgba = np.zeros((self.height, self.width, 4), np.uint8)
@@ -187,6 +209,12 @@ class RefScene(_SceneBase):
         t = np.empty(n)
         self.lib.ref_trace(self.h, _p(rays_f64), n, _p(ids), _p(t))
         return ids, t
+
+    def pick(self, x: int, y: int) -> int:
+        return int(self.lib.ref_pick(self.h, int(x), int(y)))
+
+    def set_material(self, first: int, end: int, alpha_x: float, alpha_y: float, glass: bool) -> None:
+        self.lib.ref_change_material(self.h, int(first), int(end), float(alpha_x), float(alpha_y), 1 if glass else 0)
 
     def render(self, spp: int, seed: int = 0, row_begin: int = 0, row_end: int = 0, threads: int = 0):
         rgb = np.zeros((self.height, self.width, 3))

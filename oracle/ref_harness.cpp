@@ -322,6 +322,32 @@ REF_API void ref_render(void* p, int spp, uint64_t seed, int r0, int r1, double*
         }
 }
 
+// The reference's getObject kernel (Render.cu:485-496) as a host call: the object under pixel
+// (x, y), or -1.
+REF_API int ref_pick(void* p, int x, int y)
+{
+    RefScene* s = (RefScene*)p;
+    int sel = -1;
+    getObject(s->objs, s->cam, s->internal.data(), &sel, x, y);
+    return sel;
+}
+
+// The reference's changeMaterial kernel (Render.cu:498-522) over [first, end), one call per
+// thread of the launch Window.cu:333-338 makes (512 threads per block).
+REF_API void ref_change_material(void* p, int first, int end, double alphaX, double alphaY, int glass)
+{
+    RefScene* s = (RefScene*)p;
+    const int threads = 512;
+    const int blocks = (end - first + threads - 1) / threads;
+    blockDim = dim3(threads, 1, 1);
+    for (int b = 0; b < blocks; ++b)
+        for (int t = 0; t < threads; ++t) {
+            blockIdx = make_uint3(b, 0, 0);
+            threadIdx = make_uint3(t, 0, 0);
+            changeMaterial(s->objs, first, end, alphaX, alphaY, glass != 0);
+        }
+}
+
 // IniParser::Parse flattened: returns the number of doubles written.
 // Layout: camera[bg3, width, aspect, lookFrom3, lookAt3, vFov], nL, L*[center3, w, h, normal3, color3, visible],
 // nS, S*[center3, r, color3, ax, ay, type], nF, F*[lt3, rt3, lb3, rb3, color3, ax, ay, type],

@@ -64,3 +64,20 @@ def outward_f32(lo: np.ndarray, hi: np.ndarray):
     flo = np.where(flo.astype(np.float64) > lo, np.nextafter(flo, np.float32(-np.inf)), flo)
     fhi = np.where(fhi.astype(np.float64) < hi, np.nextafter(fhi, np.float32(np.inf)), fhi)
     return flo, fhi
+
+
+def check_rgba8(gpu_rgba8, ref_rgba8, gpu_rgb, ref_rgb, equal_frac=0.98):
+    """The 8-bit display image (sqrt gamma, x254.99, clamp; Render.cu:229-260) of an FP32 render
+    against the FP64 one: at least `equal_frac` of the bytes are equal, and every byte of a pixel
+    whose radiance agrees to 1e-4 (the same path, FP32 rounding only) is within one step, since
+    rounding can only move a value across one quantisation boundary.  Pixels whose path diverged
+    (an edge hit or a roulette draw at its threshold) are bounded by the radiance tolerance."""
+    g8 = gpu_rgba8.astype(np.int32)
+    r8 = ref_rgba8.astype(np.int32)
+    same = (np.abs(gpu_rgb.astype(np.float64) - ref_rgb) <= 1e-4 * np.maximum(1.0, np.abs(ref_rgb))).all(-1)
+    d = np.abs(g8 - r8)[..., :3]
+    eq = (d == 0).mean()
+    print(f"rgba8: {eq:.5f} of bytes equal; max step on same-path pixels {d[same].max() if same.any() else 0}")
+    assert eq >= equal_frac, eq
+    assert (d[same] <= 1).all(), int(d[same].max())
+    assert same.mean() >= 0.9, same.mean()

@@ -65,6 +65,32 @@ def mixed_scene(seed: int = 11) -> abi.SceneDesc:
     return d
 
 
+# Material edits of the pick fixtures (changeMaterial, Render.cu:498-522): (first, end, alphaX,
+# alphaY, glass).  A first of None means "the primitive picked at the image centre".
+PICK_EDITS = [(0, 10, 0.3, 0.1, True), (None, 40, 0.05, 0.6, False)]
+
+
+def pick_edits(center_pick: int):
+    out = []
+    for first, n, ax, ay, glass in PICK_EDITS:
+        f = center_pick if first is None else first
+        out.append((f, f + n if first is None else n, ax, ay, glass))
+    return out
+
+
+def pick_fixture(name: str, desc: abi.SceneDesc, spp: int = 4) -> None:
+    """getObject at every pixel, then the edits above and a STATIC render of the edited scene."""
+    ref = O.RefScene(desc)
+    W, H = ref.width, ref.height
+    picks = np.array([[ref.pick(x, y) for x in range(W)] for y in range(H)], np.int32)
+    edits = pick_edits(int(picks[H // 2, W // 2]))
+    for e in edits:
+        ref.set_material(*e)
+    r = ref.render(spp, seed=0)
+    np.savez_compressed(os.path.join(HERE, f"pick_{name}.npz"), picks=picks, edits=np.array(edits, np.float64),
+                        rgb=r["rgb"], rgba8=r["rgba8"], spp=spp)
+
+
 def lbvh_fixture(name: str, ref: O.RefScene) -> None:
     L = ref.lbvh()
     np.savez_compressed(os.path.join(HERE, f"lbvh_{name}.npz"), **{k: L[k] for k in
@@ -104,6 +130,10 @@ def main() -> None:
                            ("glossy", O.RefScene(ini_path=os.path.join(SCENES, "glossy.ini")), 4)):
         r = ref.render(spp, seed=0)
         np.savez_compressed(os.path.join(HERE, f"render_{name}.npz"), rgb=r["rgb"], rgba8=r["rgba8"], spp=spp)
+
+    # picking and material edits (getObject / changeMaterial)
+    pick_fixture("cornell", cornell)
+    pick_fixture("mixed", mixed)
 
     # the reference's INI parser, flattened
     for ini in ("volume_glass", "glossy", "parser_edge"):

@@ -211,3 +211,42 @@ def test_denoise_unaligned_gbuffer(ctx):
     got = net.denoise(r_t, g_u)
     net.check()
     assert torch.equal(got, want)
+
+
+def test_fused_apply_matches_training_path_and_logits_not_exported(ctx):
+    """At inference the default engine applies the predicted kernels inside the logits
+    convolution (no logits stored); the training pass stores the logits and applies them with a
+    separate kernel.  On the same weights and inputs both give the same output up to FP32
+    summation order, and exporting "logits" after the fused pass is refused, not stale."""
+    from cudapathtracing_gb300 import denoiser as D
+    rng = np.random.default_rng(13)
+    rgb, g, tgt = _batch(rng, 1, 32, 256)   # padded width 256: row tiles, the fused epilogue
+    net = D.Denoiser(seed=5)
+    r_t, g_t, t_t = _cuda(rgb, g, tgt)
+    net.train_step(r_t, g_t, t_t, update=False)
+    unfused = net.export("out").reshape(rgb.shape)
+    fused = net.denoise(r_t, g_t).cpu().numpy()
+    net.check()
+    err = np.abs(fused - unfused) / np.maximum(1.0, np.abs(unfused))
+    assert err.max() < 1e-5, err.max()
+    with pytest.raises(Exception, match="logits"):
+        net.export("logits")
+
+
+def test_barrier_wait_limit_reports_timeout(ctx):
+    """The bounded mbarrier wait of the tensor-core kernels gives up on a barrier that nothing
+    arrives on and sets the error word: cpt_denoiser_check reports CPT_ERR_TIMEOUT once, then the
+    denoiser checks clean and still matches the oracle."""
+    from cudapathtracing_gb300 import denoiser as D, _lib
+    net = D.Denoiser(seed=5)
+    _lib.check(_lib.lib().cpt_denoiser_wait_selftest(net.h), "cpt_denoiser_wait_selftest")
+    with pytest.raises(_lib.CptError) as e:
+        net.check()
+    assert e.value.status == 4
+    net.check()
+    rng = np.random.default_rng(9)
+    rgb, g, _ = _batch(rng, 1, 16, 32)
+    out = net.denoise(*_cuda(rgb, g)).cpu().numpy()
+    net.check()
+    want = K.Net(net.params).forward(rgb, g)
+    assert (np.abs(out - want) / np.maximum(1.0, np.abs(want))).max() < 1e-3

@@ -10,7 +10,10 @@ import pytest
 from conftest import SCENES, golden
 from cudapathtracing_gb300 import _lib, abi, api
 
-REF_INI = "/root/reference/CudaPathTracing/scene_ini"
+import oracle as _oracle
+
+_REF_DIR = _oracle.reference_dir()
+REF_INI = os.path.join(_REF_DIR, "scene_ini") if _REF_DIR else ""
 
 
 def _unflatten(v):

@@ -66,6 +66,39 @@ def test_oracle_against_live_reference(oracle_mod):
         assert np.array_equal(ro["rgb"], rr["rgb"]) and np.array_equal(ro["rgba8"], rr["rgba8"])
 
 
+@pytest.mark.parametrize("name", ["cornell", "mixed"])
+def test_oracle_pick_and_material_edit_match_reference(oracle_mod, name):
+    """getObject at every pixel, then changeMaterial edits (a range over lights, spheres and
+    triangles; a range from the picked primitive) and a STATIC render: the restated oracle equals
+    the reference's own kernels bit for bit (tests/golden/pick_*.npz)."""
+    G = golden(f"pick_{name}.npz")
+    o = oracle_mod.OracleScene(scenes.by_name(name))
+    picks = np.array([[o.pick(x, y) for x in range(o.width)] for y in range(o.height)], np.int32)
+    assert np.array_equal(picks, G["picks"])
+    for first, end, ax, ay, glass in G["edits"]:
+        o.set_material(int(first), int(end), ax, ay, bool(glass))
+    r = o.render(abi.render_params(spp=int(G["spp"]), seed=0))
+    assert np.array_equal(r["rgb"], G["rgb"])
+    assert np.array_equal(r["rgba8"], G["rgba8"])
+
+
+def test_oracle_pick_against_live_reference(oracle_mod):
+    lib = oracle_mod.ref_lib()
+    if lib is None or not hasattr(lib, "ref_pick"):
+        pytest.skip("oracle/_ref not built (reference not mounted)")
+    for seed in (21, 22):
+        d = scenes.mixed_scene(seed)
+        o, r = oracle_mod.OracleScene(d), oracle_mod.RefScene(d)
+        for y in range(0, o.height, 3):
+            for x in range(o.width):
+                assert o.pick(x, y) == r.pick(x, y), (seed, x, y)
+        for rr in (o, r):
+            rr.set_material(3, 200, 0.15, 0.45, True)
+        a = o.render(abi.render_params(spp=2, seed=seed))
+        b = r.render(2, seed=seed)
+        assert np.array_equal(a["rgb"], b["rgb"])
+
+
 def test_oracle_single_and_empty_scenes(oracle_mod):
     d = abi.SceneDesc()
     d.add_material((1, 1, 1))

@@ -12,7 +12,8 @@ import ctypes as C
 import numpy as np
 import pytest
 
-from cudapathtracing_gb300 import _lib, procedural as P
+from conftest import outward_f32
+from cudapathtracing_gb300 import _lib, abi, procedural as P
 
 pytestmark = pytest.mark.gpu
 
@@ -109,3 +110,47 @@ def test_static_scratch_rejects_builds_above_its_maximum():
     assert b"65536" in lib.cpt_last_error_string()
     torch.cuda.synchronize()
     assert (out["order"] == -1).all()   # nothing was written
+
+
+def test_static_scratch_at_its_maximum_matches_oracle_and_allocates_nothing(oracle_mod):
+    """Exactly CPT_LBVH_STATIC_MAX_PRIMS primitives (the size the 3 MiB array is sized for):
+    keys, order and topology bit-exact against the FP64 oracle's LBVH and boxes equal to its
+    boxes rounded outwards.  After a warm-up call (which may load the kernels' code), a second
+    call must leave the device's free memory and the caching allocator's reservation unchanged."""
+    import torch
+    lib = _lib.lib()
+    static_build = _bind(lib)
+    n_sph = 6
+    n_tri = MAX_PRIMS - n_sph
+    ctr, boxes, tri, bmin, bmax = _inputs(41, n_tri, n_sph)
+    out = _outputs(torch, MAX_PRIMS)
+    keep, head, tail = _args(torch, ctr, boxes, tri, bmin, bmax, out)
+    st = static_build(*head, *tail, None)   # warm-up
+    assert st == 0, lib.cpt_last_error_string()
+    torch.cuda.synchronize()
+    free0, reserved0 = torch.cuda.mem_get_info()[0], torch.cuda.memory_reserved()
+    st = static_build(*head, *tail, None)
+    assert st == 0, lib.cpt_last_error_string()
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+    assert torch.cuda.memory_reserved() == reserved0
+    got = _host(out)
+    del keep
+
+    d = abi.SceneDesc()
+    m = d.add_material((0.5, 0.5, 0.5))
+    d.spheres = [dict(center=tuple(c), radius=float(r), material=m)
+                 for c, r in zip(ctr, np.linspace(0.2, 0.6, n_sph))]
+    d.tri_vertices = tri
+    d.tri_material = np.zeros(n_tri, np.uint32)
+    d.bounds_min, d.bounds_max = bmin, bmax
+    d.camera = abi.Camera(8, 1.0, (0, 0, 5), (0, 0, 0), 40.0)
+    G = oracle_mod.OracleScene(d).lbvh()
+    assert np.array_equal(got["keys"].view(np.uint64), G["keys"])
+    assert np.array_equal(got["order"].view(np.uint32), G["order"])
+    assert np.array_equal(got["children"][:, 0], G["child_a"])
+    assert np.array_equal(got["children"][:, 1], G["child_b"])
+    for k, gk in (("node_boxes", "node_boxes"), ("leaf_boxes", "leaf_boxes")):
+        lo, hi = outward_f32(G[gk][:, :3], G[gk][:, 3:])
+        assert np.array_equal(got[k][:, 0:3], lo), k
+        assert np.array_equal(got[k][:, 4:7], hi), k
