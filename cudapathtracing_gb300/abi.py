@@ -41,7 +41,7 @@ class cpt_material(C.Structure):
         ("alpha_x", C.c_double),
         ("alpha_y", C.c_double),
         ("type", C.c_int32),
-        ("reserved", C.c_int32),
+        ("texture", C.c_int32),
         ("eta", C.c_double),
         ("sigma_t", C.c_double),
         ("albedo", C.c_double),
@@ -91,6 +91,10 @@ class cpt_camera(C.Structure):
     ]
 
 
+class cpt_image(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("rgb", C.POINTER(C.c_uint8))]
+
+
 class cpt_scene_desc(C.Structure):
     _fields_ = [
         ("num_lights", C.c_uint32),
@@ -107,6 +111,10 @@ class cpt_scene_desc(C.Structure):
         ("bounds_min", C.c_double * 3),
         ("bounds_max", C.c_double * 3),
         ("camera", cpt_camera),
+        ("tri_uvs", C.POINTER(C.c_float)),
+        ("num_textures", C.c_uint32),
+        ("textures", C.POINTER(cpt_image)),
+        ("sky", cpt_image),
     ]
 
 
@@ -213,6 +221,9 @@ class SceneDesc:
     tri_vertices: np.ndarray | None = None            # (T, 9) float32 or float64
     tri_normals: np.ndarray | None = None             # (T, 9) float32
     tri_material: np.ndarray | None = None            # (T,) uint32
+    tri_uvs: np.ndarray | None = None                 # (T, 6) float32: uv0, uv1, uv2
+    textures: list = field(default_factory=list)      # (h, w, 3) uint8 images; material texture k -> [k-1]
+    sky: np.ndarray | None = None                     # (h, w, 3) uint8 equirectangular sky image
     bounds_min: tuple = (999999.0,) * 3
     bounds_max: tuple = (-999999.0,) * 3
     camera: Camera = field(default_factory=Camera)
@@ -225,10 +236,18 @@ class SceneDesc:
     def num_prims(self) -> int:
         return len(self.lights) + len(self.spheres) + self.num_triangles
 
-    def add_material(self, color, alpha_x=0.5, alpha_y=0.5, type=M_OPAQUE, eta=1.51, sigma_t=0.0, albedo=0.0) -> int:
+    def add_material(self, color, alpha_x=0.5, alpha_y=0.5, type=M_OPAQUE, eta=1.51, sigma_t=0.0, albedo=0.0,
+                     texture=0) -> int:
         self.materials.append(dict(color=tuple(color), alpha_x=alpha_x, alpha_y=alpha_y, type=type, eta=eta,
-                                   sigma_t=sigma_t, albedo=albedo))
+                                   sigma_t=sigma_t, albedo=albedo, texture=texture))
         return len(self.materials) - 1
+
+    def add_texture(self, rgb: np.ndarray) -> int:
+        """Registers an (h, w, 3) uint8 image; returns the material texture number (1-based)."""
+        rgb = np.ascontiguousarray(rgb, dtype=np.uint8)
+        assert rgb.ndim == 3 and rgb.shape[2] == 3
+        self.textures.append(rgb)
+        return len(self.textures)
 
     def to_c(self):
         """Returns (cpt_scene_desc, keepalive) — keep `keepalive` referenced during the call."""
@@ -253,8 +272,9 @@ class SceneDesc:
                                        sigma_t=0.0, albedo=0.0)]
         marr = (cpt_material * len(mats))()
         for i, m in enumerate(mats):
-            marr[i] = cpt_material((C.c_double * 3)(*m["color"]), m["alpha_x"], m["alpha_y"], int(m["type"]), 0,
-                                   m.get("eta", 1.51), m.get("sigma_t", 0.0), m.get("albedo", 0.0))
+            marr[i] = cpt_material((C.c_double * 3)(*m["color"]), m["alpha_x"], m["alpha_y"], int(m["type"]),
+                                   int(m.get("texture", 0)), m.get("eta", 1.51), m.get("sigma_t", 0.0),
+                                   m.get("albedo", 0.0))
         keep.append(marr)
         d.materials = C.cast(marr, C.POINTER(cpt_material))
         d.num_materials = len(mats)
@@ -277,6 +297,22 @@ class SceneDesc:
                   else np.ascontiguousarray(self.tri_material, dtype=np.uint32))
             keep.append(tm)
             d.tri_material = _ptr(tm, C.c_uint32)
+            if self.tri_uvs is not None:
+                tu = np.ascontiguousarray(self.tri_uvs, dtype=np.float32).reshape(T, 6)
+                keep.append(tu)
+                d.tri_uvs = _ptr(tu, C.c_float)
+
+        def image(a):
+            a = np.ascontiguousarray(a, dtype=np.uint8)
+            keep.append(a)
+            return cpt_image(int(a.shape[1]), int(a.shape[0]), _ptr(a, C.c_uint8))
+        if self.textures:
+            tarr = (cpt_image * len(self.textures))(*[image(t) for t in self.textures])
+            keep.append(tarr)
+            d.textures = C.cast(tarr, C.POINTER(cpt_image))
+        d.num_textures = len(self.textures)
+        if self.sky is not None:
+            d.sky = image(self.sky)
         d.bounds_min = (C.c_double * 3)(*self.bounds_min)
         d.bounds_max = (C.c_double * 3)(*self.bounds_max)
         d.camera = self.camera.to_c()

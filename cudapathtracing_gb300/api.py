@@ -96,7 +96,7 @@ class IniParser:
         for i in range(d.num_materials):
             m = d.materials[i]
             sd.materials.append(dict(color=tuple(m.color), alpha_x=m.alpha_x, alpha_y=m.alpha_y, type=m.type, eta=m.eta,
-                                     sigma_t=m.sigma_t, albedo=m.albedo))
+                                     sigma_t=m.sigma_t, albedo=m.albedo, texture=m.texture))
         for i in range(d.num_spheres):
             S = d.spheres[i]
             sd.spheres.append(dict(center=tuple(S.center), radius=S.radius, material=S.material))
@@ -104,6 +104,15 @@ class IniParser:
         if T:
             sd.tri_vertices = np.ctypeslib.as_array(d.tri_vertices_f64, shape=(T * 9,)).reshape(T, 9).copy()
             sd.tri_material = np.ctypeslib.as_array(d.tri_material, shape=(T,)).copy()
+            if d.tri_uvs:
+                sd.tri_uvs = np.ctypeslib.as_array(d.tri_uvs, shape=(T * 6,)).reshape(T, 6).copy()
+            if d.tri_normals:
+                sd.tri_normals = np.ctypeslib.as_array(d.tri_normals, shape=(T * 9,)).reshape(T, 9).copy()
+
+        def image(im):
+            return np.ctypeslib.as_array(im.rgb, shape=(im.height * im.width * 3,)).reshape(im.height, im.width, 3).copy()
+        sd.textures = [image(d.textures[i]) for i in range(d.num_textures)]
+        sd.sky = image(d.sky) if d.sky.rgb else None
         sd.bounds_min = tuple(d.bounds_min)
         sd.bounds_max = tuple(d.bounds_max)
         c = d.camera

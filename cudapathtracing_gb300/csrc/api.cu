@@ -72,6 +72,7 @@ struct cpt_scene {
     float* tri_f32;
     double* tri_f64;
     float* tri_n;
+    float* tri_uv;
     uint32_t* tri_mat;
     float4* spheres;
     uint32_t* sphere_mat;
@@ -94,6 +95,10 @@ struct cpt_scene {
     float4* nodes;      // BVH2 nodes (width 2)
     float4* wide;       // compressed 8-wide nodes (width 8)
     float4* leaf_rec;
+    // textures (all images' texels in one buffer) and the sky image
+    uint8_t* texels;
+    DevImage* tex;
+    DevImage sky;
     // misc
     unsigned long long* ray_counter;
     int* err;
@@ -123,6 +128,7 @@ void free_scene(cpt_scene* s)
     dfree(s->sphere_mat); dfree(s->lights); dfree(s->mats); dfree(s->extra_c); dfree(s->extra_box);
     dfree(s->keys); dfree(s->order); dfree(s->child); dfree(s->range); dfree(s->node_box); dfree(s->leaf_box);
     dfree(s->scratch); dfree(s->nodes); dfree(s->wide); dfree(s->leaf_rec); dfree(s->ray_counter); dfree(s->err);
+    dfree(s->tri_uv); dfree(s->texels); dfree(s->tex);
 }
 
 // ---- reference double maths for the host-side derived quantities
@@ -230,6 +236,16 @@ cpt_status validate(const cpt_scene_desc* d)
         if (!d->tri_material) return fail(CPT_ERR_INVALID_ARGUMENT, "tri_material is NULL");
     }
     if (d->num_materials == 0 || !d->materials) return fail(CPT_ERR_INVALID_ARGUMENT, "no materials");
+    if (d->num_textures && !d->textures) return fail(CPT_ERR_INVALID_ARGUMENT, "textures pointer is NULL");
+    auto bad_image = [](const cpt_image& im) {
+        return im.width <= 0 || im.height <= 0 || !im.rgb || (uint64_t)im.width * (uint64_t)im.height > (1ull << 30);
+    };
+    for (uint32_t i = 0; i < d->num_textures; ++i)
+        if (bad_image(d->textures[i])) return fail(CPT_ERR_INVALID_ARGUMENT, "texture image without texels");
+    if (d->sky.rgb && bad_image(d->sky)) return fail(CPT_ERR_INVALID_ARGUMENT, "sky image size");
+    for (uint32_t i = 0; i < d->num_materials; ++i)
+        if (d->materials[i].texture < 0 || (uint32_t)d->materials[i].texture > d->num_textures)
+            return fail(CPT_ERR_INVALID_ARGUMENT, "material texture index out of range");
     for (uint32_t i = 0; i < d->num_spheres; ++i)
         if (d->spheres[i].material >= d->num_materials)
             return fail(CPT_ERR_INVALID_ARGUMENT, "sphere material index out of range");
@@ -252,6 +268,12 @@ cpt_status upload(T** dst, const T* src, size_t count)
     cpt_status st = dalloc(dst, count);
     if (st != CPT_OK) return st;
     if (count) CPT_CUDA(cudaMemcpy(*dst, src, count * sizeof(T), cudaMemcpyHostToDevice));
+    return CPT_OK;
+}
+
+cpt_status h2d(void* dst, const void* src, size_t bytes)
+{
+    CPT_CUDA(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice));
     return CPT_OK;
 }
 
@@ -313,6 +335,7 @@ cpt_status create_scene(cpt_context* ctx, const cpt_scene_desc* d, cpt_scene** o
         dm.eta = (float)m.eta;
         dm.sigma_t = (float)m.sigma_t;
         dm.albedo = (float)m.albedo;
+        dm.tex = m.texture - 1;
     }
     size_t T = s->n_tris;
 #define CPT_TRY(x)             \
@@ -329,6 +352,30 @@ cpt_status create_scene(cpt_context* ctx, const cpt_scene_desc* d, cpt_scene** o
     else
         CPT_TRY(upload(&s->tri_f32, d->tri_vertices, 9 * T));
     if (d->tri_normals) CPT_TRY(upload(&s->tri_n, d->tri_normals, 9 * T));
+    if (d->tri_uvs && T) CPT_TRY(upload(&s->tri_uv, d->tri_uvs, 6 * T));
+    {   // textures then the sky, packed into one texel buffer
+        std::vector<size_t> off;
+        size_t total = 0;
+        for (uint32_t i = 0; i < d->num_textures; ++i) {
+            off.push_back(total);
+            total += 3 * (size_t)d->textures[i].width * d->textures[i].height;
+        }
+        const size_t sky_off = total;
+        if (d->sky.rgb) total += 3 * (size_t)d->sky.width * d->sky.height;
+        if (total) {
+            CPT_TRY(dalloc(&s->texels, total));
+            for (uint32_t i = 0; i < d->num_textures; ++i)
+                CPT_TRY(h2d(s->texels + off[i], d->textures[i].rgb,
+                            3 * (size_t)d->textures[i].width * d->textures[i].height));
+            if (d->sky.rgb)
+                CPT_TRY(h2d(s->texels + sky_off, d->sky.rgb, 3 * (size_t)d->sky.width * d->sky.height));
+        }
+        std::vector<DevImage> imgs(d->num_textures);
+        for (uint32_t i = 0; i < d->num_textures; ++i) imgs[i] = DevImage{s->texels + off[i], d->textures[i].width,
+                                                                          d->textures[i].height};
+        if (!imgs.empty()) CPT_TRY(upload(&s->tex, imgs.data(), imgs.size()));
+        s->sky = d->sky.rgb ? DevImage{s->texels + sky_off, d->sky.width, d->sky.height} : DevImage{nullptr, 0, 0};
+    }
     CPT_TRY(upload(&s->tri_mat, d->tri_material, T));
     CPT_TRY(upload(&s->spheres, sph.data(), sph.size()));
     CPT_TRY(upload(&s->sphere_mat, sph_mat.data(), sph_mat.size()));
@@ -373,6 +420,9 @@ SceneView view_of(const cpt_scene* s)
     v.sphere_mat = s->sphere_mat;
     v.lights = s->lights;
     v.mats = s->mats;
+    v.tri_uv = s->tri_uv;
+    v.tex = s->tex;
+    v.sky = s->sky;
     v.cam = s->cam;
     return v;
 }

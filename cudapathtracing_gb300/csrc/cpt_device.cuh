@@ -39,7 +39,13 @@ struct DevMaterial {   // Material (Material.cuh:5-22) in FP32
     int type;
     float eta;
     float sigma_t, albedo;
-    float pad[3];
+    int tex;           // image index in SceneView::tex, -1 = plain colour
+    float pad[2];
+};
+
+struct DevImage {      // 8-bit RGB texels, rows in file order (Triangle::texture, Camera::d_image)
+    const uint8_t* __restrict__ rgb;
+    int w, h;
 };
 
 struct DevLight {      // Light (Hittable.cuh:346-366): centre, unit normal, edge frame
@@ -76,6 +82,9 @@ struct SceneView {
     const uint32_t* __restrict__ sphere_mat;
     const DevLight* __restrict__ lights;
     const DevMaterial* __restrict__ mats;
+    const float* __restrict__ tri_uv;      // optional: 6 per triangle (uv0, uv1, uv2)
+    const DevImage* __restrict__ tex;      // images referenced by DevMaterial::tex
+    DevImage sky;                          // equirectangular sky, rgb NULL = background colour
     DevCamera cam;
 };
 

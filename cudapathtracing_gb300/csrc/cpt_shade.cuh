@@ -30,6 +30,30 @@ __device__ __forceinline__ void set_face_normal(Surf& sf, float3 d, float3 outwa
     sf.normal = sf.front ? outward : -outward;
 }
 
+// Nearest texel of an 8-bit RGB image at (u, v) (HitRecord::sampleTexture, HitRecord.cuh:38-49;
+// the same rule in Camera::getSkyBox, Camera.cuh:56-61): x = clamp(int(u * w), 0, w - 1), y likewise,
+// texels / 255.  The float-to-int conversion saturates, so far-out coordinates clamp too.
+__device__ __forceinline__ float3 texel(const DevImage& im, float u, float v)
+{
+    const int x = min(max(__float2int_rz(u * (float)im.w), 0), im.w - 1);
+    const int y = min(max(__float2int_rz(v * (float)im.h), 0), im.h - 1);
+    const uint8_t* p = im.rgb + 3 * ((size_t)y * im.w + x);
+    const float k = 1.0f / 255.0f;
+    return f3((float)__ldg(p) * k, (float)__ldg(p + 1) * k, (float)__ldg(p + 2) * k);
+}
+
+// Radiance of a ray that leaves the scene (Camera::getSkyBox, Camera.cuh:50-63): the background
+// colour, or the equirectangular sky image at u = atan2(-z, x) / 2pi + 0.5, v = 0.5 - asin(y) / pi
+// of the unit direction.
+__device__ __forceinline__ float3 sky_radiance(const SceneView& s, float3 d)
+{
+    if (!s.sky.rgb) return s.cam.background;
+    const float3 n = unit3(d);
+    const float u = atan2f(-n.z, n.x) * (0.5f / CPT_PI_F) + 0.5f;
+    const float v = 0.5f - asinf(fminf(fmaxf(n.y, -1.0f), 1.0f)) * (1.0f / CPT_PI_F);
+    return texel(s.sky, u, v);
+}
+
 // Surface record of a hit.  reference_materials maps Lambertian to Opaque and uses
 // eta = 1.51 (the reference has neither a Lambertian nor a per-material IOR).
 __device__ __forceinline__ void make_surface(const SceneView& s, float3 o, float3 d, const Hit& h,
@@ -54,6 +78,7 @@ __device__ __forceinline__ void make_surface(const SceneView& s, float3 o, float
     }
     uint32_t mi;
     float3 outward;
+    float tu = 0.f, tv = 0.f;   // interpolated texture coordinates (triangles)
     if (kind == CPT_KIND_SPHERE) {
         mi = s.sphere_mat[sf.prim - s.n_lights];
         outward = (sf.pos - f3(r0.x, r0.y, r0.z)) / r1.x;
@@ -79,9 +104,15 @@ __device__ __forceinline__ void make_surface(const SceneView& s, float3 o, float
         } else {
             outward = unit3(cross3(e1, e2));
         }
+        if (s.tri_uv) {   // Hittable.cuh:123-125
+            const float* uv = s.tri_uv + 6 * (size_t)ti;
+            const float w = 1.0f - h.u - h.v;
+            tu = w * uv[0] + h.u * uv[2] + h.v * uv[4];
+            tv = w * uv[1] + h.u * uv[3] + h.v * uv[5];
+        }
     }
     const DevMaterial& m = s.mats[mi];
-    sf.color = m.color;
+    sf.color = (kind == CPT_KIND_TRI && m.tex >= 0) ? texel(s.tex[m.tex], tu, tv) : m.color;
     sf.ax = m.ax;
     sf.ay = m.ay;
     sf.type = m.type;

@@ -107,7 +107,7 @@ __device__ PixelResult pixel_reference(const SceneView& s, int i, int j, const R
                 continue;
             }
             if (!hit) {
-                rad = rad + thr * cam.background;
+                rad = rad + thr * sky_radiance(s, d);
                 break;
             }
             if (sf.type == M_LIGHT) {
@@ -212,7 +212,7 @@ __device__ PixelResult pixel_config(const SceneView& s, int i, int j, const Rend
                 }
             }
             if (!hit) {
-                rad = rad + thr * cam.background;
+                rad = rad + thr * sky_radiance(s, d);
                 break;
             }
             Surf sf;

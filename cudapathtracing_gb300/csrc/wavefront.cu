@@ -374,7 +374,7 @@ __global__ void __launch_bounds__(256, 4) k_wf_shade(SceneView s, Wf w, RenderAr
             }
             if (!done_vertex) {
                 if (!hit) {
-                    rad = rad + thr * s.cam.background;
+                    rad = rad + thr * sky_radiance(s, d);
                 } else {
                     Surf sf;
                     make_surface(s, o, d, h, false, sf);

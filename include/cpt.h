@@ -59,12 +59,22 @@ typedef enum cpt_material_type {
 typedef struct cpt_material {
     double color[3];
     double alpha_x, alpha_y;
-    int32_t type; /* cpt_material_type */
-    int32_t reserved;
+    int32_t type;    /* cpt_material_type */
+    int32_t texture; /* 0: none; k >= 1: image k-1 of cpt_scene_desc.textures, whose texel at the hit's
+                        interpolated UV replaces color on triangles (HitRecord::sampleTexture,
+                        HitRecord.cuh:38-49; Triangle::hit, Hittable.cuh:123-125) */
     double eta;
     double sigma_t;
     double albedo;
 } cpt_material;
+
+/* An 8-bit RGB image, 3 bytes per texel, rows in file order (the first row is v = 0), as
+ * stbi_load returns it and as the reference indexes it (HitRecord.cuh:44-48, Camera.cuh:56-61). */
+typedef struct cpt_image {
+    int32_t width;
+    int32_t height;
+    const uint8_t* rgb;
+} cpt_image;
 
 /* Rectangular one-sided area light (Light, Hittable.cuh:346-399; LightInfo, IniParser.h:26-34). */
 typedef struct cpt_light {
@@ -117,6 +127,12 @@ typedef struct cpt_scene_desc {
     double bounds_min[3];
     double bounds_max[3];
     cpt_camera camera;
+    const float* tri_uvs;         /* optional: 6 floats per triangle (uv0, uv1, uv2), Hittable.cuh:60;
+                                     NULL = all zero, as for OBJ faces without vt (ObjLoader.cuh:119-134) */
+    uint32_t num_textures;
+    const cpt_image* textures;    /* images referenced by cpt_material.texture */
+    cpt_image sky;                /* equirectangular sky returned for rays that miss (Camera::getSkyBox,
+                                     Camera.cuh:50-63); sky.rgb NULL = the camera's background colour */
 } cpt_scene_desc;
 
 typedef struct cpt_ray {

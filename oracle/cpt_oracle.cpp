@@ -171,7 +171,26 @@ struct Prim {
     double lw, lh; V3 ln, eu, ev; bool visible;
     // triangle (Hittable.cuh:57-83)
     V3 p0, p1, p2, n0, n1, n2;
+    double uv[6];                  // uv0, uv1, uv2
+    const uint8_t* tex;            // RGB8 texture or NULL (Triangle::texture)
+    int texW, texH;
 };
+
+// Nearest texel (HitRecord::sampleTexture, HitRecord.cuh:38-49; Camera::getSkyBox, Camera.cuh:56-61):
+// x = min(max(int(u * width), 0), width - 1), likewise y, texels / 255.  int(x) of a double
+// outside the int range is undefined in C++; it is taken as saturating here, as on the GPU.
+static inline int texIndex(double x, int n)
+{
+    double f = x * (double)n;
+    int i = f >= 2147483647.0 ? 2147483647 : (f <= -2147483648.0 ? (-2147483647 - 1) : (f != f ? 0 : (int)f));
+    return i < 0 ? 0 : (i > n - 1 ? n - 1 : i);
+}
+static inline V3 texel(const uint8_t* img, int w, int h, double u, double v)
+{
+    int x = texIndex(u, w), y = texIndex(v, h);
+    const uint8_t* q = img + 3 * ((size_t)y * w + x);
+    return v3(q[0] / 255.0, q[1] / 255.0, q[2] / 255.0);
+}
 
 static Prim makeLight(const cpt_light& L)   // Light ctor Hittable.cuh:359-365; Hittable(Light) :424-454
 {
@@ -227,6 +246,9 @@ static Prim makeTriangle(V3 a, V3 b, V3 c, V3 na, V3 nb, V3 nc, const Material& 
     p.kind = K_TRI;
     p.p0 = a; p.p1 = b; p.p2 = c;
     p.n0 = na; p.n1 = nb; p.n2 = nc;
+    for (double& x : p.uv) x = 0.0;
+    p.tex = nullptr;
+    p.texW = p.texH = 0;
     p.mat = m;
     p.center = (a + b + c) / 3.0;
     p.box = pad(boxOf(v3(mmin(mmin(a.x, b.x), c.x), mmin(mmin(a.y, b.y), c.y), mmin(mmin(a.z, b.z), c.z)),
@@ -272,7 +294,13 @@ static bool hitTriangle(const Prim& p, const Ray& ray, HitRecord& rec, double tm
     if (v < 0.0 || u + v > 1.0) return false;
     double t = f * dot(e2, q);
     if (t < tmin || t > tmax) return false;
-    rec.hitColor = p.mat.color;   // untextured: sampleTexture(color) (HitRecord.cuh:38-45)
+    if (p.tex) {   // Hittable.cuh:123-125
+        double uu = (1.0 - u - v) * p.uv[0] + u * p.uv[2] + v * p.uv[4];
+        double vv = (1.0 - u - v) * p.uv[1] + u * p.uv[3] + v * p.uv[5];
+        rec.hitColor = texel(p.tex, p.texW, p.texH, uu, vv);
+    } else {
+        rec.hitColor = p.mat.color;   // sampleTexture(color) (HitRecord.cuh:34-37)
+    }
     rec.hitPos = at(ray, t);
     rec.t = t;
     rec.material = &p.mat;
@@ -394,6 +422,8 @@ struct Scene {
     // camera (Camera.cu:5-40)
     int width = 0, height = 0;
     V3 lookFrom, lookAt, background, dh, dv, pixelCenter;
+    const uint8_t* sky = nullptr;   // equirectangular sky image (Camera::d_image) or NULL
+    int skyW = 0, skyH = 0;
     V3 bmin, bmax;
     bool refMode = true;   // which estimator the materials were prepared for
     // LBVH (child encoding: >= 0 internal node, < 0 leaf ~k)
@@ -833,6 +863,15 @@ static void setupCamera(Scene& s, const cpt_camera& c)
     s.pixelCenter = ul + s.dh / 2 + s.dv / 2;
 }
 
+static V3 skyBox(const Scene& s, V3 direction)   // Camera::getSkyBox, Camera.cuh:50-63
+{
+    if (!s.sky) return s.background;
+    V3 dir = unit(direction);
+    double u = std::atan2(-dir.z, dir.x) / (2.0 * PI) + 0.5;
+    double v = 0.5 - std::asin(dir.y) / PI;
+    return texel(s.sky, s.skyW, s.skyH, u, v);
+}
+
 static inline Ray cameraRay(const Scene& s, int x, int y, double rx, double ry)   // Camera.cuh:37-43
 {
     V3 p = s.pixelCenter + (rx - 0.5 + x) * s.dh + (ry - 0.5 + y) * s.dv;
@@ -899,7 +938,7 @@ static PixelOut renderPixelReference(const Scene& s, int i, int j, int spp, uint
                 }
                 continue;
             }
-            if (hitId < 0) { rad = rad + thr * s.background; break; }
+            if (hitId < 0) { rad = rad + thr * skyBox(s, ray.d); break; }
             if (rec.material->type == M_LIGHT) {
                 if (!hasSampleLight) rad = rad + thr * rec.hitColor;
                 break;
@@ -1004,7 +1043,7 @@ static PixelOut renderPixelConfig(const Scene& s, int i, int j, const cpt_render
                     continue;
                 }
             }
-            if (hitId < 0) { rad = rad + thr * s.background; break; }
+            if (hitId < 0) { rad = rad + thr * skyBox(s, ray.d); break; }
             const Material& m = *rec.material;
             if (m.type == M_VOLUME) {
                 inMedium = rec.frontFace;
@@ -1119,6 +1158,22 @@ static int buildScene(Scene& s, const cpt_scene_desc* d, bool refMode)
         uint32_t mi = d->tri_material ? d->tri_material[i] : 0;
         if (mi >= d->num_materials) return 1;
         s.prims.push_back(makeTriangle(p[0], p[1], p[2], n[0], n[1], n[2], toMaterial(d->materials[mi], refMode)));
+        Prim& t = s.prims.back();
+        if (d->tri_uvs)
+            for (int k = 0; k < 6; ++k) t.uv[k] = d->tri_uvs[6 * i + k];
+        int tx = d->materials[mi].texture;
+        if (tx < 0 || (uint32_t)tx > d->num_textures) return 1;
+        if (tx > 0) {
+            const cpt_image& im = d->textures[tx - 1];
+            t.tex = im.rgb;
+            t.texW = im.width;
+            t.texH = im.height;
+        }
+    }
+    if (d->sky.rgb) {
+        s.sky = d->sky.rgb;
+        s.skyW = d->sky.width;
+        s.skyH = d->sky.height;
     }
     s.bmin = v3(d->bounds_min[0], d->bounds_min[1], d->bounds_min[2]);
     s.bmax = v3(d->bounds_max[0], d->bounds_max[1], d->bounds_max[2]);

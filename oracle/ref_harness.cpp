@@ -30,15 +30,35 @@ thread_local uint3 blockIdx;
 thread_local dim3 blockDim;
 uint64_t cpt_ref_seed = 0;
 
-// The reference only calls these for sky-box / texture images, which the harness never
-// loads; they are stubs with hidden visibility so they never shadow the CUDA runtime.
-extern "C" unsigned char* stbi_load(char const*, int*, int*, int*, int) { return nullptr; }
-extern "C" cudaError_t cudaMalloc(void** p, size_t)
+// The reference calls these only to load a sky-box image into device memory (Camera.cu:33-39).
+// Here "device memory" is host memory: stbi_load hands out the image the harness staged for the
+// camera being constructed (3 channels), or fails (NULL) like a missing file; cudaMalloc and
+// cudaMemcpy are malloc and memcpy.  They have hidden visibility, so they never shadow the CUDA
+// runtime of another library in the process.
+static thread_local const cpt_image* g_staged_image = nullptr;
+extern "C" unsigned char* stbi_load(char const*, int* w, int* h, int* c, int)
 {
-    if (p) *p = nullptr;
-    return cudaErrorNotSupported;
+    const cpt_image* im = g_staged_image;
+    if (!im || !im->rgb) return nullptr;
+    size_t bytes = 3 * (size_t)im->width * im->height;
+    unsigned char* p = (unsigned char*)std::malloc(bytes);
+    std::memcpy(p, im->rgb, bytes);
+    *w = im->width;
+    *h = im->height;
+    *c = 3;
+    return p;
 }
-extern "C" cudaError_t cudaMemcpy(void*, const void*, size_t, enum cudaMemcpyKind) { return cudaErrorNotSupported; }
+extern "C" cudaError_t cudaMalloc(void** p, size_t bytes)
+{
+    if (!p) return cudaErrorInvalidValue;
+    *p = std::malloc(bytes ? bytes : 1);
+    return *p ? cudaSuccess : cudaErrorMemoryAllocation;
+}
+extern "C" cudaError_t cudaMemcpy(void* dst, const void* src, size_t bytes, enum cudaMemcpyKind)
+{
+    std::memcpy(dst, src, bytes);
+    return cudaSuccess;
+}
 
 #define REF_API extern "C" __attribute__((visibility("default")))
 
@@ -110,10 +130,15 @@ int encodeChild(const RefScene& s, const Node* c)
     return (int)(c - s.internal.data());
 }
 
-void setupCamera(RefScene& s, const cpt_camera& c)
+void setupCamera(RefScene& s, const cpt_camera& c, const cpt_image* sky = nullptr)
 {
     s.cam = (Camera*)std::malloc(sizeof(Camera));
-    new (s.cam) Camera(c.width, c.aspect_ratio, d3(c.background), d3(c.look_from), d3(c.look_at), c.vfov_deg, std::string());
+    // A sky image goes in through the reference's own loading path (Camera.cu:33-39): a non-empty
+    // skyBox name makes the constructor call stbi_load, which returns the staged image.
+    g_staged_image = sky && sky->rgb ? sky : nullptr;
+    new (s.cam) Camera(c.width, c.aspect_ratio, d3(c.background), d3(c.look_from), d3(c.look_at), c.vfov_deg,
+                       g_staged_image ? std::string("sky") : std::string());
+    g_staged_image = nullptr;
     s.W = c.width;
     s.H = (int)(c.width / c.aspect_ratio);
 }
@@ -151,14 +176,22 @@ REF_API void* ref_scene_create(const cpt_scene_desc* d)
                                    : make_double3(0.0, 0.0, 0.0);
         }
         const cpt_material& m = d->materials[d->tri_material ? d->tri_material[i] : 0];
-        double2 z = make_double2(0.0, 0.0);
-        new (&s->objs[k++]) Hittable(Triangle(p[0], p[1], p[2], d3(m.color), m.alpha_x, m.alpha_y, refType(m.type), z, z, z,
-                                              nn[0], nn[1], nn[2], NULL, 0, 0, 0));
+        double2 uv[3];
+        for (int v = 0; v < 3; ++v)
+            uv[v] = d->tri_uvs ? make_double2(d->tri_uvs[6 * i + 2 * v], d->tri_uvs[6 * i + 2 * v + 1])
+                               : make_double2(0.0, 0.0);
+        // allocateMeshesOnDevice passes the mesh's image with its width, height and channel count
+        // (Device.cuh:56-79); the texels are host memory here.
+        const cpt_image* tx = m.texture > 0 ? &d->textures[m.texture - 1] : nullptr;
+        new (&s->objs[k++]) Hittable(Triangle(p[0], p[1], p[2], d3(m.color), m.alpha_x, m.alpha_y, refType(m.type),
+                                              uv[0], uv[1], uv[2], nn[0], nn[1], nn[2],
+                                              tx ? const_cast<unsigned char*>(tx->rgb) : NULL, tx ? tx->width : 0,
+                                              tx ? tx->height : 0, tx ? 3 : 0));
     }
     s->nLights = (int)d->num_lights;
     s->minB = d3(d->bounds_min);
     s->maxB = d3(d->bounds_max);
-    setupCamera(*s, d->camera);
+    setupCamera(*s, d->camera, &d->sky);
     buildBVH(*s);
     return s;
 }

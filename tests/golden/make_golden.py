@@ -91,6 +91,45 @@ def pick_fixture(name: str, desc: abi.SceneDesc, spp: int = 4) -> None:
                         rgb=r["rgb"], rgba8=r["rgba8"], spp=spp)
 
 
+def textured_scene(width: int = 48) -> abi.SceneDesc:
+    """Two textured quads (UVs partly outside [0, 1], so the texel indices clamp), one untextured
+    triangle, spheres of three materials, one light, and an equirectangular sky image."""
+    d = abi.SceneDesc()
+    g = P.PCG32Streams(5, np.arange(4096, dtype=np.uint64))
+
+    def image(h, w):
+        a = np.zeros((h, w, 3), np.uint8)
+        for c in range(3):
+            a[..., c] = (g.next()[: h * w].reshape(h, w) >> np.uint32(24)).astype(np.uint8)
+        return a
+
+    t_floor = d.add_texture(image(24, 32))
+    t_wall = d.add_texture(image(40, 16))
+    m_floor = d.add_material((0.7, 0.7, 0.7), 0.4, 0.4, abi.M_OPAQUE, texture=t_floor)
+    m_wall = d.add_material((0.5, 0.5, 0.5), 0.2, 0.6, abi.M_OPAQUE, texture=t_wall)
+    m_plain = d.add_material((0.8, 0.3, 0.2), 0.3, 0.3, abi.M_OPAQUE)
+    m_glass = d.add_material((1.0, 1.0, 1.0), 0.1, 0.1, abi.M_SPECULAR_DIELECTRIC)
+    tris = [((-3, -1, 3), (3, -1, 3), (-3, -1, -3)), ((3, -1, 3), (3, -1, -3), (-3, -1, -3)),     # floor
+            ((-3, -1, -3), (3, -1, -3), (-3, 2, -3)), ((3, -1, -3), (3, 2, -3), (-3, 2, -3)),     # wall
+            ((1.5, -1, 1.0), (2.5, -1, 0.5), (2.0, 0.5, 0.8))]                                    # plain
+    uvs = [((0, 0), (1, 0), (0, 1)), ((1, 0), (1, 1), (0, 1)),
+           ((-0.2, 0), (1.3, 0), (-0.2, 1.1)), ((1.3, 0), (1.3, 1.1), (-0.2, 1.1)),
+           ((0, 0), (0, 0), (0, 0))]
+    d.tri_vertices = np.array([sum(map(list, t), []) for t in tris], np.float32)
+    d.tri_uvs = np.array([sum(map(list, u), []) for u in uvs], np.float32)
+    d.tri_material = np.array([m_floor, m_floor, m_wall, m_wall, m_plain], np.uint32)
+    d.spheres = [dict(center=(-1.0, -0.4, 0.5), radius=0.6, material=m_glass),
+                 dict(center=(0.6, -0.5, -0.8), radius=0.5, material=m_plain),
+                 dict(center=(-1.8, 0.3, -1.6), radius=0.4, material=m_floor)]
+    d.lights.append(dict(center=(0.0, 2.5, 0.5), normal=(0.0, -1.0, 0.0), width=1.5, height=1.0,
+                         color=(6.0, 6.0, 6.0), visible=1))
+    d.sky = image(16, 32)
+    pts = d.tri_vertices.reshape(-1, 3).astype(np.float64)
+    d.bounds_min, d.bounds_max = tuple(pts.min(0)), tuple(pts.max(0))
+    d.camera = abi.Camera(width, 1.0, (0.5, 1.2, 6.0), (0.0, 0.0, 0.0), 60.0, (0.1, 0.1, 0.1))
+    return d
+
+
 def lbvh_fixture(name: str, ref: O.RefScene) -> None:
     L = ref.lbvh()
     np.savez_compressed(os.path.join(HERE, f"lbvh_{name}.npz"), **{k: L[k] for k in
@@ -130,6 +169,10 @@ def main() -> None:
                            ("glossy", O.RefScene(ini_path=os.path.join(SCENES, "glossy.ini")), 4)):
         r = ref.render(spp, seed=0)
         np.savez_compressed(os.path.join(HERE, f"render_{name}.npz"), rgb=r["rgb"], rgba8=r["rgba8"], spp=spp)
+
+    # textures and the sky image (HitRecord::sampleTexture, Camera::getSkyBox)
+    r = O.RefScene(textured_scene()).render(8, seed=0)
+    np.savez_compressed(os.path.join(HERE, "render_textured.npz"), rgb=r["rgb"], rgba8=r["rgba8"], spp=8)
 
     # picking and material edits (getObject / changeMaterial)
     pick_fixture("cornell", cornell)

@@ -8,7 +8,7 @@ import sys
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
 
-from make_golden import degenerate_scene, mixed_scene  # noqa: E402,F401
+from make_golden import degenerate_scene, mixed_scene, textured_scene  # noqa: E402,F401
 
 from cudapathtracing_gb300 import api, procedural as P  # noqa: E402
 
@@ -30,4 +30,6 @@ def by_name(name: str):
         return mixed_scene()
     if name == "ico3":
         return P.icosphere_scene(level=3)
+    if name == "textured":
+        return textured_scene()
     return ini_desc(name)

@@ -67,7 +67,7 @@ def test_spheres_1080p_band_vs_oracle(ctx, spheres, integrator, width):
         finally:
             ctx.set_bvh_width(2)
     s = scenes[width]
-    assert s.num_prims == 4096014
+    assert s.num_prims == d.num_prims == 4096016   # 4,096,014 triangles + 2 lights
     r = s.render(integrator=integrator, rows=BAND, **SPHERES_PRM)
     band = slice(BAND[0], BAND[1])
     compare(r["rgb"][band], ref["rgb"][band])

@@ -227,7 +227,7 @@ def test_pick_and_material_edit_vs_reference_golden(ctx, oracle_mod, name):
     nbad, unexplained = classify(o, rays, hits, G["picks"].reshape(-1), t)
     print(f"{name}: {nbad} of {H * W} picks differ, all explained" if not unexplained else unexplained)
     assert not unexplained, (nbad, unexplained[:10])
-    assert nbad <= 0.005 * H * W
+    assert nbad <= 0.01 * H * W   # shared edges of the axis-aligned quads under pixel centres
     assert s.pick(-1, 0) == -1 and s.pick(0, 10 ** 6) == -1
     for first, end, ax, ay, glass in G["edits"]:
         s.set_material(int(first), int(end), ax, ay, bool(glass))
@@ -298,3 +298,68 @@ def test_device_loop_limits_report_timeout(ctx):
     for integ in (abi.INTEGRATOR_MEGAKERNEL, abi.INTEGRATOR_WAVEFRONT):
         r = s.render(integrator=integ, **cfg)
         assert r["rays"] > 0 and np.isfinite(r["rgb"]).all()
+
+
+def test_textures_and_sky_match_reference_golden(ctx):
+    """Textured triangles and the equirectangular sky (HitRecord::sampleTexture, HitRecord.cuh:38-49;
+    Camera::getSkyBox, Camera.cuh:50-63) against the reference's own render of the same scene."""
+    G = golden("render_textured.npz")
+    s = api.Scene(ctx, scenes.by_name("textured")).init()
+    r = s.render(spp=int(G["spp"]), seed=0)
+    compare(r["rgb"], G["rgb"])
+    check_rgba8(r["rgba8"], G["rgba8"], r["rgb"], G["rgb"])
+
+
+@pytest.mark.parametrize("width", [2, 8])
+@pytest.mark.parametrize("integrator", [abi.INTEGRATOR_MEGAKERNEL, abi.INTEGRATOR_WAVEFRONT],
+                         ids=["megakernel", "wavefront"])
+def test_textures_and_sky_config_estimator_vs_oracle(ctx, oracle_mod, integrator, width):
+    d = scenes.by_name("textured")
+    ctx.set_bvh_width(width)
+    try:
+        s = api.Scene(ctx, d).init()
+    finally:
+        ctx.set_bvh_width(2)
+    prm = dict(spp=8, estimator=abi.ESTIMATOR_CONFIG, max_depth=8, rr_depth=3, rr_prob=0.8, seed=4)
+    r = s.render(integrator=integrator, **prm)
+    o = oracle_mod.OracleScene(d).render(abi.render_params(**prm))
+    compare(r["rgb"], o["rgb"])
+    assert abs(r["rays"] - o["rays"]) / o["rays"] < 0.01
+
+
+def test_texture_arguments_are_checked(ctx):
+    from cudapathtracing_gb300._lib import CptError
+    d = scenes.by_name("textured")
+    d.materials[0]["texture"] = len(d.textures) + 1
+    with pytest.raises(CptError):
+        api.Scene(ctx, d)
+
+
+def test_ini_textured_mesh_and_sky_vs_oracle(ctx, oracle_mod, tmp_path):
+    """An INI scene through cpt_scene_load_ini: an OBJ mesh with texture coordinates, a PPM
+    texture and a PPM sky box, rendered on the GPU and by the oracle from the parsed scene."""
+    rng = np.random.default_rng(3)
+    tex = rng.integers(0, 256, size=(12, 20, 3), dtype=np.uint8)
+    sky = rng.integers(0, 256, size=(8, 16, 3), dtype=np.uint8)
+    for name, img in (("t.ppm", tex), ("sky.ppm", sky)):
+        h, w, _ = img.shape
+        (tmp_path / name).write_bytes(f"P6\n{w} {h}\n255\n".encode() + img.tobytes())
+    (tmp_path / "quad.obj").write_text("v -2 0 -2\nv 2 0 -2\nv 2 0 2\nv -2 0 2\nvt -0.1 0\nvt 1.2 0\nvt 1 1\n"
+                                       "vt 0 1.1\nf 1/1 2/2 3/3 4/4\n")
+    ini = tmp_path / "scene.ini"
+    ini.write_text(f"[Camera]\nwidth=40\naspectRatio=1.0\nlookFrom=(0, 3, 5)\nlookAt=(0, 0, 0)\nvFov=60\n"
+                   f"skyBox={tmp_path / 'sky.ppm'}\n"
+                   f"[Light]\ncenter=(0, 4, 0)\nwidth=2\nheight=2\nnormal=(0, -1, 0)\ncolor=(2550, 2550, 2550)\n"
+                   f"[Sphere]\ncenter=(0, 0.8, 0)\nradius=0.8\ncolor=(200, 120, 80)\n"
+                   f"[Mesh]\npath={tmp_path / 'quad.obj'}\ntexture={tmp_path / 't.ppm'}\ncenter=(0, -0.2, 0)\n")
+    s = api.Scene(ctx, ini_path=str(ini)).init()
+    p = api.IniParser()
+    p.Parse(str(ini))
+    d = p.to_scene_desc()
+    assert len(d.textures) == 1 and d.sky is not None and d.tri_uvs is not None
+    o = oracle_mod.OracleScene(d)
+    for prm in (dict(spp=4, seed=1), dict(spp=4, estimator=abi.ESTIMATOR_CONFIG, max_depth=6, rr_depth=3,
+                                          rr_prob=0.8, seed=2)):
+        r = s.render(**prm)
+        ref = o.render(abi.render_params(**prm))
+        compare(r["rgb"], ref["rgb"])

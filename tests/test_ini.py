@@ -115,3 +115,43 @@ def test_reference_scene_files_parse_identically(oracle_mod, cptlib):
         pytest.skip("oracle/_ref not built")
     for path in sorted(glob.glob(os.path.join(REF_INI, "*.ini"))):
         compare_with_dump(path, oracle_mod.ref_ini_dump(path))
+
+
+def _ppm(path, rgb):
+    h, w, _ = rgb.shape
+    path.write_bytes(f"P6\n# test image\n{w} {h}\n255\n".encode() + rgb.astype(np.uint8).tobytes())
+
+
+def test_ini_obj_texcoords_normals_textures_and_sky(cptlib, tmp_path):
+    """vt per corner ((0, 0) without one), vn only with usingNV=1 (the reference's loader flag,
+    which its Scene::init leaves off), texture= and skyBox= images (binary PPM), and the
+    fallbacks of an unreadable image: untextured mesh, background sky."""
+    obj = tmp_path / "quad.obj"
+    obj.write_text("v -1 0 -1\nv 1 0 -1\nv 1 0 1\nv -1 0 1\nvt 0 0\nvt 1 0\nvt 1 1\nvt 0.25 0.75\n"
+                   "vn 0 1 0\nvn 0.6 0.8 0\nf 1/1/1 2/2/2 3/3/1 4/4/2\nf 1//1 3//2 4//1\n")
+    tex = np.arange(4 * 6 * 3, dtype=np.uint8).reshape(4, 6, 3)
+    sky = (np.arange(2 * 8 * 3, dtype=np.uint8) * 3).reshape(2, 8, 3)
+    _ppm(tmp_path / "t.ppm", tex)
+    _ppm(tmp_path / "sky.ppm", sky)
+    ini = tmp_path / "m.ini"
+    ini.write_text(f"[Camera]\nwidth=16\nskyBox={tmp_path / 'sky.ppm'}\n"
+                   f"[Floor]\nlt=(-1,0,1)\nrt=(1,0,1)\nlb=(-1,0,-1)\nrb=(1,0,-1)\n"
+                   f"[Mesh]\npath={obj}\ntexture={tmp_path / 't.ppm'}\nusingNV=1\n"
+                   f"[Mesh]\npath={obj}\ntexture={tmp_path / 'missing.ppm'}\n")
+    p = api.IniParser()
+    p.Parse(str(ini))
+    d = p.to_scene_desc()
+    assert d.tri_vertices.shape == (2 + 3 + 3, 9)
+    uv = d.tri_uvs.reshape(-1, 3, 2)
+    assert np.array_equal(uv[:2], np.zeros((2, 3, 2)))                      # floor: no texcoords
+    assert np.allclose(uv[2], [[0, 0], [1, 0], [1, 1]])                       # fan (1, 2, 3)
+    assert np.allclose(uv[3], [[0, 0], [1, 1], [0.25, 0.75]])                 # fan (1, 3, 4)
+    assert np.allclose(uv[4], 0.0)                                            # f 1//1 ...: no vt
+    n = d.tri_normals.reshape(-1, 3, 3)
+    assert np.allclose(n[2], [[0, 1, 0], [0.6, 0.8, 0], [0, 1, 0]])          # usingNV=1
+    assert np.allclose(n[4], [[0, 1, 0], [0.6, 0.8, 0], [0, 1, 0]])
+    assert np.array_equal(n[5:], np.zeros((3, 3, 3)))                         # second mesh: flat
+    assert len(d.textures) == 1 and np.array_equal(d.textures[0], tex)
+    m1, m2 = d.materials[d.tri_material[2]], d.materials[d.tri_material[5]]
+    assert m1["texture"] == 1 and m2["texture"] == 0                          # unreadable image: colour
+    assert np.array_equal(d.sky, sky)
