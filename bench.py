@@ -221,6 +221,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=2, help="steps of the end-to-end leg (0: skip)")
     ap.add_argument("--bvh-width", type=int, default=2, choices=[2, 8], help="traversal layout")
     ap.add_argument("--no-autotune", action="store_true", help="use the library defaults (no autotuner)")
+    ap.add_argument("--material-sort", type=int, default=-1, choices=[-1, 0, 1],
+                    help="force the wavefront's material sort off (0) or on (1); -1: the tuned / default choice")
     ap.add_argument("--no-denoise-eval", action="store_true",
                     help="skip the wall-time-to-RMSE comparison of denoised and plain renders")
     args = ap.parse_args()
@@ -261,6 +263,8 @@ def main():
                                                                 "tune_cache.json"),
                                    probe_spp=min(16, wl["spp"]), repeats=2)
         tuned = tuner.tune(scene, dict(wl, seed=seed), integ)
+    if args.material_sort >= 0:
+        ctx.set_material_sort(bool(args.material_sort))
     if trace_only:
         from cudapathtracing_gb300 import procedural as P
         n_rays = 10_000_000
@@ -331,6 +335,8 @@ def main():
                    "tuned": mk_tuned.to_json()["knobs"] if mk_tuned else None}
         if tuner:   # back to the wavefront's choice for the end-to-end leg
             tuner.tune(scene, dict(wl, seed=seed), integ)
+        if args.material_sort >= 0:
+            ctx.set_material_sort(bool(args.material_sort))
     if world > 1:
         import torch.distributed as dist
         t = torch.tensor([elapsed, float(rays)], device="cuda", dtype=torch.float64)
@@ -416,6 +422,8 @@ def main():
         "config": {"workload": args.workload, "width": W, "height": H, "spp": wl["spp"],
                    "triangles": desc.num_triangles, "integrator": args.integrator,
                    "bvh_width": int(tuned.knobs["bvh_width"]) if tuned else args.bvh_width,
+                   "material_sort": (bool(args.material_sort) if args.material_sort >= 0 else
+                                     bool(tuned.knobs.get("material_sort", 0)) if tuned else False),
                    "estimator": "config" if wl["estimator"] == 1 else "reference",
                    "max_depth": wl["max_depth"], "rr_depth": wl["rr_depth"], "rr_prob": wl["rr_prob"],
                    "step": "LBVH build + full render", "l2": "inputs larger than L2 (BVH + leaf records)",

@@ -51,6 +51,10 @@ class Context:
         check(lib().cpt_context_set_wavefront(self.h, slots, block_trace, block_shade, use_graph),
               "cpt_context_set_wavefront")
 
+    def set_material_sort(self, on: bool) -> None:
+        """Wavefront shade queue binned by material (cpt_context_set_material_sort)."""
+        check(lib().cpt_context_set_material_sort(self.h, 1 if on else 0), "cpt_context_set_material_sort")
+
     def set_loop_limits(self, max_trips: int = 1 << 16, max_replays: int = 1 << 20) -> None:
         """Device loop bounds (cpt_context_set_loop_limits); the defaults are the maxima."""
         check(lib().cpt_context_set_loop_limits(self.h, max_trips, max_replays), "cpt_context_set_loop_limits")

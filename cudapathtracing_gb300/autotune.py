@@ -3,7 +3,7 @@
 Knobs (all set through the C ABI on the context):
   megakernel   thread-block shape (block_x, block_y)
   wavefront    path slots (the wavefront size), trace / shade block sizes, traversal short-stack
-               depth (entries kept in shared memory)
+               depth (entries kept in shared memory), material sort of the shade queue
   both         BVH layout width (2 or 8; changing it rebuilds the scene's trace layout)
 
 Tuning is coordinate descent from the defaults: each knob in turn is swept with the others held
@@ -32,6 +32,7 @@ DEFAULTS = {
     "block_shade": 128,
     "short_stack": 16,
     "bvh_width": 2,
+    "material_sort": 0,
 }
 
 CANDIDATES = {
@@ -41,11 +42,12 @@ CANDIDATES = {
     "block_shade": [64, 128, 256],
     "short_stack": [8, 16, 24, 32],
     "bvh_width": [2, 8],
+    "material_sort": [0, 1],
 }
 
 KNOBS = {
     abi.INTEGRATOR_MEGAKERNEL: ["bvh_width", "render_block"],
-    abi.INTEGRATOR_WAVEFRONT: ["bvh_width", "slots", "block_trace", "short_stack", "block_shade"],
+    abi.INTEGRATOR_WAVEFRONT: ["bvh_width", "slots", "block_trace", "short_stack", "block_shade", "material_sort"],
 }
 
 
@@ -70,7 +72,8 @@ class Choice:
 
     @staticmethod
     def from_json(d: dict) -> "Choice":
-        knobs = {k: tuple(v) if isinstance(v, list) else v for k, v in d["knobs"].items()}
+        knobs = dict(DEFAULTS)   # knobs added after a cache entry was written take their defaults
+        knobs.update({k: tuple(v) if isinstance(v, list) else v for k, v in d["knobs"].items()})
         return Choice(knobs=knobs, score=d["score"], default_score=d["default_score"], trials=d.get("trials", []))
 
 
@@ -151,6 +154,7 @@ class Autotuner:
         c.set_render_block(int(bx), int(by))
         c.set_wavefront(int(knobs["slots"]), int(knobs["block_trace"]), int(knobs["block_shade"]), 1)
         c.set_short_stack(int(knobs["short_stack"]))
+        c.set_material_sort(bool(knobs.get("material_sort", 0)))
         if scene is not None and getattr(scene, "_tuned_width", None) != knobs["bvh_width"]:
             c.set_bvh_width(int(knobs["bvh_width"]))
             scene.buildBVH()

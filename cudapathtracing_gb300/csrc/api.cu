@@ -554,6 +554,13 @@ CPT_EXPORT cpt_status cpt_context_set_wavefront(cpt_context* ctx, int slots, int
     return CPT_OK;
 }
 
+CPT_EXPORT cpt_status cpt_context_set_material_sort(cpt_context* ctx, int on)
+{
+    if (!ctx) return fail(CPT_ERR_INVALID_ARGUMENT, "cpt_context_set_material_sort: null context");
+    ctx->wf.material_sort = on != 0;
+    return CPT_OK;
+}
+
 CPT_EXPORT cpt_status cpt_context_set_loop_limits(cpt_context* ctx, int32_t max_trips, int32_t max_replays)
 {
     if (!ctx || max_trips < 1 || max_trips > CPT_ITER_LIMIT || max_replays < 1 || max_replays > CPT_MAX_REPLAYS)

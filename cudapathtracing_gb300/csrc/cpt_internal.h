@@ -100,6 +100,7 @@ struct WavefrontTuning {
     int grid_shade, block_shade;
     int short_stack;             // traversal stack entries kept in shared memory (8, 16, 24, 32)
     bool use_graph;
+    bool material_sort;          // shade slots binned by the material their ray hit
     int max_replays;             // iteration chunks replayed before the render gives up (CPT_ERR_TIMEOUT)
     cudaStream_t capture_stream; // non-default stream used only to capture the iteration graph
     cudaStream_t side_stream;    // second capture stream: shadow rays traced beside extension rays

@@ -17,7 +17,13 @@
 //                 BSDF sampling (appends to Q_{i+1}); a finished sample starts the next one
 //
 // Queues are appended with warp-aggregated atomics; counters for iteration i+1 are cleared by
-// k_wf_trace of iteration i.  The host replays a CUDA graph of CHUNK iterations and reads
+// k_wf_trace of iteration i.
+//
+// Material sort (optional, Wf::sort): k_wf_trace files every traced slot into one of NBIN bins by
+// the material its ray hit (miss / light / medium boundary, diffuse-like surfaces with next-event
+// estimation, specular dielectrics, rough dielectrics) and k_wf_shade walks the bins in order, so
+// the lanes of a warp run the same BSDF code.  A slot's result does not depend on the order in which
+// slots are shaded (its random numbers come from its own sample stream), so the image is the same.  The host replays a CUDA graph of CHUNK iterations and reads
 // the queue sizes after each replay to stop.
 #include <cooperative_groups.h>
 #include <cooperative_groups/reduce.h>
@@ -36,6 +42,9 @@ namespace cpt {
 namespace {
 
 constexpr int CHUNK = 8;              // iterations per graph replay (even: parities repeat)
+constexpr int NBIN = 4;               // shade-queue bins of the material sort
+constexpr int CNT_BIN = 16;           // cnt[CNT_BIN + parity * NBIN + bin]: bin sizes
+constexpr int CNT_WORDS = CNT_BIN + 2 * NBIN;
 
 enum : uint32_t {
     F_CE = 1u << 0,        // count emission at the next surface
@@ -69,7 +78,9 @@ struct Wf {
     float4* sd;
     float4* sc;
     int* svis;
-    int* cnt;               // [0,1] Q sizes, [2,3] R sizes, [4,5] S sizes, [6] next item
+    int* cnt;               // [0,1] Q sizes, [2,3] R sizes, [4,5] S sizes, [6] next item, [8..11] fetch
+                            // counters, [CNT_BIN..] bin sizes
+    int* bins;              // material sort: 2 * NBIN * M slots ([parity][bin][M]), NULL when off
     unsigned long long* rays;
     int* err;
 };
@@ -81,6 +92,39 @@ __device__ __forceinline__ void append(int* base, int* counter, int v)
     if (g.thread_rank() == 0) b = atomicAdd(counter, (int)g.size());
     b = g.shfl(b, 0);
     base[b + g.thread_rank()] = v;
+}
+
+// Appends v to bin `bin` of a binned queue (bins of M entries, sizes in counters[bin]); the lanes
+// of the calling warp that pick the same bin share one atomic.
+__device__ __forceinline__ void append_binned(int* bins, int* counters, int M, int bin, int v)
+{
+    cg::coalesced_group g = cg::coalesced_threads();
+    cg::coalesced_group p = cg::labeled_partition(g, bin);
+    int b = 0;
+    if (p.thread_rank() == 0) b = atomicAdd(&counters[bin], (int)p.size());
+    b = p.shfl(b, 0);
+    bins[(size_t)bin * M + b + p.thread_rank()] = v;
+}
+
+// Shade bin of a traced ray: 0 miss, light, medium boundary (or any other cheap vertex); 1 Opaque
+// or Lambertian (next-event estimation, GGX / cosine sampling); 2 specular dielectric; 3 rough
+// dielectric.
+__device__ __forceinline__ int shade_bin(const SceneView& s, int leaf)
+{
+    if (leaf < 0) return 0;
+    const float4* r = s.leaf_rec + 3 * (size_t)leaf;
+    const int prim = __float_as_int(__ldg(&r[0].w));
+    const int kind = __float_as_int(__ldg(&r[1].w));
+    if (kind == CPT_KIND_LIGHT) return 0;
+    const uint32_t mi = kind == CPT_KIND_SPHERE ? __ldg(s.sphere_mat + (prim - s.n_lights))
+                                                : __ldg(s.tri_mat + (prim - s.n_lights - s.n_spheres));
+    switch (s.mats[mi].type) {
+    case M_OPAQUE:
+    case M_LAMBERT: return 1;
+    case M_SPEC: return 2;
+    case M_ROUGH: return 3;
+    default: return 0;
+    }
 }
 
 __device__ __forceinline__ void count_rays(unsigned long long* counter, uint32_t n)
@@ -175,6 +219,7 @@ __global__ void k_wf_init(SceneView s, Wf w, RenderArgs a)
         w.cnt[1] = w.cnt[2] = w.cnt[3] = w.cnt[4] = w.cnt[5] = 0;
         w.cnt[6] = w.M;
         w.cnt[8] = w.cnt[9] = w.cnt[10] = w.cnt[11] = 0;
+        for (int k = CNT_BIN; k < CNT_WORDS; ++k) w.cnt[k] = 0;
     }
     start_item(s, w, a, slot, slot);
     w.q[slot] = slot;   // Q_0 holds every slot in order
@@ -203,7 +248,7 @@ __global__ void k_wf_finish(Wf w, RenderArgs a, int groups)
 
 // At most 48 registers (5 blocks of 256 per SM): 62 % occupancy instead of 50 % for a few spilled
 // values, +5.7 % on the 1080p spheres render (the shadow kernel is faster uncapped).
-template <bool WIDE, int SHORT>
+template <bool WIDE, int SHORT, bool SORT>
 __global__ void __launch_bounds__(256, 5) k_wf_trace(SceneView s, Wf w, int par)
 {
     const int n = w.cnt[par];
@@ -214,8 +259,11 @@ __global__ void __launch_bounds__(256, 5) k_wf_trace(SceneView s, Wf w, int par)
         w.cnt[4 + nq] = 0;
         w.cnt[8 + 2 * nq] = 0;   // fetch counters of the next iteration's trace and shadow kernels
         w.cnt[9 + 2 * nq] = 0;
+        for (int b = 0; b < NBIN; ++b) w.cnt[CNT_BIN + nq * NBIN + b] = 0;   // its shade bins
     }
     const int* q = w.q + (size_t)par * w.M;
+    int* const bins = SORT ? w.bins + (size_t)par * NBIN * w.M : nullptr;
+    int* const bin_cnt = w.cnt + CNT_BIN + par * NBIN;
     uint32_t rays = 0;
     if (!WIDE && s.n_internal > 0) {
         rays = trace_items_bvh2<false, ShortStackN<SHORT>>(
@@ -228,7 +276,9 @@ __global__ void __launch_bounds__(256, 5) k_wf_trace(SceneView s, Wf w, int par)
                 tmx = CPT_INF_F;
             },
             [&](int i, const Hit& h) {
-                w.hit[q[i]] = make_float4(h.t, __int_as_float(h.leaf), h.u, h.v);
+                const int slot = q[i];
+                w.hit[slot] = make_float4(h.t, __int_as_float(h.leaf), h.u, h.v);
+                if (SORT) append_binned(bins, bin_cnt, w.M, shade_bin(s, h.leaf), slot);
             });
     } else {
         for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
@@ -237,6 +287,7 @@ __global__ void __launch_bounds__(256, 5) k_wf_trace(SceneView s, Wf w, int par)
             Hit h;
             bool hit = trace_closest<WIDE>(s, xyz(o), xyz(d), 0.001f, CPT_INF_F, h, w.err);
             w.hit[slot] = make_float4(h.t, __int_as_float(hit ? h.leaf : -1), h.u, h.v);
+            if (SORT) append_binned(bins, bin_cnt, w.M, shade_bin(s, hit ? h.leaf : -1), slot);
             rays++;
         }
     }
@@ -303,11 +354,24 @@ __global__ void __launch_bounds__(256) k_wf_resolve(SceneView s, Wf w, RenderArg
 // +4.4 % on the 1080p spheres render; 48 registers: +3.7 %.
 __global__ void __launch_bounds__(256, 4) k_wf_shade(SceneView s, Wf w, RenderArgs a, int par)
 {
-    const int n = w.cnt[par];
     const int nq = par ^ 1;
-    const int* q = w.q + (size_t)par * w.M;
+    // the traced slots: the bins in order (material sort), else the trace queue
+    const int* q = w.bins ? w.bins + (size_t)par * NBIN * w.M : w.q + (size_t)par * w.M;
+    int bin_end[NBIN];
+    int n = w.cnt[par];
+    if (w.bins) {
+        int acc = 0;
+        for (int b = 0; b < NBIN; ++b) bin_end[b] = acc += w.cnt[CNT_BIN + par * NBIN + b];
+        n = acc;
+    }
     for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
-        const int slot = q[idx];
+        int pos = idx;
+        if (w.bins) {
+            int b = 0;
+            while (b < NBIN - 1 && idx >= bin_end[b]) ++b;
+            pos = b * w.M + idx - (b ? bin_end[b - 1] : 0);
+        }
+        const int slot = q[pos];
         const int pixel = w.pixel[slot];
         uint32_t fl = w.flags[slot];
         Pcg32 rng;
@@ -487,16 +551,24 @@ struct TracePair {
     WfKernel trace, shadow;
 };
 
-// The trace kernels for the scene's layout and the short-stack depth (binary layout only).
-TracePair trace_pair(bool wide, int short_entries)
+// The trace kernels for the scene's layout, the short-stack depth (binary layout only) and the
+// material sort (the binning is compiled only into the sorting variants, so that the default
+// trace kernel keeps its registers).
+template <bool SORT>
+TracePair trace_pair_of(bool wide, int short_entries)
 {
-    if (wide) return {k_wf_trace<true, CPT_SHORT_STACK>, k_wf_shadow<true, CPT_SHORT_STACK>};
+    if (wide) return {k_wf_trace<true, CPT_SHORT_STACK, SORT>, k_wf_shadow<true, CPT_SHORT_STACK>};
     switch (short_entries) {
-    case 8: return {k_wf_trace<false, 8>, k_wf_shadow<false, 8>};
-    case 24: return {k_wf_trace<false, 24>, k_wf_shadow<false, 24>};
-    case 32: return {k_wf_trace<false, 32>, k_wf_shadow<false, 32>};
-    default: return {k_wf_trace<false, 16>, k_wf_shadow<false, 16>};
+    case 8: return {k_wf_trace<false, 8, SORT>, k_wf_shadow<false, 8>};
+    case 24: return {k_wf_trace<false, 24, SORT>, k_wf_shadow<false, 24>};
+    case 32: return {k_wf_trace<false, 32, SORT>, k_wf_shadow<false, 32>};
+    default: return {k_wf_trace<false, 16, SORT>, k_wf_shadow<false, 16>};
     }
+}
+
+TracePair trace_pair(bool wide, int short_entries, bool sort = false)
+{
+    return sort ? trace_pair_of<true>(wide, short_entries) : trace_pair_of<false>(wide, short_entries);
 }
 
 // CHUNK iterations: trace, shadow, resolve, shade, with the traversal of the scene's layout.
@@ -505,7 +577,7 @@ TracePair trace_pair(bool wide, int short_entries)
 void enqueue_chunk(const SceneView& view, const Wf& w, const RenderArgs& args, int gt, int bt, int gs, int bs,
                    int short_entries, cudaStream_t st, const WavefrontTuning* fork)
 {
-    const TracePair kp = trace_pair(view.wide != nullptr, short_entries);
+    const TracePair kp = trace_pair(view.wide != nullptr, short_entries, w.bins != nullptr);
     const size_t smem = short_stack_bytes(bt, short_entries);
     for (int it = 0; it < CHUNK; ++it) {
         int par = it & 1;
@@ -537,12 +609,12 @@ cpt_status carve(char*& p, size_t& left, T** out, size_t count)
     return CPT_OK;
 }
 
-size_t wf_bytes(int M, int L, size_t n_items)
+size_t wf_bytes(int M, int L, size_t n_items, bool sort)
 {
     size_t m = (size_t)M, ml = (size_t)M * std::max(L, 1);
     auto a = [](size_t b) { return align_up(b, 256); };
     return a(m * 4) * 6 + a(m * 8) + a(m * 16) * 8 + a(n_items * 16) + a(m * 8) + a(2 * m * 4) * 2 +
-           a(2 * ml * 4) + a(ml * 16) * 3 + a(ml * 4) + a(64);
+           a(2 * ml * 4) + a(ml * 16) * 3 + a(ml * 4) + a(CNT_WORDS * 4) + (sort ? a(2 * NBIN * m * 4) : 0);
 }
 
 }  // namespace
@@ -572,7 +644,7 @@ cpt_status launch_render_wavefront(const SceneView& view, const RenderArgs& args
     w.n_items = (int)n_items;
     w.rays = args.ray_counter;
     w.err = args.err;
-    size_t bytes = wf_bytes(M, L, n_items);
+    size_t bytes = wf_bytes(M, L, n_items, tune.material_sort);
     char* base = nullptr;
     CPT_CUDA(cudaMallocAsync((void**)&base, bytes, stream));
     char* p = base;
@@ -585,7 +657,8 @@ cpt_status launch_render_wavefront(const SceneView& view, const RenderArgs& args
     CARVE(rng, M) CARVE(o, M) CARVE(d, M) CARVE(thr, M) CARVE(rad, M) CARVE(radp, M) CARVE(pix, M) CARVE(hit, M)
     CARVE(part, n_items)
     CARVE(so, ml) CARVE(med, M) CARVE(q, 2 * (size_t)M) CARVE(rq, 2 * (size_t)M) CARVE(sq, 2 * ml) CARVE(sd, ml)
-    CARVE(sc, ml) CARVE(svis, ml) CARVE(cnt, 16)
+    CARVE(sc, ml) CARVE(svis, ml) CARVE(cnt, CNT_WORDS)
+    if (tune.material_sort) CARVE(bins, 2 * (size_t)NBIN * M)
 #undef CARVE
     if (st != CPT_OK) {
         cudaFreeAsync(base, stream);

@@ -245,6 +245,11 @@ cpt_status cpt_context_set_short_stack(cpt_context* ctx, int entries);
  * both child boxes per 64-byte node (the default), 8 = the compressed 8-wide BVH (96-byte nodes,
  * 8-bit quantised child boxes, direction-ordered slots). */
 cpt_status cpt_context_set_bvh_width(cpt_context* ctx, int width);
+/* Wavefront integrator: when on, every iteration files the traced paths into bins by the material
+ * their ray hit (miss / light / medium, Opaque and Lambertian, specular dielectric, rough
+ * dielectric) and shades the bins in order, so that a warp's lanes run one BSDF.  The image is
+ * the same either way.  Default off. */
+cpt_status cpt_context_set_material_sort(cpt_context* ctx, int on);
 /* Bounds of the device loops that replace the reference's unbounded `while (true)` bounce loop
  * (Render.cu:58) and its exit(99) on failure (Device.cuh:9-19): max_trips = loop trips per sample
  * (bounces plus volume steps) after which a path is stopped and the render returns
