@@ -79,6 +79,7 @@ def lib():
             "cpt_trace_closest": (S, [P, P, C.c_uint64, P, C.c_int, P]),
             "cpt_render": (S, [P, C.POINTER(abi.cpt_render_params), C.POINTER(abi.cpt_render_output), P,
                                C.POINTER(abi.cpt_render_stats)]),
+            "cpt_render_batch": (S, [P, C.POINTER(abi.cpt_render_job), C.c_uint32, P, C.POINTER(abi.cpt_render_stats)]),
         }
         for name, (res, args) in sigs.items():
             f = getattr(L, name)

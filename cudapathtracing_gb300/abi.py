@@ -172,6 +172,10 @@ class cpt_render_output(C.Structure):
     ]
 
 
+class cpt_render_job(C.Structure):
+    _fields_ = [("scene", C.c_void_p), ("params", cpt_render_params), ("output", cpt_render_output)]
+
+
 class cpt_render_stats(C.Structure):
     _fields_ = [("rays", C.c_uint64), ("paths", C.c_uint64), ("ms", C.c_double)]
 

@@ -290,3 +290,31 @@ def filter_temporal(ctx: Context, rgb, prev, gbuf, camera, prev_camera, alpha: f
     check(lib().cpt_filter_temporal(ctx.h, _vp(rgb), _vp(prev), _vp(gbuf), C.byref(c), C.byref(pc), float(alpha),
                                     _vp(stream)), "cpt_filter_temporal")
     return rgb
+
+
+def render_batch(ctx: Context, jobs: list, stream=None) -> dict:
+    """Renders several jobs in one wavefront (cpt_render_batch).  Each job is a dict with "scene"
+    (a built Scene of ctx), the render parameters of Scene.render (spp, max_depth, rr_depth,
+    rr_prob, seed, rows, flags; the config estimator) and optionally "rgb" / "rgba8" / "gbuffer"
+    outputs (torch CUDA tensors, or omitted for host numpy arrays, as in Scene.render).  Returns
+    the batch's stats and the jobs' outputs."""
+    arr = (abi.cpt_render_job * len(jobs))()
+    outs = []
+    for i, j in enumerate(jobs):
+        sc = j["scene"]
+        rows = j.get("rows", (0, 0))
+        params = abi.render_params(j.get("spp", 1), abi.ESTIMATOR_CONFIG, abi.INTEGRATOR_WAVEFRONT,
+                                   j.get("max_depth", 0), j.get("rr_depth", 0), j.get("rr_prob", 0.8),
+                                   j.get("seed", 0), rows[0], rows[1], j.get("flags", 0))
+        rgb, rgba8, gbuf = j.get("rgb"), j.get("rgba8"), j.get("gbuffer")
+        on_device = rgb is not None and not isinstance(rgb, np.ndarray)
+        if rgb is None:
+            rgb = np.zeros((sc.height, sc.width, 3), np.float32)
+            rgba8 = np.zeros((sc.height, sc.width, 4), np.uint8) if j.get("want_rgba8", True) else None
+        out = abi.cpt_render_output(_vp(rgb).value, _vp(rgba8).value if rgba8 is not None else None,
+                                    _vp(gbuf).value if gbuf is not None else None, 1 if on_device else 0, 0)
+        arr[i] = abi.cpt_render_job(sc.h.value if hasattr(sc.h, "value") else sc.h, params, out)
+        outs.append(dict(rgb=rgb, rgba8=rgba8, gbuffer=gbuf))
+    st = abi.cpt_render_stats()
+    check(lib().cpt_render_batch(ctx.h, arr, len(jobs), _vp(stream), C.byref(st)), "cpt_render_batch")
+    return dict(jobs=outs, rays=int(st.rays), paths=int(st.paths), ms=float(st.ms))

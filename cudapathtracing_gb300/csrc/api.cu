@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "cpt_internal.h"
@@ -1025,4 +1026,137 @@ CPT_EXPORT cpt_status cpt_render(cpt_scene* s, const cpt_render_params* p, const
     }
     if (host || stats) return check_device_error(s, stream);
     return CPT_OK;
+}
+
+// Several renders in one wavefront (see cpt.h).
+CPT_EXPORT cpt_status cpt_render_batch(cpt_context* ctx, const cpt_render_job* jobs, uint32_t count, void* stream_,
+                                       cpt_render_stats* stats)
+{
+    if (!ctx || (count && !jobs)) return fail(CPT_ERR_INVALID_ARGUMENT, "cpt_render_batch: null argument");
+    if (count == 0) return CPT_OK;
+    if (count > 4096) return fail(CPT_ERR_INVALID_ARGUMENT, "cpt_render_batch: at most 4096 jobs");
+    std::vector<int> r0(count), r1(count);
+    cpt_scene* s0 = jobs[0].scene;
+    for (uint32_t i = 0; i < count; ++i) {
+        const cpt_render_job& j = jobs[i];
+        cpt_scene* s = j.scene;
+        if (!s || !j.output.rgb) return fail(CPT_ERR_INVALID_ARGUMENT, "cpt_render_batch: job without scene or rgb");
+        if (s->ctx != ctx) return fail(CPT_ERR_INVALID_ARGUMENT, "cpt_render_batch: scene of another context");
+        if (!s->built && s->n) return fail(CPT_ERR_NOT_BUILT, "cpt_render_batch: build the LBVH first");
+        const cpt_render_params* p = &j.params;
+        if (p->spp <= 0) return fail(CPT_ERR_INVALID_ARGUMENT, "cpt_render_batch: spp must be positive");
+        if (p->estimator != CPT_ESTIMATOR_CONFIG)
+            return fail(CPT_ERR_UNSUPPORTED, "cpt_render_batch: the wavefront integrator runs the config estimator");
+        if (!(p->rr_prob > 0.f && p->rr_prob <= 1.f))
+            return fail(CPT_ERR_INVALID_ARGUMENT, "cpt_render_batch: rr_prob must be in (0, 1]");
+        if (s->width != s0->width)
+            return fail(CPT_ERR_UNSUPPORTED, "cpt_render_batch: all scenes must use the same BVH width");
+        int H = s->cam.height;
+        r0[i] = p->row_begin;
+        r1[i] = p->row_end;
+        if (r0[i] == 0 && r1[i] == 0) r1[i] = H;
+        if (r0[i] < 0 || r1[i] > H || r0[i] > r1[i]) return fail(CPT_ERR_INVALID_ARGUMENT, "cpt_render_batch: bad row range");
+    }
+    cudaStream_t stream = (cudaStream_t)stream_;
+    CPT_CUDA(cudaSetDevice(ctx->device));
+    std::vector<SceneView> views(count);
+    std::vector<RenderArgs> args(count);
+    std::vector<void*> temps;
+    auto release = [&]() {
+        for (void* t : temps) cudaFreeAsync(t, stream);
+    };
+    cpt_status st = CPT_OK;
+    uint64_t paths = 0;
+    for (uint32_t i = 0; i < count && st == CPT_OK; ++i) {
+        const cpt_render_job& j = jobs[i];
+        cpt_scene* s = j.scene;
+        const size_t np = (size_t)s->cam.width * s->cam.height;
+        RenderArgs& a = args[i];
+        a.spp = j.params.spp;
+        a.estimator = j.params.estimator;
+        a.max_depth = j.params.max_depth;
+        a.rr_depth = j.params.rr_depth;
+        a.rr_prob = j.params.rr_prob;
+        a.seed = j.params.seed;
+        a.row_begin = r0[i];
+        a.row_end = r1[i];
+        a.flags = j.params.flags;
+        a.rgb = j.output.rgb;
+        a.rgba8 = j.output.rgba8;
+        a.gbuf = j.output.gbuffer;
+        a.ray_counter = s0->ray_counter;
+        a.err = s0->err;
+        a.iter_limit = ctx->iter_limit;
+        if (!j.output.on_device) {   // device copies of host outputs for the duration of the call
+            auto tmp = [&](auto** dst, size_t bytes, const void* init) {
+                void* d = nullptr;
+                cudaError_t e = cudaMallocAsync(&d, bytes, stream);
+                if (e == cudaSuccess && init) e = cudaMemcpyAsync(d, init, bytes, cudaMemcpyHostToDevice, stream);
+                if (e != cudaSuccess) {
+                    if (d) cudaFreeAsync(d, stream);
+                    st = cuda_fail(e, "cpt_render_batch: device output");
+                    return;
+                }
+                temps.push_back(d);
+                *dst = static_cast<std::remove_pointer_t<decltype(dst)>>(d);
+            };
+            tmp(&a.rgb, np * 12, (j.params.flags & CPT_RENDER_ACCUMULATE) ? j.output.rgb : nullptr);
+            if (st == CPT_OK && j.output.rgba8) tmp(&a.rgba8, np * 4, nullptr);
+            if (st == CPT_OK && j.output.gbuffer) tmp(&a.gbuf, np * 32, nullptr);
+        }
+        views[i] = view_of(s);
+        paths += (uint64_t)(r1[i] - r0[i]) * s->cam.width * j.params.spp;
+    }
+    if (st != CPT_OK) {
+        release();
+        return st;
+    }
+    if (!ctx->wf_grids_ready) {
+        st = wavefront_grids(ctx->sm_count, ctx->wf.block_trace, ctx->wf.block_shade, ctx->wf.short_stack,
+                             &ctx->wf.grid_trace, &ctx->wf.grid_shade);
+        ctx->wf_grids_ready = st == CPT_OK;
+        if (st != CPT_OK) {
+            release();
+            return st;
+        }
+    }
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (stats) {
+        CPT_CUDA(cudaEventCreate(&e0));
+        CPT_CUDA(cudaEventCreate(&e1));
+    }
+    CPT_CUDA(cudaMemsetAsync(s0->ray_counter, 0, sizeof(unsigned long long), stream));
+    if (stats) CPT_CUDA(cudaEventRecord(e0, stream));
+    st = launch_render_wavefront_batch(views.data(), args.data(), (int)count, stream, ctx->wf);
+    if (stats) CPT_CUDA(cudaEventRecord(e1, stream));
+    for (uint32_t i = 0; i < count && st == CPT_OK; ++i) {
+        const cpt_render_job& j = jobs[i];
+        if (j.output.on_device) continue;
+        const int W = j.scene->cam.width;
+        const size_t off = (size_t)r0[i] * W, cnt = (size_t)(r1[i] - r0[i]) * W;
+        cudaError_t e = cudaMemcpyAsync(j.output.rgb + 3 * off, args[i].rgb + 3 * off, cnt * 12, cudaMemcpyDeviceToHost,
+                                        stream);
+        if (e == cudaSuccess && j.output.rgba8)
+            e = cudaMemcpyAsync(j.output.rgba8 + 4 * off, args[i].rgba8 + 4 * off, cnt * 4, cudaMemcpyDeviceToHost, stream);
+        if (e == cudaSuccess && j.output.gbuffer)
+            e = cudaMemcpyAsync(j.output.gbuffer + 8 * off, args[i].gbuf + 8 * off, cnt * 32, cudaMemcpyDeviceToHost,
+                                stream);
+        if (e != cudaSuccess) st = cuda_fail(e, "cpt_render_batch: read-back");
+    }
+    release();
+    if (st != CPT_OK) return st;
+    if (stats) {
+        unsigned long long rays = 0;
+        CPT_CUDA(cudaMemcpyAsync(&rays, s0->ray_counter, sizeof rays, cudaMemcpyDeviceToHost, stream));
+        CPT_CUDA(cudaEventSynchronize(e1));
+        float ms = 0;
+        CPT_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        CPT_CUDA(cudaStreamSynchronize(stream));
+        stats->rays = rays;
+        stats->paths = paths;
+        stats->ms = ms;
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+    }
+    return check_device_error(s0, stream);
 }

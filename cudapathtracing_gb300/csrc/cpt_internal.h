@@ -109,6 +109,10 @@ struct WavefrontTuning {
 
 cpt_status launch_render_wavefront(const SceneView& view, const RenderArgs& args, cudaStream_t stream,
                                    const WavefrontTuning& tune);
+// Several renders (jobs) in one wavefront; every job's args share ray_counter and err with args[0],
+// and every view has the same traversal layout.
+cpt_status launch_render_wavefront_batch(const SceneView* views, const RenderArgs* args, int n_jobs,
+                                         cudaStream_t stream, const WavefrontTuning& tune);
 
 // The reference's joint-bilateral and temporal filters (filter.cu); device buffers.
 DevCamera camera_of(const cpt_camera& c);

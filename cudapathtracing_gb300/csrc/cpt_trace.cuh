@@ -353,20 +353,21 @@ __device__ __forceinline__ uint32_t lane_mask_lt()
 
 // Traces work items [0, n) through the BVH2 with dynamic fetching: every loop trip each busy lane
 // advances its ray by one node, and once CPT_REFILL lanes (or all) are idle they take the next
-// items from *fetch (one atomic per warp).  load(i, o, d, tmin, tmax, skip) supplies item i's ray
-// (skip: the light an occlusion query aims at), store(i, hit) takes its result (for ANY,
-// hit.leaf >= 0 means occluded).  All 32 lanes of every warp must call this together.  Returns
-// the number of rays traced by the lane.
+// items from *fetch (one atomic per warp).  load(i, o, d, tmin, tmax, skip, scene) supplies item
+// i's ray (skip: the light an occlusion query aims at; scene: which of views(scene) it traverses,
+// for batches that mix scenes), store(i, hit) takes its result (for ANY, hit.leaf >= 0 means
+// occluded).  All 32 lanes of every warp must call this together.  Returns the number of rays
+// traced by the lane.
 constexpr int CPT_REFILL = 8;
 
-template <bool ANY, typename Stack = ShortStack, typename Load, typename Store>
-__device__ __forceinline__ uint32_t trace_items_bvh2(const SceneView& s, int n, int* fetch, int* err, Load load,
-                                                     Store store)
+template <bool ANY, typename Stack, typename Views, typename Load, typename Store>
+__device__ __forceinline__ uint32_t trace_items_bvh2_views(const Views& views, int n, int* fetch, int* err, Load load,
+                                                           Store store)
 {
     const int lane = threadIdx.x & 31;
     Bvh2Walk<ANY, Stack> w;
     w.stack.init();
-    int item = -1;
+    int item = -1, scene = 0;
     bool exhausted = false;
     uint32_t rays = 0;
     for (;;) {
@@ -385,7 +386,7 @@ __device__ __forceinline__ uint32_t trace_items_bvh2(const SceneView& s, int n, 
                     float3 o, d;
                     float tmn, tmx;
                     int skip = -1;
-                    load(r, o, d, tmn, tmx, skip);
+                    load(r, o, d, tmn, tmx, skip, scene);
                     w.start(o, d, tmn, tmx, skip);
                     item = r;
                     rays++;
@@ -393,12 +394,23 @@ __device__ __forceinline__ uint32_t trace_items_bvh2(const SceneView& s, int n, 
             }
         }
         if (__all_sync(0xffffffffu, item < 0)) break;
-        if (item >= 0 && w.step(s, err)) {
-            store(item, w.hit);
+        if (item >= 0 && w.step(views(scene), err)) {
+            store(item, w.hit, scene);
             item = -1;
         }
     }
     return rays;
+}
+
+// The same over one scene.
+template <bool ANY, typename Stack = ShortStack, typename Load, typename Store>
+__device__ __forceinline__ uint32_t trace_items_bvh2(const SceneView& s, int n, int* fetch, int* err, Load load,
+                                                     Store store)
+{
+    return trace_items_bvh2_views<ANY, Stack>(
+        [&](int) -> const SceneView& { return s; }, n, fetch, err,
+        [&](int i, float3& o, float3& d, float& tmn, float& tmx, int& skip, int&) { load(i, o, d, tmn, tmx, skip); },
+        [&](int i, const Hit& h, int) { store(i, h); });
 }
 
 // Closest hit over [tmin (boxes), tmax]; false on a miss.  WIDE selects the traversal layout at

@@ -19,7 +19,14 @@
 // Queues are appended with warp-aggregated atomics; counters for iteration i+1 are cleared by
 // k_wf_trace of iteration i.
 //
-// Material sort (optional, Wf::sort): k_wf_trace files every traced slot into one of NBIN bins by
+// Batches (cpt_render_batch): one wavefront renders several jobs — different scenes, image sizes,
+// sample counts and depth settings.  Items are numbered job after job; each slot records the job
+// of its item (Wf::job) and every kernel reads that job's scene view and parameters (WfJob) in
+// place of its own.  A job's pixels draw the same streams as in a render of its own, so its image
+// is the one cpt_render gives.  Kernels are instantiated with MULTI = false for single renders,
+// which keep the scene and parameters in kernel arguments.
+//
+// Material sort (optional, Wf::bins): k_wf_trace files every traced slot into one of NBIN bins by
 // the material its ray hit (miss / light / medium boundary, diffuse-like surfaces with next-event
 // estimation, specular dielectrics, rough dielectrics) and k_wf_shade walks the bins in order, so
 // the lanes of a warp run the same BSDF code.  A slot's result does not depend on the order in which
@@ -31,6 +38,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <vector>
 
 #include "cpt_internal.h"
 #include "cpt_shade.cuh"
@@ -52,6 +60,8 @@ enum : uint32_t {
     F_NEE_PREV = 1u << 2,  // pending shadow results belong to the finished sample (radp)
     F_GBUF = 1u << 3,      // G-buffer written for this pixel
 };
+
+struct WfJob;
 
 struct Wf {
     int M, L, first_pix, npix, S, n_items;
@@ -83,7 +93,45 @@ struct Wf {
     int* bins;              // material sort: 2 * NBIN * M slots ([parity][bin][M]), NULL when off
     unsigned long long* rays;
     int* err;
+    // batches
+    const WfJob* jobs;      // device array of n_jobs, NULL for a single render
+    int n_jobs;
+    int* job;               // job of the slot's item
+    int all_bvh2;           // every job's scene has a BVH2 with internal nodes (dynamic fetching)
 };
+
+// One render of a batch: its scene and parameters, and its share of the items and group sums.
+struct WfJob {
+    SceneView view;
+    RenderArgs args;
+    int first_pix, npix, S;
+    int item_base;          // global number of the job's first item
+    long long part_base;    // offset of its group sums in Wf::part (groups x npix)
+};
+
+// Pixel range, sample group size and group-sum array of the render a slot belongs to.
+struct JobGeo {
+    int first_pix, npix, S;
+    float4* part;
+};
+
+__device__ __forceinline__ JobGeo geo_of(const Wf& w) { return JobGeo{w.first_pix, w.npix, w.S, w.part}; }
+__device__ __forceinline__ JobGeo geo_of(const Wf& w, const WfJob& J)
+{
+    return JobGeo{J.first_pix, J.npix, J.S, w.part + J.part_base};
+}
+
+// Job of global item `item` (jobs are in item order).
+__device__ __forceinline__ int job_of_item(const Wf& w, int item)
+{
+    int lo = 0, hi = w.n_jobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (w.jobs[mid].item_base <= item) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
 
 __device__ __forceinline__ void append(int* base, int* counter, int v)
 {
@@ -171,11 +219,12 @@ __device__ __forceinline__ void start_sample(const SceneView& s, const Wf& w, ui
 
 // The item in the slot is done: store its group sum (and a miss G-buffer entry when no sample of
 // group 0 found a surface).
-__device__ __forceinline__ void finish_item(const Wf& w, const RenderArgs& a, int slot, int pixel, uint32_t fl)
+__device__ __forceinline__ void finish_item(const Wf& w, const RenderArgs& a, const JobGeo& jg, int slot, int pixel,
+                                            uint32_t fl)
 {
-    const int g = (w.sample[slot] - 1) / w.S;
-    const size_t off = (size_t)(pixel - w.first_pix);
-    w.part[(size_t)g * w.npix + off] = w.pix[slot];
+    const int g = (w.sample[slot] - 1) / jg.S;
+    const size_t off = (size_t)(pixel - jg.first_pix);
+    jg.part[(size_t)g * jg.npix + off] = w.pix[slot];
     if (g == 0 && a.gbuf && !(fl & F_GBUF)) {
         float4* gb = reinterpret_cast<float4*>(a.gbuf) + 2 * (size_t)pixel;
         gb[0] = make_float4(0.f, 0.f, 0.f, CPT_INF_F);
@@ -183,34 +232,46 @@ __device__ __forceinline__ void finish_item(const Wf& w, const RenderArgs& a, in
     }
 }
 
-// Starts item `item` (group major) in the slot with its first sample.
-__device__ __forceinline__ void start_item(const SceneView& s, const Wf& w, const RenderArgs& a, int slot, int item)
+// Starts item `item` (group major within its render) in the slot with its first sample.  For a
+// batch, item is global and the slot takes the item's job.
+template <bool MULTI>
+__device__ __forceinline__ void start_item(const SceneView& s0, const Wf& w, const RenderArgs& a0, int slot, int item)
 {
-    const int g = item / w.npix;
-    const int p = w.first_pix + (item - g * w.npix);
+    const int j = MULTI ? job_of_item(w, item) : 0;
+    const SceneView& s = MULTI ? w.jobs[j].view : s0;
+    const RenderArgs& a = MULTI ? w.jobs[j].args : a0;
+    const JobGeo jg = MULTI ? geo_of(w, w.jobs[j]) : geo_of(w);
+    if (MULTI) {
+        item -= w.jobs[j].item_base;
+        w.job[slot] = j;
+    }
+    const int g = item / jg.npix;
+    const int p = jg.first_pix + (item - g * jg.npix);
     uint32_t fl = g == 0 ? 0u : F_GBUF;   // only group 0 writes the G-buffer
     Pcg32 rng;
     w.pixel[slot] = p;
     w.pix[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
     w.nee[slot] = 0;
-    start_sample(s, w, a.seed, slot, p, g * w.S, rng, fl);
+    start_sample(s, w, a.seed, slot, p, g * jg.S, rng, fl);
     w.flags[slot] = fl;
     w.rng[slot] = rng.state;
 }
 
 // Takes the next item for the slot (or leaves it idle) and queues its first ray.
-__device__ __forceinline__ void next_item(const SceneView& s, const Wf& w, const RenderArgs& a, int slot, int nq)
+template <bool MULTI>
+__device__ __forceinline__ void next_item(const SceneView& s0, const Wf& w, const RenderArgs& a0, int slot, int nq)
 {
     int item = atomicAdd(&w.cnt[6], 1);
     if (item >= w.n_items) {
         w.pixel[slot] = -1;
         return;
     }
-    start_item(s, w, a, slot, item);
+    start_item<MULTI>(s0, w, a0, slot, item);
     append(w.q + (size_t)nq * w.M, &w.cnt[nq], slot);
 }
 
-__global__ void k_wf_init(SceneView s, Wf w, RenderArgs a)
+template <bool MULTI>
+__global__ void k_wf_init(const __grid_constant__ SceneView s, Wf w, const __grid_constant__ RenderArgs a)
 {
     int slot = blockIdx.x * blockDim.x + threadIdx.x;
     if (slot >= w.M) return;
@@ -221,19 +282,20 @@ __global__ void k_wf_init(SceneView s, Wf w, RenderArgs a)
         w.cnt[8] = w.cnt[9] = w.cnt[10] = w.cnt[11] = 0;
         for (int k = CNT_BIN; k < CNT_WORDS; ++k) w.cnt[k] = 0;
     }
-    start_item(s, w, a, slot, slot);
+    start_item<MULTI>(s, w, a, slot, slot);
     w.q[slot] = slot;   // Q_0 holds every slot in order
 }
 
-// Pixel = (sum of its group sums in group order) / spp, as the megakernel adds them.
-__global__ void k_wf_finish(Wf w, RenderArgs a, int groups)
+// Pixel = (sum of its group sums in group order) / spp, as the megakernel adds them (one render,
+// or one job of a batch).
+__global__ void k_wf_finish(JobGeo jg, RenderArgs a, int groups)
 {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= w.npix) return;
+    if (p >= jg.npix) return;
     float3 sum = f3(0.f, 0.f, 0.f);
-    for (int g = 0; g < groups; ++g) sum = sum + xyz(w.part[(size_t)g * w.npix + p]);
+    for (int g = 0; g < groups; ++g) sum = sum + xyz(jg.part[(size_t)g * jg.npix + p]);
     float3 v = sum / (float)a.spp;
-    size_t off = (size_t)(w.first_pix + p);
+    size_t off = (size_t)(jg.first_pix + p);
     if (a.flags & CPT_RENDER_ACCUMULATE) {
         a.rgb[3 * off] += v.x;
         a.rgb[3 * off + 1] += v.y;
@@ -248,8 +310,8 @@ __global__ void k_wf_finish(Wf w, RenderArgs a, int groups)
 
 // At most 48 registers (5 blocks of 256 per SM): 62 % occupancy instead of 50 % for a few spilled
 // values, +5.7 % on the 1080p spheres render (the shadow kernel is faster uncapped).
-template <bool WIDE, int SHORT, bool SORT>
-__global__ void __launch_bounds__(256, 5) k_wf_trace(SceneView s, Wf w, int par)
+template <bool WIDE, int SHORT, bool SORT, bool MULTI>
+__global__ void __launch_bounds__(256, 5) k_wf_trace(const __grid_constant__ SceneView s, Wf w, int par)
 {
     const int n = w.cnt[par];
     const int nq = par ^ 1;
@@ -264,46 +326,50 @@ __global__ void __launch_bounds__(256, 5) k_wf_trace(SceneView s, Wf w, int par)
     const int* q = w.q + (size_t)par * w.M;
     int* const bins = SORT ? w.bins + (size_t)par * NBIN * w.M : nullptr;
     int* const bin_cnt = w.cnt + CNT_BIN + par * NBIN;
+    const auto views = [&](int j) -> const SceneView& { return MULTI ? w.jobs[j].view : s; };
     uint32_t rays = 0;
-    if (!WIDE && s.n_internal > 0) {
-        rays = trace_items_bvh2<false, ShortStackN<SHORT>>(
-            s, n, &w.cnt[8 + 2 * par], w.err,
-            [&](int i, float3& o, float3& d, float& tmn, float& tmx, int&) {
+    if (!WIDE && (MULTI ? w.all_bvh2 != 0 : s.n_internal > 0)) {
+        rays = trace_items_bvh2_views<false, ShortStackN<SHORT>>(
+            views, n, &w.cnt[8 + 2 * par], w.err,
+            [&](int i, float3& o, float3& d, float& tmn, float& tmx, int&, int& j) {
                 int slot = q[i];
                 o = xyz(w.o[slot]);
                 d = xyz(w.d[slot]);
                 tmn = 0.001f;
                 tmx = CPT_INF_F;
+                j = MULTI ? w.job[slot] : 0;
             },
-            [&](int i, const Hit& h) {
+            [&](int i, const Hit& h, int j) {
                 const int slot = q[i];
                 w.hit[slot] = make_float4(h.t, __int_as_float(h.leaf), h.u, h.v);
-                if (SORT) append_binned(bins, bin_cnt, w.M, shade_bin(s, h.leaf), slot);
+                if (SORT) append_binned(bins, bin_cnt, w.M, shade_bin(views(j), h.leaf), slot);
             });
     } else {
         for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
             int slot = q[idx];
+            const SceneView& sv = views(MULTI ? w.job[slot] : 0);
             float4 o = w.o[slot], d = w.d[slot];
             Hit h;
-            bool hit = trace_closest<WIDE>(s, xyz(o), xyz(d), 0.001f, CPT_INF_F, h, w.err);
+            bool hit = trace_closest<WIDE>(sv, xyz(o), xyz(d), 0.001f, CPT_INF_F, h, w.err);
             w.hit[slot] = make_float4(h.t, __int_as_float(hit ? h.leaf : -1), h.u, h.v);
-            if (SORT) append_binned(bins, bin_cnt, w.M, shade_bin(s, hit ? h.leaf : -1), slot);
+            if (SORT) append_binned(bins, bin_cnt, w.M, shade_bin(sv, hit ? h.leaf : -1), slot);
             rays++;
         }
     }
     count_rays(w.rays, rays);
 }
 
-template <bool WIDE, int SHORT>
-__global__ void __launch_bounds__(256) k_wf_shadow(SceneView s, Wf w, int par)
+template <bool WIDE, int SHORT, bool MULTI>
+__global__ void __launch_bounds__(256) k_wf_shadow(const __grid_constant__ SceneView s, Wf w, int par)
 {
     const int n = w.cnt[4 + par];
     const int* sq = w.sq + (size_t)par * w.M * w.L;
+    const auto views = [&](int j) -> const SceneView& { return MULTI ? w.jobs[j].view : s; };
     uint32_t rays = 0;
-    if (!WIDE && s.n_internal > 0) {
-        rays = trace_items_bvh2<true, ShortStackN<SHORT>>(
-            s, n, &w.cnt[9 + 2 * par], w.err,
-            [&](int i, float3& o, float3& d, float& tmn, float& tmx, int& skip) {
+    if (!WIDE && (MULTI ? w.all_bvh2 != 0 : s.n_internal > 0)) {
+        rays = trace_items_bvh2_views<true, ShortStackN<SHORT>>(
+            views, n, &w.cnt[9 + 2 * par], w.err,
+            [&](int i, float3& o, float3& d, float& tmn, float& tmx, int& skip, int& j) {
                 int e = sq[i];
                 float4 dd = w.sd[e];
                 o = xyz(w.so[e]);
@@ -311,13 +377,15 @@ __global__ void __launch_bounds__(256) k_wf_shadow(SceneView s, Wf w, int par)
                 tmn = 0.001f;
                 tmx = dd.w;
                 skip = e % w.L;
+                j = MULTI ? w.job[e / w.L] : 0;
             },
-            [&](int i, const Hit& h) { w.svis[sq[i]] = h.leaf < 0 ? 1 : 0; });
+            [&](int i, const Hit& h, int) { w.svis[sq[i]] = h.leaf < 0 ? 1 : 0; });
     } else {
         for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
             int e = sq[idx];
+            const SceneView& sv = views(MULTI ? w.job[e / w.L] : 0);
             float4 dd = w.sd[e];
-            w.svis[e] = occluded<WIDE>(s, xyz(w.so[e]), xyz(dd), dd.w, e % w.L, w.err) ? 0 : 1;
+            w.svis[e] = occluded<WIDE>(sv, xyz(w.so[e]), xyz(dd), dd.w, e % w.L, w.err) ? 0 : 1;
             rays++;
         }
     }
@@ -335,7 +403,9 @@ __device__ __forceinline__ float3 add_visible(const Wf& w, int slot, int mask, f
     return acc;
 }
 
-__global__ void __launch_bounds__(256) k_wf_resolve(SceneView s, Wf w, RenderArgs a, int par)
+template <bool MULTI>
+__global__ void __launch_bounds__(256) k_wf_resolve(const __grid_constant__ SceneView s, Wf w,
+                                                    const __grid_constant__ RenderArgs a, int par)
 {
     const int n = w.cnt[2 + par];
     const int nq = par ^ 1;
@@ -345,14 +415,21 @@ __global__ void __launch_bounds__(256) k_wf_resolve(SceneView s, Wf w, RenderArg
         float3 acc = add_visible(w, slot, w.nee[slot], xyz(w.radp[slot]));
         w.pix[slot] = w0(xyz(w.pix[slot]) + acc);
         w.nee[slot] = 0;
-        finish_item(w, a, slot, w.pixel[slot], w.flags[slot]);
-        next_item(s, w, a, slot, nq);
+        if (MULTI) {
+            const WfJob& J = w.jobs[w.job[slot]];
+            finish_item(w, J.args, geo_of(w, J), slot, w.pixel[slot], w.flags[slot]);
+        } else {
+            finish_item(w, a, geo_of(w), slot, w.pixel[slot], w.flags[slot]);
+        }
+        next_item<MULTI>(s, w, a, slot, nq);
     }
 }
 
 // At most 64 registers (4 blocks of 256 per SM, 50 % occupancy instead of 37 % at 79 registers):
 // +4.4 % on the 1080p spheres render; 48 registers: +3.7 %.
-__global__ void __launch_bounds__(256, 4) k_wf_shade(SceneView s, Wf w, RenderArgs a, int par)
+template <bool MULTI>
+__global__ void __launch_bounds__(256, 4) k_wf_shade(const __grid_constant__ SceneView s0, Wf w,
+                                                     const __grid_constant__ RenderArgs a0, int par)
 {
     const int nq = par ^ 1;
     // the traced slots: the bins in order (material sort), else the trace queue
@@ -373,6 +450,9 @@ __global__ void __launch_bounds__(256, 4) k_wf_shade(SceneView s, Wf w, RenderAr
         }
         const int slot = q[pos];
         const int pixel = w.pixel[slot];
+        const int job = MULTI ? w.job[slot] : 0;
+        const SceneView& s = MULTI ? w.jobs[job].view : s0;
+        const RenderArgs& a = MULTI ? w.jobs[job].args : a0;
         uint32_t fl = w.flags[slot];
         Pcg32 rng;
         rng.state = w.rng[slot];
@@ -526,13 +606,14 @@ __global__ void __launch_bounds__(256, 4) k_wf_shade(SceneView s, Wf w, RenderAr
             } else {
                 w.pix[slot] = w0(xyz(w.pix[slot]) + rad);
             }
-            if (k % w.S != 0 && k < a.spp) {   // the item's group has samples left
+            const JobGeo jg = MULTI ? geo_of(w, w.jobs[job]) : geo_of(w);
+            if (k % jg.S != 0 && k < a.spp) {   // the item's group has samples left
                 start_sample(s, w, a.seed, slot, pixel, k, rng, fl);
                 to_trace = true;
             } else {
                 w.sample[slot] = k;
                 if (nee) to_resolve = true;
-                else finish_item(w, a, slot, pixel, fl);
+                else finish_item(w, a, jg, slot, pixel, fl);
             }
         }
         w.flags[slot] = fl;
@@ -542,7 +623,7 @@ __global__ void __launch_bounds__(256, 4) k_wf_shade(SceneView s, Wf w, RenderAr
                 if ((nee >> k) & 1) append(w.sq + (size_t)nq * w.M * w.L, &w.cnt[4 + nq], slot * w.L + k);
         if (to_trace) append(w.q + (size_t)nq * w.M, &w.cnt[nq], slot);
         if (to_resolve) append(w.rq + (size_t)nq * w.M, &w.cnt[2 + nq], slot);
-        if (!cont && !to_trace && !to_resolve) next_item(s, w, a, slot, nq);
+        if (!cont && !to_trace && !to_resolve) next_item<MULTI>(s0, w, a0, slot, nq);
     }
 }
 
@@ -551,33 +632,35 @@ struct TracePair {
     WfKernel trace, shadow;
 };
 
-// The trace kernels for the scene's layout, the short-stack depth (binary layout only) and the
+// The trace kernels for the scene's layout, the short-stack depth (binary layout only), the
 // material sort (the binning is compiled only into the sorting variants, so that the default
-// trace kernel keeps its registers).
-template <bool SORT>
+// trace kernel keeps its registers) and batches.
+template <bool SORT, bool MULTI>
 TracePair trace_pair_of(bool wide, int short_entries)
 {
-    if (wide) return {k_wf_trace<true, CPT_SHORT_STACK, SORT>, k_wf_shadow<true, CPT_SHORT_STACK>};
+    if (wide) return {k_wf_trace<true, CPT_SHORT_STACK, SORT, MULTI>, k_wf_shadow<true, CPT_SHORT_STACK, MULTI>};
     switch (short_entries) {
-    case 8: return {k_wf_trace<false, 8, SORT>, k_wf_shadow<false, 8>};
-    case 24: return {k_wf_trace<false, 24, SORT>, k_wf_shadow<false, 24>};
-    case 32: return {k_wf_trace<false, 32, SORT>, k_wf_shadow<false, 32>};
-    default: return {k_wf_trace<false, 16, SORT>, k_wf_shadow<false, 16>};
+    case 8: return {k_wf_trace<false, 8, SORT, MULTI>, k_wf_shadow<false, 8, MULTI>};
+    case 24: return {k_wf_trace<false, 24, SORT, MULTI>, k_wf_shadow<false, 24, MULTI>};
+    case 32: return {k_wf_trace<false, 32, SORT, MULTI>, k_wf_shadow<false, 32, MULTI>};
+    default: return {k_wf_trace<false, 16, SORT, MULTI>, k_wf_shadow<false, 16, MULTI>};
     }
 }
 
-TracePair trace_pair(bool wide, int short_entries, bool sort = false)
+TracePair trace_pair(bool wide, int short_entries, bool sort = false, bool multi = false)
 {
-    return sort ? trace_pair_of<true>(wide, short_entries) : trace_pair_of<false>(wide, short_entries);
+    if (multi) return sort ? trace_pair_of<true, true>(wide, short_entries) : trace_pair_of<false, true>(wide, short_entries);
+    return sort ? trace_pair_of<true, false>(wide, short_entries) : trace_pair_of<false, false>(wide, short_entries);
 }
 
 // CHUNK iterations: trace, shadow, resolve, shade, with the traversal of the scene's layout.
 // When capturing with a side stream, the shadow kernel is forked onto it so that the two
 // traversal kernels of an iteration overlap (each one's tail fills with the other's warps).
+template <bool MULTI>
 void enqueue_chunk(const SceneView& view, const Wf& w, const RenderArgs& args, int gt, int bt, int gs, int bs,
                    int short_entries, cudaStream_t st, const WavefrontTuning* fork)
 {
-    const TracePair kp = trace_pair(view.wide != nullptr, short_entries, w.bins != nullptr);
+    const TracePair kp = trace_pair(view.wide != nullptr, short_entries, w.bins != nullptr, MULTI);
     const size_t smem = short_stack_bytes(bt, short_entries);
     for (int it = 0; it < CHUNK; ++it) {
         int par = it & 1;
@@ -593,8 +676,8 @@ void enqueue_chunk(const SceneView& view, const Wf& w, const RenderArgs& args, i
             cudaEventRecord(fork->join, ss);
             cudaStreamWaitEvent(st, fork->join, 0);
         }
-        k_wf_resolve<<<gs, bs, 0, st>>>(view, w, args, par);
-        k_wf_shade<<<gs, bs, 0, st>>>(view, w, args, par);
+        k_wf_resolve<MULTI><<<gs, bs, 0, st>>>(view, w, args, par);
+        k_wf_shade<MULTI><<<gs, bs, 0, st>>>(view, w, args, par);
     }
 }
 
@@ -609,63 +692,100 @@ cpt_status carve(char*& p, size_t& left, T** out, size_t count)
     return CPT_OK;
 }
 
-size_t wf_bytes(int M, int L, size_t n_items, bool sort)
+size_t wf_bytes(int M, int L, size_t n_parts, bool sort, int n_jobs)
 {
     size_t m = (size_t)M, ml = (size_t)M * std::max(L, 1);
     auto a = [](size_t b) { return align_up(b, 256); };
-    return a(m * 4) * 6 + a(m * 8) + a(m * 16) * 8 + a(n_items * 16) + a(m * 8) + a(2 * m * 4) * 2 +
-           a(2 * ml * 4) + a(ml * 16) * 3 + a(ml * 4) + a(CNT_WORDS * 4) + (sort ? a(2 * NBIN * m * 4) : 0);
+    return a(m * 4) * 6 + a(m * 8) + a(m * 16) * 8 + a(n_parts * 16) + a(m * 8) + a(2 * m * 4) * 2 +
+           a(2 * ml * 4) + a(ml * 16) * 3 + a(ml * 4) + a(CNT_WORDS * 4) + (sort ? a(2 * NBIN * m * 4) : 0) +
+           (n_jobs > 0 ? a(m * 4) + a((size_t)n_jobs * sizeof(WfJob)) : 0);
 }
 
 }  // namespace
 
-cpt_status launch_render_wavefront(const SceneView& view, const RenderArgs& args, cudaStream_t stream,
-                                   const WavefrontTuning& tune)
+namespace {
+
+// A single render (jobs empty: scene and parameters in kernel arguments) or a batch (MULTI).
+template <bool MULTI>
+cpt_status run_wavefront(const SceneView& view, const RenderArgs& args, const std::vector<WfJob>& jobs,
+                         cudaStream_t stream, const WavefrontTuning& tune)
 {
-    int W = view.cam.width;
-    int first = args.row_begin * W, end = args.row_end * W;
-    int npix = end - first;
-    if (npix <= 0) return CPT_OK;
-    int L = std::max(view.n_lights, 1);
-    if (view.n_lights > 30) return fail(CPT_ERR_UNSUPPORTED, "wavefront integrator: at most 30 lights");
-    if (args.spp <= 0) return fail(CPT_ERR_INVALID_ARGUMENT, "spp must be positive");
-    const int S = sample_group(args.spp);
-    const int groups = (args.spp + S - 1) / S;
-    const size_t n_items = (size_t)groups * (size_t)npix;
-    if (n_items > (size_t)INT32_MAX / 2) return fail(CPT_ERR_UNSUPPORTED, "wavefront integrator: too many pixel groups");
-    int M = (int)std::min(n_items, (size_t)std::max(tune.slots, 1024));
     Wf w;
     std::memset(&w, 0, sizeof w);
+    size_t n_items = 0, n_parts = 0;
+    int L = 1;
+    std::vector<WfJob> J = jobs;
+    if (!MULTI) {
+        const int W = view.cam.width;
+        const int first = args.row_begin * W, end = args.row_end * W;
+        w.first_pix = first;
+        w.npix = end - first;
+        if (w.npix <= 0) return CPT_OK;
+        if (view.n_lights > 30) return fail(CPT_ERR_UNSUPPORTED, "wavefront integrator: at most 30 lights");
+        if (args.spp <= 0) return fail(CPT_ERR_INVALID_ARGUMENT, "spp must be positive");
+        w.S = sample_group(args.spp);
+        n_items = n_parts = (size_t)((args.spp + w.S - 1) / w.S) * (size_t)w.npix;
+        L = std::max(view.n_lights, 1);
+    } else {
+        for (WfJob& j : J) {
+            if (j.view.n_lights > 30) return fail(CPT_ERR_UNSUPPORTED, "wavefront integrator: at most 30 lights");
+            if (j.args.spp <= 0) return fail(CPT_ERR_INVALID_ARGUMENT, "spp must be positive");
+            const int W = j.view.cam.width;
+            j.first_pix = j.args.row_begin * W;
+            j.npix = j.args.row_end * W - j.first_pix;
+            j.S = sample_group(j.args.spp);
+            j.item_base = (int)std::min(n_items, (size_t)INT32_MAX);
+            j.part_base = (long long)n_parts;
+            const size_t items = (size_t)((j.args.spp + j.S - 1) / j.S) * (size_t)std::max(j.npix, 0);
+            n_items += items;
+            n_parts += items;
+            L = std::max(L, j.view.n_lights);
+        }
+        w.all_bvh2 = 1;
+        for (const WfJob& j : J)
+            if (j.view.wide != nullptr || j.view.n_internal <= 0) w.all_bvh2 = 0;
+        if (n_items == 0) return CPT_OK;
+    }
+    if (n_items > (size_t)INT32_MAX / 2) return fail(CPT_ERR_UNSUPPORTED, "wavefront integrator: too many pixel groups");
+    const int M = (int)std::min(n_items, (size_t)std::max(tune.slots, 1024));
     w.M = M;
     w.L = L;
-    w.first_pix = first;
-    w.npix = npix;
-    w.S = S;
     w.n_items = (int)n_items;
     w.rays = args.ray_counter;
     w.err = args.err;
-    size_t bytes = wf_bytes(M, L, n_items, tune.material_sort);
+    w.n_jobs = MULTI ? (int)J.size() : 0;
+    size_t bytes = wf_bytes(M, L, n_parts, tune.material_sort, w.n_jobs);
     char* base = nullptr;
     CPT_CUDA(cudaMallocAsync((void**)&base, bytes, stream));
     char* p = base;
     size_t left = bytes;
     size_t ml = (size_t)M * L;
     cpt_status st = CPT_OK;
+    WfJob* d_jobs = nullptr;
 #define CARVE(f, n)                                   \
     if (st == CPT_OK) st = carve(p, left, &w.f, (n));
     CARVE(pixel, M) CARVE(sample, M) CARVE(flags, M) CARVE(depth, M) CARVE(guard, M) CARVE(nee, M)
     CARVE(rng, M) CARVE(o, M) CARVE(d, M) CARVE(thr, M) CARVE(rad, M) CARVE(radp, M) CARVE(pix, M) CARVE(hit, M)
-    CARVE(part, n_items)
+    CARVE(part, n_parts)
     CARVE(so, ml) CARVE(med, M) CARVE(q, 2 * (size_t)M) CARVE(rq, 2 * (size_t)M) CARVE(sq, 2 * ml) CARVE(sd, ml)
     CARVE(sc, ml) CARVE(svis, ml) CARVE(cnt, CNT_WORDS)
     if (tune.material_sort) CARVE(bins, 2 * (size_t)NBIN * M)
+    if (MULTI) CARVE(job, M)
 #undef CARVE
+    if (MULTI && st == CPT_OK) {
+        st = carve(p, left, &d_jobs, J.size());
+        if (st == CPT_OK) {
+            cudaError_t e = cudaMemcpyAsync(d_jobs, J.data(), J.size() * sizeof(WfJob), cudaMemcpyHostToDevice, stream);
+            if (e != cudaSuccess) st = cuda_fail(e, "batch job table");
+        }
+        w.jobs = d_jobs;
+    }
     if (st != CPT_OK) {
         cudaFreeAsync(base, stream);
         return st;
     }
     // Q_0 = all M slots
-    k_wf_init<<<(M + 255) / 256, 256, 0, stream>>>(view, w, args);
+    k_wf_init<MULTI><<<(M + 255) / 256, 256, 0, stream>>>(view, w, args);
     add_launches(1);
     const int gt = tune.grid_trace, gs = tune.grid_shade;
     const int bt = tune.block_trace, bs = tune.block_shade;
@@ -676,7 +796,7 @@ cpt_status launch_render_wavefront(const SceneView& view, const RenderArgs& args
         // Capture CHUNK iterations (4 launches each) once; replay until the queues drain.
         cudaStream_t cs = tune.capture_stream;
         CPT_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
-        enqueue_chunk(view, w, args, gt, bt, gs, bs, tune.short_stack, cs, tune.side_stream ? &tune : nullptr);
+        enqueue_chunk<MULTI>(view, w, args, gt, bt, gs, bs, tune.short_stack, cs, tune.side_stream ? &tune : nullptr);
         cudaError_t ce = cudaStreamEndCapture(cs, &graph);
         if (ce != cudaSuccess) {
             cudaFreeAsync(base, stream);
@@ -696,7 +816,7 @@ cpt_status launch_render_wavefront(const SceneView& view, const RenderArgs& args
         if (use_graph) {
             CPT_CUDA(cudaGraphLaunch(exec, stream));
         } else {
-            enqueue_chunk(view, w, args, gt, bt, gs, bs, tune.short_stack, stream, nullptr);
+            enqueue_chunk<MULTI>(view, w, args, gt, bt, gs, bs, tune.short_stack, stream, nullptr);
         }
         add_launches(4 * CHUNK);
         CPT_CUDA(cudaMemcpyAsync(host_cnt, w.cnt, sizeof host_cnt, cudaMemcpyDeviceToHost, stream));
@@ -708,13 +828,46 @@ cpt_status launch_render_wavefront(const SceneView& view, const RenderArgs& args
     }
     if (exec) cudaGraphExecDestroy(exec);
     if (drained) {
-        k_wf_finish<<<(npix + 255) / 256, 256, 0, stream>>>(w, args, groups);
-        add_launches(1);
+        if (!MULTI) {
+            const int groups = (args.spp + w.S - 1) / w.S;
+            k_wf_finish<<<(w.npix + 255) / 256, 256, 0, stream>>>(JobGeo{w.first_pix, w.npix, w.S, w.part}, args,
+                                                                  groups);
+            add_launches(1);
+        } else {
+            for (const WfJob& j : J) {
+                if (j.npix <= 0) continue;
+                const int groups = (j.args.spp + j.S - 1) / j.S;
+                k_wf_finish<<<(j.npix + 255) / 256, 256, 0, stream>>>(
+                    JobGeo{j.first_pix, j.npix, j.S, w.part + j.part_base}, j.args, groups);
+                add_launches(1);
+            }
+        }
     }
     cudaFreeAsync(base, stream);
     CPT_CUDA(cudaGetLastError());
     if (!drained) return fail(CPT_ERR_TIMEOUT, "wavefront integrator did not drain");
     return CPT_OK;
+}
+
+}  // namespace
+
+cpt_status launch_render_wavefront(const SceneView& view, const RenderArgs& args, cudaStream_t stream,
+                                   const WavefrontTuning& tune)
+{
+    return run_wavefront<false>(view, args, {}, stream, tune);
+}
+
+cpt_status launch_render_wavefront_batch(const SceneView* views, const RenderArgs* args, int n_jobs,
+                                         cudaStream_t stream, const WavefrontTuning& tune)
+{
+    if (n_jobs <= 0) return CPT_OK;
+    std::vector<WfJob> jobs(n_jobs);
+    for (int i = 0; i < n_jobs; ++i) {
+        std::memset(&jobs[i], 0, sizeof(WfJob));
+        jobs[i].view = views[i];
+        jobs[i].args = args[i];
+    }
+    return run_wavefront<true>(views[0], args[0], jobs, stream, tune);
 }
 
 }  // namespace cpt
@@ -732,14 +885,14 @@ cpt_status wavefront_grids(int sm_count, int block_trace, int block_shade, int s
     cudaFuncAttributes fa[3];
     CPT_CUDA(cudaFuncGetAttributes(&fa[0], wide.trace));
     CPT_CUDA(cudaFuncGetAttributes(&fa[1], bin.trace));
-    CPT_CUDA(cudaFuncGetAttributes(&fa[2], k_wf_shade));
+    CPT_CUDA(cudaFuncGetAttributes(&fa[2], k_wf_shade<false>));
     if (block_trace > std::min(fa[0].maxThreadsPerBlock, fa[1].maxThreadsPerBlock) ||
         block_shade > fa[2].maxThreadsPerBlock)
         return fail(CPT_ERR_INVALID_ARGUMENT, "wavefront block size above the kernels' limit");
     CPT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bt, wide.trace, block_trace, smem));
     CPT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bt2, bin.trace, block_trace, smem));
     bt = std::min(bt, bt2);
-    CPT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bs, k_wf_shade, block_shade, 0));
+    CPT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bs, k_wf_shade<false>, block_shade, 0));
     *grid_trace = std::max(1, bt) * sm_count;
     *grid_shade = std::max(1, bs) * sm_count;
     return CPT_OK;

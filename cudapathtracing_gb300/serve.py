@@ -1,4 +1,5 @@
-"""Render serving loop: Poisson-arriving jobs, admission by HBM budget, concurrent lanes.
+"""Render serving loop: Poisson-arriving jobs, admission by HBM budget, concurrent lanes, and
+wavefronts batched across jobs.
 
 A job is a seeded scene of the icosphere type (procedural.random_scene) at one resolution and
 spp, optionally denoised.  Jobs arrive as a Poisson process; the scheduler admits them in arrival
@@ -8,11 +9,18 @@ to a free lane.  A lane is a host thread with its own library context and CUDA s
 on different lanes overlap on the GPU; a job's scene, BVH and accumulation buffers stay on the
 device for its whole life (uploaded once, rendered into device buffers, denoised in place).
 
-The scheduler is plain host logic over an executor interface (run(job) -> rays), so its
-admission, ordering and failure handling are tested without a GPU (tests/test_serve.py, with a
-fake executor that can fail or report out-of-memory on demand).
+With batch > 1 a free lane takes up to `batch` queued jobs that fit the budget together and runs
+them as one batch: their scenes are uploaded and built, then one cpt_render_batch renders all of
+them in a single wavefront (paths of every job share the path slots and persistent kernels, so a
+few small jobs fill the GPU together), then each job is denoised.  A batch's rays are recorded on
+each of its jobs as batch_rays and counted once in the summary.
 
-    python -m cudapathtracing_gb300.serve --jobs 24 --rate 20 --lanes 3
+The scheduler is plain host logic over an executor interface (run(job, lane) -> rays, and
+run_batch(jobs, lane) -> rays for batches), so its admission, ordering, batching and failure
+handling are tested without a GPU (tests/test_serve.py, with a fake executor that can fail or
+report out-of-memory on demand).
+
+    python -m cudapathtracing_gb300.serve --jobs 24 --rate 20 --lanes 3 --batch 4
 """
 from __future__ import annotations
 
@@ -42,6 +50,7 @@ class Job:
     start: float = field(compare=False, default=0.0)
     end: float = field(compare=False, default=0.0)
     rays: int = field(compare=False, default=0)
+    batch: int = field(compare=False, default=-1)      # batch number (-1: rendered alone)
     status: str = field(compare=False, default="queued")
     error: str = field(compare=False, default="")
 
@@ -69,25 +78,29 @@ def job_bytes(num_triangles: int, size: int, spp: int, slots: int = 1 << 21) -> 
 
 class Scheduler:
     """Admission by HBM budget (FIFO: a job that does not fit waits, and so do the jobs behind
-    it), up to `lanes` jobs at once.  executor.run(job, lane) returns the rays traced or raises;
-    MemoryError from the executor puts the job back at the head of the queue until another job
-    frees memory (or fails it when nothing else is running)."""
+    it), up to `lanes` batches at once, each of up to `batch` jobs.  executor.run(job, lane)
+    returns the rays traced or raises; executor.run_batch(jobs, lane) does the same for a batch
+    of two or more jobs (its rays are the whole batch's).  MemoryError from the executor puts
+    the jobs back at the head of the queue until other jobs free memory (or fails them when
+    nothing else is running); any other exception fails every job of the batch."""
 
-    def __init__(self, executor, budget_bytes: int, lanes: int = 2, clock=time.perf_counter):
+    def __init__(self, executor, budget_bytes: int, lanes: int = 2, clock=time.perf_counter, batch: int = 1):
         self.ex = executor
         self.budget = budget_bytes
         self.lanes = lanes
+        self.batch = max(1, int(batch))
         self.clock = clock
         self.in_use = 0
         self.peak = 0
+        self.batches = 0
         self.lock = threading.Condition()
         self.free_lanes = list(range(lanes))
 
-    def _admit(self, job) -> bool:
+    def _admit(self, job, need_lane: bool = True) -> bool:
         if job.bytes > self.budget:
             job.status, job.error = "rejected", "larger than the HBM budget"
             return True
-        if self.in_use + job.bytes <= self.budget and self.free_lanes:
+        if self.in_use + job.bytes <= self.budget and (self.free_lanes or not need_lane):
             self.in_use += job.bytes
             self.peak = max(self.peak, self.in_use)
             return True
@@ -100,21 +113,32 @@ class Scheduler:
         running = [0]
         t0 = self.clock()
 
-        def worker(job, lane):
+        def worker(batch, lane):
             failed_oom = False
             try:
-                job.rays = int(self.ex.run(job, lane))
-                job.status = "done"
+                if len(batch) == 1:
+                    rays = [int(self.ex.run(batch[0], lane))]
+                else:
+                    total = int(self.ex.run_batch(batch, lane))
+                    rays = [total] * len(batch)
+                for job, r in zip(batch, rays):
+                    job.rays = r
+                    job.status = "done"
             except MemoryError as e:
-                job.status, job.error, failed_oom = "oom", str(e), True
-            except Exception as e:   # a failed job frees its budget and its lane
-                job.status, job.error = "failed", f"{type(e).__name__}: {e}"
-            job.end = self.clock() - t0
+                failed_oom = True
+                for job in batch:
+                    job.status, job.error = "oom", str(e)
+            except Exception as e:   # a failed batch frees its budget and its lane
+                for job in batch:
+                    job.status, job.error = "failed", f"{type(e).__name__}: {e}"
+            end = self.clock() - t0
             with self.lock:
-                self.in_use -= job.bytes
+                for job in batch:
+                    job.end = end
+                    self.in_use -= job.bytes
                 running[0] -= 1
                 self.free_lanes.append(lane)
-                (oom if failed_oom else done).append(job)
+                (oom if failed_oom else done).extend(batch)
                 self.lock.notify_all()
 
         i = 0
@@ -136,20 +160,31 @@ class Scheduler:
                     else:
                         job.status = "queued"
                         heapq.heappush(queue, job)
-                while queue:
-                    job = queue[0]
-                    if not self._admit(job):
+                while queue and self.free_lanes:
+                    batch = []
+                    while queue and len(batch) < self.batch:
+                        job = queue[0]
+                        if not self._admit(job, need_lane=not batch):
+                            break
+                        heapq.heappop(queue)
+                        if job.status == "rejected":
+                            job.end = self.clock() - t0
+                            done.append(job)
+                            continue
+                        batch.append(job)
+                    if not batch:
                         break
-                    heapq.heappop(queue)
-                    if job.status == "rejected":
-                        job.end = self.clock() - t0
-                        done.append(job)
-                        continue
                     lane = self.free_lanes.pop(0)
-                    job.status = "running"
-                    job.start = self.clock() - t0
+                    bid = -1
+                    if len(batch) > 1:
+                        bid = self.batches
+                        self.batches += 1
+                    for job in batch:
+                        job.status = "running"
+                        job.start = self.clock() - t0
+                        job.batch = bid
                     running[0] += 1
-                    th = threading.Thread(target=worker, args=(job, lane), daemon=True)
+                    th = threading.Thread(target=worker, args=(batch, lane), daemon=True)
                     threads.append(th)
                     th.start()
                 if len(done) >= len(jobs):
@@ -166,13 +201,15 @@ class Scheduler:
 def summary(jobs, wall: float) -> dict:
     ok = [j for j in jobs if j.status == "done"]
     lat = np.array([j.end - j.arrival for j in ok]) if ok else np.zeros(1)
-    rays = sum(j.rays for j in ok)
+    batched = {j.batch: j.rays for j in ok if j.batch >= 0}   # a batch's rays once
+    rays = sum(j.rays for j in ok if j.batch < 0) + sum(batched.values())
     return {"jobs": len(jobs), "done": len(ok), "failed": sum(j.status == "failed" for j in jobs),
             "rejected": sum(j.status == "rejected" for j in jobs),
             "latency_p50_s": round(float(np.percentile(lat, 50)), 4),
             "latency_p99_s": round(float(np.percentile(lat, 99)), 4),
             "latency_mean_s": round(float(lat.mean()), 4), "wall_s": round(wall, 3),
-            "mrays_per_s": round(rays / max(wall, 1e-9) / 1e6, 1), "rays": int(rays)}
+            "mrays_per_s": round(rays / max(wall, 1e-9) / 1e6, 1), "rays": int(rays),
+            "batches": len(batched), "jobs_in_batches": sum(j.batch >= 0 for j in ok)}
 
 
 class GpuExecutor:
@@ -220,6 +257,37 @@ class GpuExecutor:
         return r["rays"]
 
 
+    def run_batch(self, jobs, lane) -> int:
+        """The jobs' scenes uploaded and built on the lane's stream, one cpt_render_batch over all
+        of them (one wavefront), then each denoised; returns the batch's rays."""
+        import torch
+        from . import api
+        from .training import RENDER
+        st = self.streams[lane]
+        scenes, outs = [], []
+        try:
+            with torch.cuda.stream(st):
+                for job in jobs:
+                    sc = api.Scene(self.ctx[lane], self.descs[job.jid])
+                    sc.buildBVH(st.cuda_stream)
+                    scenes.append(sc)
+                    outs.append((torch.zeros((sc.height, sc.width, 3), device="cuda"),
+                                 torch.zeros((sc.height, sc.width, 8), device="cuda") if job.denoise else None))
+                prm = {k: v for k, v in RENDER.items() if k not in ("estimator", "integrator")}
+                r = api.render_batch(self.ctx[lane], [dict(scene=sc, spp=job.spp, seed=job.seed, rgb=o[0],
+                                                           gbuffer=o[1], **prm)
+                                                      for sc, job, o in zip(scenes, jobs, outs)],
+                                     stream=st.cuda_stream)
+                for job, o in zip(jobs, outs):
+                    if job.denoise:
+                        self.den[lane].denoise(o[0], o[1], stream=C_stream(st))
+                st.synchronize()
+        finally:
+            for sc in scenes:
+                sc.close()
+        return r["rays"]
+
+
 def C_stream(st):
     import ctypes
     return ctypes.c_void_p(st.cuda_stream)
@@ -233,6 +301,7 @@ def main():
     ap.add_argument("--budget-gb", type=float, default=64.0)
     ap.add_argument("--max-level", type=int, default=6)
     ap.add_argument("--seed", type=int, default=3)
+    ap.add_argument("--batch", type=int, default=1, help="jobs per wavefront (cross-job batching)")
     args = ap.parse_args()
     import json
     from .training import DEFAULT_WEIGHTS
@@ -244,13 +313,13 @@ def main():
         w = Job(0.0, -1 - lane, seed=1, size=256, spp=1, denoise=True)
         ex.descs[w.jid] = ex.descs[jobs[0].jid]
         ex.run(w, lane)
-    sched = Scheduler(ex, int(args.budget_gb * (1 << 30)), args.lanes)
+    sched = Scheduler(ex, int(args.budget_gb * (1 << 30)), args.lanes, batch=args.batch)
     t0 = time.perf_counter()
     done = sched.run(jobs)
     wall = time.perf_counter() - t0
     res = summary(done, wall)
     offered = sum(j.size * j.size * j.spp for j in jobs) / max(jobs[-1].arrival, 1e-9)
-    res.update({"rate_per_s": args.rate, "lanes": args.lanes, "budget_gb": args.budget_gb,
+    res.update({"rate_per_s": args.rate, "lanes": args.lanes, "batch": args.batch, "budget_gb": args.budget_gb,
                 "peak_admitted_gb": round(sched.peak / (1 << 30), 2),
                 "offered_samples_per_s": round(offered / 1e6, 1), "offered_unit": "M samples/s"})
     print(json.dumps(res), flush=True)

@@ -412,6 +412,22 @@ cpt_status cpt_denoiser_wait_selftest(cpt_denoiser* d);
 cpt_status cpt_render(cpt_scene* scene, const cpt_render_params* params, const cpt_render_output* out,
                       void* stream, cpt_render_stats* stats);
 
+/* One render of a batch. */
+typedef struct cpt_render_job {
+    cpt_scene* scene;
+    cpt_render_params params; /* config estimator; integrator is ignored (the batch is a wavefront) */
+    cpt_render_output output;
+} cpt_render_job;
+
+/* No counterpart in the reference (its render kernel draws one image per launch, Render.cu:16).
+ * Renders several jobs — scenes of one context, any image sizes, sample counts, depth settings
+ * and seeds — in one wavefront: paths of all jobs share the path slots, queues and persistent
+ * kernels, so small jobs fill the GPU together.  Each job's outputs are exactly what cpt_render
+ * gives for it alone with the wavefront integrator.  All scenes must use the same BVH width.
+ * stats (optional) sums rays and paths over the jobs; ms is the batch's device time. */
+cpt_status cpt_render_batch(cpt_context* ctx, const cpt_render_job* jobs, uint32_t count, void* stream,
+                            cpt_render_stats* stats);
+
 #ifdef __cplusplus
 }
 #endif

@@ -392,3 +392,68 @@ def test_wavefront_material_sort_gives_the_same_image(ctx, name, width):
     assert np.array_equal(out[False][0], out[True][0])
     assert np.array_equal(out[False][1], out[True][1])
     assert out[False][2] == out[True][2]
+
+
+@pytest.mark.parametrize("width", [2, 8])
+@pytest.mark.parametrize("slots,sort", [(1 << 21, 0), (1024, 0), (1536, 1)])
+def test_render_batch_equals_single_renders(ctx, width, slots, sort):
+    """cpt_render_batch runs several jobs (four scenes, image sizes, spp, depths, seeds, a row band)
+    in one wavefront.  Paths of all jobs share the slots, but each pixel draws its own streams, so
+    every job's image, display bytes and G-buffer are bit for bit those of its own wavefront
+    render, and the batch traces the sum of their rays.  With fewer slots than items, slots move
+    between jobs as they finish."""
+    import torch
+    ctx.set_bvh_width(width)
+    try:
+        scs = [api.Scene(ctx, d).init() for d in (config_scene("cornell"), scenes.by_name("textured"),
+                                                   config_scene("spheres"), config_scene("volume_glass"))]
+    finally:
+        ctx.set_bvh_width(2)
+    prms = [dict(spp=6, max_depth=8, rr_depth=3, rr_prob=0.8, seed=5),
+            dict(spp=3, max_depth=5, rr_depth=2, rr_prob=0.7, seed=1),
+            dict(spp=9, max_depth=16, rr_depth=3, rr_prob=0.8, seed=11, rows=(10, 50)),
+            dict(spp=17, max_depth=12, rr_depth=4, rr_prob=0.9, seed=2)]
+
+    def outs(sc):
+        return (torch.zeros((sc.height, sc.width, 3), device="cuda"),
+                torch.zeros((sc.height, sc.width, 4), dtype=torch.uint8, device="cuda"),
+                torch.zeros((sc.height, sc.width, 8), device="cuda"))
+    ctx.set_wavefront(slots, 128, 128, 1)
+    ctx.set_material_sort(bool(sort))
+    try:
+        single, rays = [], 0
+        for sc, p in zip(scs, prms):
+            o = outs(sc)
+            r = sc.render(integrator=abi.INTEGRATOR_WAVEFRONT, estimator=abi.ESTIMATOR_CONFIG, rgb=o[0], rgba8=o[1],
+                          gbuffer=o[2], **p)
+            single.append(o)
+            rays += r["rays"]
+        bo = [outs(sc) for sc in scs]
+        jobs = [dict(scene=sc, rgb=o[0], rgba8=o[1], gbuffer=o[2], **p) for sc, o, p in zip(scs, bo, prms)]
+        b = api.render_batch(ctx, jobs)
+    finally:
+        ctx.set_wavefront(1 << 21, 128, 128, 1)
+        ctx.set_material_sort(False)
+    torch.cuda.synchronize()
+    for k, (a, o) in enumerate(zip(single, bo)):
+        for x, y in zip(a, o):
+            assert torch.equal(x, y), k
+    assert b["rays"] == rays
+    # host outputs through the same call
+    h = api.render_batch(ctx, [dict(scene=scs[0], **prms[0])])
+    assert np.array_equal(h["jobs"][0]["rgb"], single[0][0].cpu().numpy())
+
+
+def test_render_batch_arguments(ctx):
+    from cudapathtracing_gb300._lib import CptError
+    a = api.Scene(ctx, config_scene("cornell")).init()
+    ctx.set_bvh_width(8)
+    try:
+        b = api.Scene(ctx, config_scene("cornell")).init()
+    finally:
+        ctx.set_bvh_width(2)
+    with pytest.raises(CptError):   # different traversal layouts
+        api.render_batch(ctx, [dict(scene=a, spp=1), dict(scene=b, spp=1)])
+    with pytest.raises(CptError):   # bad row range
+        api.render_batch(ctx, [dict(scene=a, spp=1, rows=(5, 10 ** 6))])
+    assert api.render_batch(ctx, [])["rays"] == 0

@@ -37,6 +37,12 @@ class FakeExecutor:
                 self.active -= 1
 
 
+    def run_batch(self, jobs, lane):
+        with self.lock:
+            self.batches = getattr(self, "batches", []) + [[j.jid for j in jobs]]
+        return sum(self.run(j, lane) for j in jobs)
+
+
 def _jobs(n, size=256, spp=4):
     return [S.Job(arrival=0.001 * i, jid=i, seed=i, size=size, spp=spp, denoise=False) for i in range(n)]
 
@@ -90,3 +96,28 @@ def test_poisson_jobs_and_memory_estimate():
     assert 0.03 < sum(gaps) / len(gaps) < 0.07       # mean 1 / 20 s
     assert {j.size for j in jobs} <= set(S.RESOLUTIONS) and {j.spp for j in jobs} <= set(S.SPPS)
     assert S.job_bytes(2_000_000, 2048, 256) > S.job_bytes(50_000, 256, 1) > 0
+
+
+def test_batches_of_jobs_share_a_lane():
+    """With batch=3 a free lane takes up to three queued jobs that fit the budget together; the
+    batch's rays are counted once, FIFO order and the budget hold, and a failure or an
+    out-of-memory report applies to the whole batch."""
+    ex = FakeExecutor(lambda j: 20)
+    sch = S.Scheduler(ex, budget_bytes=100, lanes=2, batch=3)
+    done = sch.run(_jobs(11), realtime=False)
+    assert all(j.status == "done" for j in done)
+    assert ex.batches and all(2 <= len(b) <= 3 for b in ex.batches)
+    assert sum(len(b) for b in ex.batches) + sum(j.batch < 0 for j in done) == 11
+    assert sch.peak <= 100
+    assert all(b == list(range(b[0], b[0] + len(b))) for b in ex.batches)   # FIFO: consecutive arrivals
+    res = S.summary(done, 1.0)
+    assert res["rays"] == sum(1000 * (i + 1) for i in range(11))
+    assert res["batches"] == len(ex.batches)
+
+    ex = FakeExecutor(lambda j: 20, fail={4}, oom_once={1})
+    sch = S.Scheduler(ex, budget_bytes=100, lanes=1, batch=2)
+    done = sch.run(_jobs(6), realtime=False)
+    st = {j.jid: j.status for j in done}
+    partner = [b for b in ex.batches if 4 in b][0]
+    assert all(st[k] == "failed" for k in partner)          # the failing job's batch fails
+    assert st[1] == "done" and sch.in_use == 0               # the out-of-memory batch was retried
