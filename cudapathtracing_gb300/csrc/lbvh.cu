@@ -62,6 +62,60 @@ __device__ __forceinline__ void load_tri(const VT* __restrict__ v, uint32_t t, d
     for (int k = 0; k < 9; ++k) p[k] = (double)v[9ull * t + k];
 }
 
+// Constants of the fast Morton path for one axis: the reference's bounds and the scale
+// k = 1024 / (max - min) in FP64 and FP32.
+struct MortonAxis {
+    double mn, mx, k64;
+    float mn32, k32;
+};
+
+// Morton cell of a triangle-centroid coordinate, equal to the reference's exactly rounded FP64
+// sequence morton_axis(RN((p0 + p1 + p2) / 3), min, max) (BVH.cuh:23-33 on the centroid of
+// Hittable.cuh:459-461), computed without its two FP64 divisions where that is provably safe:
+//   1. FP32: x = (s * (1/3) - min) * k with s = p0 + p1 + p2.  Its distance to the reference's
+//      x is below tol = 2^-20 (k (|p0| + |p1| + |p2| + |min| + |x / k|) + |x|), four times the
+//      worst-case sum of the rounding errors (conversions, two additions, the multiplications
+//      and the rounded 1/3 and k, each at most 2^-24 relative).  The cell is floor(x) when x is
+//      farther than tol from every cell boundary (the integers 1 .. 1023; below 1 the cell is 0,
+//      at or above 1023 it is 1023).
+//   2. Otherwise the same in FP64 (s and min exact as in the reference, tol with 2^-48).
+//   3. Otherwise the reference's own sequence with IEEE divisions.
+// Non-finite intermediates (a degenerate axis) always take step 3.
+__device__ __forceinline__ int cell_of(float x, float tol)
+{
+    if (!(tol < 0.25f) || !isfinite(x)) return -1;
+    if (x < 1.0f - tol) return 0;
+    if (x > 1023.0f + tol) return 1023;
+    const float f = floorf(x);
+    return (x - f > tol && f + 1.0f - x > tol) ? (int)f : -1;
+}
+
+__device__ __forceinline__ int cell_of(double x, double tol)
+{
+    if (!(tol < 0.25) || !isfinite(x)) return -1;
+    if (x < 1.0 - tol) return 0;
+    if (x > 1023.0 + tol) return 1023;
+    const double f = floor(x);
+    return (x - f > tol && f + 1.0 - x > tol) ? (int)f : -1;
+}
+
+template <typename VT>
+__device__ __forceinline__ uint32_t morton_tri_axis(VT a, VT b, VT c, const MortonAxis& m)
+{
+    const float a32 = (float)a, b32 = (float)b, c32 = (float)c;
+    const float x32 = ((a32 + b32 + c32) * (1.0f / 3.0f) - m.mn32) * m.k32;
+    const float mag = fabsf(a32) + fabsf(b32) + fabsf(c32) + fabsf(m.mn32);
+    const float tol32 = 0x1p-20f * (m.k32 * mag + 2.0f * fabsf(x32));
+    int cell = cell_of(x32, tol32);
+    if (cell >= 0) return (uint32_t)cell;
+    const double s = __dadd_rn(__dadd_rn((double)a, (double)b), (double)c);   // the reference's sum
+    const double x64 = __dmul_rn(__dsub_rn(__dmul_rn(s, 1.0 / 3.0), m.mn), m.k64);
+    const double tol64 = 0x1p-48 * (m.k64 * (fabs(s) + fabs(m.mn)) + 2.0 * fabs(x64));
+    cell = cell_of(x64, tol64);
+    if (cell >= 0) return (uint32_t)cell;
+    return morton_axis(__ddiv_rn(s, 3.0), m.mn, m.mx);
+}
+
 // Triangle centroid and padded box (Hittable.cuh:459-461, AABB.cuh:30-40), boxes rounded
 // outwards to FP32.
 __device__ __forceinline__ void tri_center_box(const double p[9], double c[3], float4& bmin, float4& bmax)
@@ -77,31 +131,58 @@ __device__ __forceinline__ void tri_center_box(const double p[9], double c[3], f
     bmax = make_float4(__double2float_ru(mx[0]), __double2float_ru(mx[1]), __double2float_ru(mx[2]), 0.f);
 }
 
+// Padded triangle box (AABB::pad, AABB.cuh:30-40) rounded outwards to FP32.  For FP32 vertices
+// the minimum and maximum are exact in FP32; the padding is the reference's FP64 operation.
+__device__ __forceinline__ void tri_box(const float p[9], float4& bmin, float4& bmax)
+{
+    float mn[3], mx[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        mn[a] = fminf(fminf(p[a], p[3 + a]), p[6 + a]);
+        mx[a] = fmaxf(fmaxf(p[a], p[3 + a]), p[6 + a]);
+    }
+    bmin = make_float4(__double2float_rd(__dsub_rn((double)mn[0], 0.0001)),
+                       __double2float_rd(__dsub_rn((double)mn[1], 0.0001)),
+                       __double2float_rd(__dsub_rn((double)mn[2], 0.0001)), 0.f);
+    bmax = make_float4(__double2float_ru(__dadd_rn((double)mx[0], 0.0001)),
+                       __double2float_ru(__dadd_rn((double)mx[1], 0.0001)),
+                       __double2float_ru(__dadd_rn((double)mx[2], 0.0001)), 0.f);
+}
+
 template <typename VT>
 __global__ void k_prep(uint32_t n_extra, const double* __restrict__ extra_c, const float4* __restrict__ extra_box,
-                       uint32_t n_tri, const VT* __restrict__ tri_v, double3 smin, double3 smax,
+                       uint32_t n_tri, const VT* __restrict__ tri_v, MortonAxis ax, MortonAxis ay, MortonAxis az,
                        uint32_t* __restrict__ code, uint32_t* __restrict__ idx, float4* __restrict__ box)
 {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t n = n_extra + n_tri;
     if (i >= n) return;
-    double c[3];
     float4 bmin, bmax;
+    uint32_t xx, yy, zz;
     if (i < n_extra) {
-        c[0] = extra_c[3ull * i];
-        c[1] = extra_c[3ull * i + 1];
-        c[2] = extra_c[3ull * i + 2];
         bmin = extra_box[2ull * i];
         bmax = extra_box[2ull * i + 1];
+        xx = morton_axis(extra_c[3ull * i], ax.mn, ax.mx);
+        yy = morton_axis(extra_c[3ull * i + 1], ay.mn, ay.mx);
+        zz = morton_axis(extra_c[3ull * i + 2], az.mn, az.mx);
+    } else if (sizeof(VT) == sizeof(float)) {
+        const float* v = reinterpret_cast<const float*>(tri_v) + 9ull * (i - n_extra);
+        float p[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) p[k] = __ldg(v + k);
+        tri_box(p, bmin, bmax);
+        xx = morton_tri_axis(p[0], p[3], p[6], ax);
+        yy = morton_tri_axis(p[1], p[4], p[7], ay);
+        zz = morton_tri_axis(p[2], p[5], p[8], az);
     } else {
-        double p[9];
+        double p[9], c[3];
         load_tri(tri_v, i - n_extra, p);
         tri_center_box(p, c, bmin, bmax);
+        xx = morton_axis(c[0], ax.mn, ax.mx);
+        yy = morton_axis(c[1], ay.mn, ay.mx);
+        zz = morton_axis(c[2], az.mn, az.mx);
     }
-    uint32_t xx = expand_bits(morton_axis(c[0], smin.x, smax.x));
-    uint32_t yy = expand_bits(morton_axis(c[1], smin.y, smax.y));
-    uint32_t zz = expand_bits(morton_axis(c[2], smin.z, smax.z));
-    code[i] = xx * 4 + yy * 2 + zz;
+    code[i] = expand_bits(xx) * 4 + expand_bits(yy) * 2 + expand_bits(zz);
     idx[i] = i;
     box[2ull * i] = bmin;
     box[2ull * i + 1] = bmax;
@@ -119,6 +200,12 @@ __global__ void k_prim_boxes(uint32_t n_extra, const float4* __restrict__ extra_
     if (i < n_extra) {
         bmin = extra_box[2ull * i];
         bmax = extra_box[2ull * i + 1];
+    } else if (sizeof(VT) == sizeof(float)) {
+        const float* v = reinterpret_cast<const float*>(tri_v) + 9ull * (i - n_extra);
+        float p[9];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) p[q] = __ldg(v + q);
+        tri_box(p, bmin, bmax);
     } else {
         double p[9], c[3];
         load_tri(tri_v, i - n_extra, p);
@@ -598,12 +685,22 @@ cpt_status lbvh_build(uint32_t n_extra, const double* extra_centroid, const floa
     if (timings)
         for (auto& e : ev) CPT_CUDA(cudaEventCreate(&e));
     if (timings) CPT_CUDA(cudaEventRecord(ev[0], stream));
+    auto axis = [](double mn, double mx) {
+        MortonAxis m;
+        m.mn = mn;
+        m.mx = mx;
+        m.k64 = 1024.0 / (mx - mn);
+        m.mn32 = (float)mn;
+        m.k32 = (float)m.k64;
+        return m;
+    };
+    const MortonAxis ax = axis(smin.x, smax.x), ay = axis(smin.y, smax.y), az = axis(smin.z, smax.z);
     if (tri_f64)
-        k_prep<double><<<blocks_for(n, 256), 256, 0, stream>>>(n_extra, extra_centroid, extra_box, n_tri, tri_f64, smin,
-                                                               smax, code0, val0, box_unsorted);
+        k_prep<double><<<blocks_for(n, 256), 256, 0, stream>>>(n_extra, extra_centroid, extra_box, n_tri, tri_f64, ax,
+                                                               ay, az, code0, val0, box_unsorted);
     else
-        k_prep<float><<<blocks_for(n, 256), 256, 0, stream>>>(n_extra, extra_centroid, extra_box, n_tri, tri_f32, smin,
-                                                              smax, code0, val0, box_unsorted);
+        k_prep<float><<<blocks_for(n, 256), 256, 0, stream>>>(n_extra, extra_centroid, extra_box, n_tri, tri_f32, ax,
+                                                              ay, az, code0, val0, box_unsorted);
     CPT_CUDA(cudaGetLastError());
     add_launches(1);
     if (timings) CPT_CUDA(cudaEventRecord(ev[1], stream));

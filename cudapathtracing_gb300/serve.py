@@ -55,14 +55,15 @@ class Job:
     error: str = field(compare=False, default="")
 
 
-def poisson_jobs(n: int, rate: float = 20.0, seed: int = 3, denoise_frac: float = 0.5, max_level: int = 6):
+def poisson_jobs(n: int, rate: float = 20.0, seed: int = 3, denoise_frac: float = 0.5, max_level: int = 6,
+                 sizes=RESOLUTIONS, spps=SPPS):
     """n jobs drawn from numpy's generator seeded by `seed`: exponential inter-arrival times with
-    the given rate, resolution uniform over RESOLUTIONS (square), spp uniform over SPPS, and the
+    the given rate, resolution uniform over `sizes` (square), spp uniform over `spps`, and the
     denoiser on with odds denoise_frac."""
     rng = np.random.default_rng(seed)
     t = np.cumsum(rng.exponential(1.0 / rate, size=n))
-    return [Job(arrival=float(t[i]), jid=i, seed=int(3_000_000 + i), size=int(rng.choice(RESOLUTIONS)),
-                spp=int(rng.choice(SPPS)), denoise=bool(rng.uniform() < denoise_frac), max_level=max_level)
+    return [Job(arrival=float(t[i]), jid=i, seed=int(3_000_000 + i), size=int(rng.choice(sizes)),
+                spp=int(rng.choice(spps)), denoise=bool(rng.uniform() < denoise_frac), max_level=max_level)
             for i in range(n)]
 
 
@@ -84,11 +85,16 @@ class Scheduler:
     the jobs back at the head of the queue until other jobs free memory (or fails them when
     nothing else is running); any other exception fails every job of the batch."""
 
-    def __init__(self, executor, budget_bytes: int, lanes: int = 2, clock=time.perf_counter, batch: int = 1):
+    def __init__(self, executor, budget_bytes: int, lanes: int = 2, clock=time.perf_counter, batch: int = 1,
+                 batch_samples: int | None = None):
         self.ex = executor
         self.budget = budget_bytes
         self.lanes = lanes
         self.batch = max(1, int(batch))
+        # a batch grows while its jobs' samples (pixels x spp) stay within batch_samples, so small
+        # jobs are batched together and a large one (which fills the GPU alone) is not joined by
+        # small ones that would then wait for it
+        self.batch_samples = batch_samples
         self.clock = clock
         self.in_use = 0
         self.peak = 0
@@ -162,8 +168,12 @@ class Scheduler:
                         heapq.heappush(queue, job)
                 while queue and self.free_lanes:
                     batch = []
+                    work = 0
                     while queue and len(batch) < self.batch:
                         job = queue[0]
+                        w = job.size * job.size * job.spp
+                        if batch and self.batch_samples is not None and work + w > self.batch_samples:
+                            break
                         if not self._admit(job, need_lane=not batch):
                             break
                         heapq.heappop(queue)
@@ -172,6 +182,7 @@ class Scheduler:
                             done.append(job)
                             continue
                         batch.append(job)
+                        work += w
                     if not batch:
                         break
                     lane = self.free_lanes.pop(0)
@@ -302,10 +313,16 @@ def main():
     ap.add_argument("--max-level", type=int, default=6)
     ap.add_argument("--seed", type=int, default=3)
     ap.add_argument("--batch", type=int, default=1, help="jobs per wavefront (cross-job batching)")
+    ap.add_argument("--batch-samples", type=float, default=16.0,
+                    help="a batch grows while its samples (pixels x spp) stay within this many million")
+    ap.add_argument("--sizes", default="256,512,1024,2048", help="job resolutions (square)")
+    ap.add_argument("--spps", default="1,4,16,64,256", help="job sample counts")
     args = ap.parse_args()
     import json
     from .training import DEFAULT_WEIGHTS
-    jobs = poisson_jobs(args.jobs, args.rate, args.seed, max_level=args.max_level)
+    jobs = poisson_jobs(args.jobs, args.rate, args.seed, max_level=args.max_level,
+                        sizes=tuple(int(x) for x in args.sizes.split(",")),
+                        spps=tuple(int(x) for x in args.spps.split(",")))
     ex = GpuExecutor(args.lanes, weights=DEFAULT_WEIGHTS)
     ex.prepare(jobs)
     # warm-up: one small job per lane (graph capture, denoiser allocation)
@@ -313,13 +330,16 @@ def main():
         w = Job(0.0, -1 - lane, seed=1, size=256, spp=1, denoise=True)
         ex.descs[w.jid] = ex.descs[jobs[0].jid]
         ex.run(w, lane)
-    sched = Scheduler(ex, int(args.budget_gb * (1 << 30)), args.lanes, batch=args.batch)
+    sched = Scheduler(ex, int(args.budget_gb * (1 << 30)), args.lanes, batch=args.batch,
+                      batch_samples=int(args.batch_samples * 1e6))
     t0 = time.perf_counter()
     done = sched.run(jobs)
     wall = time.perf_counter() - t0
     res = summary(done, wall)
     offered = sum(j.size * j.size * j.spp for j in jobs) / max(jobs[-1].arrival, 1e-9)
-    res.update({"rate_per_s": args.rate, "lanes": args.lanes, "batch": args.batch, "budget_gb": args.budget_gb,
+    res.update({"rate_per_s": args.rate, "lanes": args.lanes, "batch": args.batch,
+                "batch_msamples": args.batch_samples, "sizes": args.sizes, "spps": args.spps,
+                "budget_gb": args.budget_gb,
                 "peak_admitted_gb": round(sched.peak / (1 << 30), 2),
                 "offered_samples_per_s": round(offered / 1e6, 1), "offered_unit": "M samples/s"})
     print(json.dumps(res), flush=True)

@@ -121,3 +121,15 @@ def test_batches_of_jobs_share_a_lane():
     partner = [b for b in ex.batches if 4 in b][0]
     assert all(st[k] == "failed" for k in partner)          # the failing job's batch fails
     assert st[1] == "done" and sch.in_use == 0               # the out-of-memory batch was retried
+
+
+def test_batch_sample_cap_keeps_large_jobs_alone():
+    ex = FakeExecutor(lambda j: 10)
+    jobs = [S.Job(arrival=0.0, jid=i, seed=i, size=(2048 if i in (2, 5) else 256), spp=4, denoise=False)
+            for i in range(8)]
+    sch = S.Scheduler(ex, budget_bytes=1000, lanes=1, batch=4, batch_samples=4 * 256 * 256 * 4)
+    done = sch.run(jobs, realtime=False)
+    assert all(j.status == "done" for j in done)
+    by = {j.jid: j.batch for j in done}
+    assert by[2] == -1 and by[5] == -1                    # over the cap: rendered alone
+    assert all(len(b) <= 4 and 2 not in b and 5 not in b for b in ex.batches)
