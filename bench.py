@@ -184,26 +184,68 @@ def run_reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
-def denoise_eval(ctx, scenes=(0, 1, 2), size=512):
-    """Held-out seeded scenes at size x size: the smallest spp (of a fixed ladder) at which the
-    plain render, and the denoised render, reach display-space RMSE 0.01 against an 8192-spp
-    render of another seed, and their device times (render, plus denoiser)."""
+def denoise_eval(ctx, scenes=tuple(range(8)), size=512, ref_spp=16384):
+    """Held-out seeded scenes at size x size: the smallest spp (of a geometric ladder, ratio
+    2^(1/4)) at which the plain render, and the denoised render, reach display-space RMSE 0.01
+    against a ref_spp render of another seed, and their device times (render, plus denoiser)."""
     from cudapathtracing_gb300 import procedural as P, training as T
     from cudapathtracing_gb300.denoiser import Denoiser
     net = Denoiser()
     net.load(T.DEFAULT_WEIGHTS)
     out = []
     for k in scenes:
-        r = T.evaluate(ctx, net, P.random_scene(T.EVAL_SEED0 + k, width=size))
+        r = T.evaluate(ctx, net, P.random_scene(T.EVAL_SEED0 + k, width=size), ref_spp=ref_spp)
         best_bil = min(row["bilateral"] for row in r["rows"])
-        out.append({"scene_seed": T.EVAL_SEED0 + k, "plain_spp": r["plain_spp"], "plain_ms": r["plain_ms"],
-                    "denoised_spp": r["denoised_spp"], "denoised_ms": r["denoised_ms"],
+        out.append({"scene_seed": T.EVAL_SEED0 + k, "plain_spp": r["plain_spp"],
+                    "plain_ms": None if r["plain_ms"] is None else round(r["plain_ms"], 2),
+                    "denoised_spp": r["denoised_spp"],
+                    "denoised_ms": None if r["denoised_ms"] is None else round(r["denoised_ms"], 2),
                     "speedup": None if r["speedup"] is None else round(r["speedup"], 2),
                     "bilateral_best_rmse": round(best_bil, 4)})
     sp = [o["speedup"] for o in out if o["speedup"]]
-    return {"target_rmse": 0.01, "size": f"{size}x{size}", "reference_spp": 8192,
+    full = len(sp) == len(out)
+    return {"target_rmse": 0.01, "size": f"{size}x{size}", "reference_spp": ref_spp,
             "space": "sqrt-gamma display values clamped to [0,1]", "scenes": out,
-            "speedup_geomean": round(float(np.exp(np.mean(np.log(sp)))), 2) if len(sp) == len(out) else None}
+            "speedup_min": round(min(sp), 2) if full else None,
+            "speedup_geomean": round(float(np.exp(np.mean(np.log(sp)))), 2) if full else None,
+            "scenes_at_8x": sum(1 for x in sp if x >= 8.0)}
+
+
+def microbench_c2(ctx, steps: int = 5) -> dict:
+    """The LBVH build + traversal microbench (1,310,720-triangle displaced icosphere, 10M random
+    closest-hit rays): build ms (median over the steps, with its stage split) and Mrays/s of the
+    trace, for both traversal layouts.  Inputs are resident; CUDA events on the stream."""
+    import torch
+    from cudapathtracing_gb300 import api, procedural as P
+    d = P.icosphere_scene(level=8)
+    n = 10_000_000
+    rays = torch.from_numpy(P.uniform_rays(n, seed=1).view(np.float32).reshape(n, 8)).cuda()
+    hits = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    out = {"triangles": d.num_triangles, "rays": n}
+    for width in (2, 8):
+        ctx.set_bvh_width(width)
+        sc = api.Scene(ctx, d)
+        builds, trace = [], []
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        for i in range(steps + 2):
+            st = sc.buildBVH(stream.cuda_stream)
+            e0.record(stream)
+            sc.trace(rays, hits, stream=stream.cuda_stream)
+            e1.record(stream)
+            e1.synchronize()
+            if i >= 2:
+                builds.append([st.ms_prep, st.ms_sort, st.ms_emit, st.ms_refit, st.ms_collapse, st.ms_total])
+                trace.append(e0.elapsed_time(e1))
+        b = np.median(np.array(builds), 0)
+        out[f"bvh{width}"] = {"build_ms": round(float(b[5]), 3),
+                              "build_split_ms": {k: round(float(v), 3) for k, v in
+                                                 zip(("prep", "sort", "emit", "refit", "layout"), b[:5])},
+                              "trace_ms": round(float(np.median(trace)), 3),
+                              "mrays_per_s": round(n / (float(np.median(trace)) / 1e3) / 1e6, 1)}
+        sc.close()
+    ctx.set_bvh_width(2)
+    return out
 
 
 def main():
@@ -217,6 +259,7 @@ def main():
     ap.add_argument("--no-compare", action="store_true",
                     help="skip timing the megakernel beside the wavefront integrator")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-microbench", action="store_true", help="skip the 1.31M-triangle build + 10M-ray microbench")
     ap.add_argument("--spp", type=int, default=0, help="override the workload's spp (profiling captures)")
     ap.add_argument("--e2e-steps", type=int, default=2, help="steps of the end-to-end leg (0: skip)")
     ap.add_argument("--bvh-width", type=int, default=2, choices=[2, 8], help="traversal layout")
@@ -407,6 +450,13 @@ def main():
         except Exception as e:  # reported, never required
             denoise = {"error": str(e)}
 
+    micro = None
+    if not trace_only and not args.no_microbench:
+        try:
+            micro = microbench_c2(ctx)
+        except Exception as e:  # reported, never required
+            micro = {"error": str(e)}
+
     cpu = None
     if not args.no_cpu_baseline:
         try:
@@ -440,6 +490,7 @@ def main():
                      "kernel_ms": round(k_ms, 3), "bytes_per_ray": round(bpr, 1), "peak_source": peak_src},
         "cpu_baseline": cpu,
         "megakernel_same_run": compare,
+        "lbvh_traversal_microbench": micro,
         "denoise": denoise,
         "clocks": clk.summary(),
         "gpu_launches": int(launches),

@@ -178,6 +178,13 @@ inline constexpr size_t short_stack_bytes(int threads, int entries = CPT_SHORT_S
     return (size_t)entries * threads * sizeof(int);
 }
 
+// The 8-wide traversal's short stack: 64-bit group entries.
+#define CPT_WIDE_SHORT_STACK 8
+inline constexpr size_t wide_short_stack_bytes(int threads, int entries = CPT_WIDE_SHORT_STACK)
+{
+    return (size_t)entries * threads * sizeof(uint64_t);
+}
+
 #ifdef __CUDACC__
 template <int SHORT>
 struct ShortStackN {

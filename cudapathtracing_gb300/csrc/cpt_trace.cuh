@@ -142,21 +142,40 @@ __device__ __forceinline__ uint32_t word_of(const float4& f, int w)
 // positions slot ^ (7 ^ octant), which orders them roughly front to back for this ray (the slots
 // were assigned by direction at build time).  Leaf children are tested at once, nearest bit
 // first (the reference tests leaves as it reaches them); the traversal continues with the first
-// internal child and keeps the rest as one node-group entry (first child index, internal-slot
-// mask, remaining hit bits) on the stack, as in compressed wide BVH traversal (Ylitie et al.
-// 2017).  Boxes are tested against the closest hit so far, so far subtrees are culled.  With ANY
-// the walk is an occlusion query (visit_leaf) that stops at the first occluder.
-template <bool ANY>
-__device__ __forceinline__ bool trace_closest_wide(const SceneView& s, float3 o, float3 d, float tmin, float tmax,
-                                                   Hit& hit, int* err, int skip)
-{
-    const float3 idir = safe_inverse(d);
-    const uint32_t first = 7u ^ ((d.x < 0.f ? 1u : 0u) | (d.y < 0.f ? 2u : 0u) | (d.z < 0.f ? 4u : 0u));
-    float best = tmax;
-    uint64_t stack[CPT_WSTACK];
-    int sp = 0;
-    uint32_t node = 0;
-    for (;;) {
+// internal child and keeps the rest as one node-group entry (node, remaining hit bits) on the
+// stack, as in compressed wide BVH traversal (Ylitie et al. 2017); a popped group yields its next
+// child from the node's child list.  Boxes are tested against the closest hit so far, so far
+// subtrees are culled.  With ANY the walk is an occlusion query (visit_leaf) that stops at the
+// first occluder.  The walk advances one node per step() so that a warp can refill finished lanes
+// (dynamic fetching); Stack64 keeps group entries (in shared and local memory, or local only).
+template <bool ANY, typename Stack64>
+struct WideWalk {
+    float3 o, d, idir;
+    float tmin, best;
+    uint32_t first, node;
+    int sp, skip;
+    Hit hit;
+    Stack64 stack;
+
+    __device__ __forceinline__ void start(float3 o_, float3 d_, float tmin_, float tmax_, int skip_)
+    {
+        o = o_;
+        d = d_;
+        idir = safe_inverse(d_);
+        first = 7u ^ ((d.x < 0.f ? 1u : 0u) | (d.y < 0.f ? 2u : 0u) | (d.z < 0.f ? 4u : 0u));
+        tmin = tmin_;
+        best = tmax_;
+        node = 0;
+        sp = 0;
+        skip = skip_;
+        hit.leaf = -1;
+        hit.t = tmax_;
+        hit.u = hit.v = 0.f;
+    }
+
+    // Visits one node; returns true when the traversal has finished.
+    __device__ __forceinline__ bool step(const SceneView& s, int* err)
+    {
         const float4* np = s.wide + CPT_WIDE_F4 * (size_t)node;
         const float4 f0 = ldg4(np), f1 = ldg4(np + 1), f2 = ldg4(np + 2);
         const float4 qx = ldg4(np + 3), qy = ldg4(np + 4), qz = ldg4(np + 5);
@@ -193,7 +212,6 @@ __device__ __forceinline__ bool trace_closest_wide(const SceneView& s, float3 o,
         }
         // Continue with the first hit internal child; the others stay on the stack as one group
         // (this node, remaining hit bits) and are read back from the node when popped.
-        bool have_next = false;
         if (ihits) {
             const uint32_t slot = (uint32_t)(__ffs(ihits) - 1) ^ first;
             const uint32_t rest = ihits & (ihits - 1);
@@ -202,23 +220,63 @@ __device__ __forceinline__ bool trace_closest_wide(const SceneView& s, float3 o,
             if (rest) {
                 if (sp >= CPT_WSTACK) {
                     if (err) atomicOr(err, CPT_DEVERR_STACK);
-                    return hit.leaf >= 0;
+                    return true;
                 }
-                stack[sp++] = (uint64_t)cur | ((uint64_t)rest << 32);
+                stack.put(sp++, (uint64_t)cur | ((uint64_t)rest << 32));
             }
-            have_next = true;
-        } else if (sp > 0) {
-            const uint64_t g = stack[--sp];
-            const uint32_t gnode = (uint32_t)g;
-            const uint32_t hits = (uint32_t)(g >> 32);
-            const uint32_t slot = (uint32_t)(__ffs(hits) - 1) ^ first;
-            const uint32_t rest = hits & (hits - 1);
-            if (rest) stack[sp++] = (uint64_t)gnode | ((uint64_t)rest << 32);
-            node = (uint32_t)__ldg(reinterpret_cast<const int*>(s.wide + CPT_WIDE_F4 * (size_t)gnode + 1) + slot);
-            have_next = true;
+            return false;
         }
-        if (!have_next) break;
+        if (sp == 0) return true;
+        const uint64_t g = stack.get(--sp);
+        const uint32_t gnode = (uint32_t)g;
+        const uint32_t hits = (uint32_t)(g >> 32);
+        const uint32_t slot = (uint32_t)(__ffs(hits) - 1) ^ first;
+        const uint32_t rest = hits & (hits - 1);
+        if (rest) stack.put(sp++, (uint64_t)gnode | ((uint64_t)rest << 32));
+        node = (uint32_t)__ldg(reinterpret_cast<const int*>(s.wide + CPT_WIDE_F4 * (size_t)gnode + 1) + slot);
+        return false;
     }
+};
+
+// Group-entry stacks of the wide traversal: the whole stack in local memory, or the bottom SHORT
+// entries in the block's dynamic shared memory (wide_short_stack_bytes) and the rest in local
+// memory; thread t owns the column t, t + T, ... of 64-bit words.
+struct LocalStack64 {
+    uint64_t s[CPT_WSTACK];
+    __device__ __forceinline__ void init() {}
+    __device__ __forceinline__ void put(int i, uint64_t v) { s[i] = v; }
+    __device__ __forceinline__ uint64_t get(int i) const { return s[i]; }
+};
+
+template <int SHORT>
+struct ShortStack64 {
+    uint64_t* col;
+    int stride;
+    uint64_t spill[CPT_WSTACK - SHORT];
+    __device__ __forceinline__ void init()
+    {
+        extern __shared__ int cpt_short_stack_smem[];
+        const int t = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+        col = reinterpret_cast<uint64_t*>(cpt_short_stack_smem) + t;
+        stride = blockDim.x * blockDim.y * blockDim.z;
+    }
+    __device__ __forceinline__ void put(int i, uint64_t v)
+    {
+        if (i < SHORT) col[i * stride] = v;
+        else spill[i - SHORT] = v;
+    }
+    __device__ __forceinline__ uint64_t get(int i) const { return i < SHORT ? col[i * stride] : spill[i - SHORT]; }
+};
+
+template <bool ANY>
+__device__ __forceinline__ bool trace_closest_wide(const SceneView& s, float3 o, float3 d, float tmin, float tmax,
+                                                   Hit& hit, int* err, int skip)
+{
+    WideWalk<ANY, LocalStack64> w;
+    w.stack.init();
+    w.start(o, d, tmin, tmax, skip);
+    while (!w.step(s, err)) {}
+    hit = w.hit;
     return hit.leaf >= 0;
 }
 
@@ -360,12 +418,12 @@ __device__ __forceinline__ uint32_t lane_mask_lt()
 // traced by the lane.
 constexpr int CPT_REFILL = 8;
 
-template <bool ANY, typename Stack, typename Views, typename Load, typename Store>
-__device__ __forceinline__ uint32_t trace_items_bvh2_views(const Views& views, int n, int* fetch, int* err, Load load,
-                                                           Store store)
+template <typename Walk, typename Views, typename Load, typename Store>
+__device__ __forceinline__ uint32_t trace_items_walk(const Views& views, int n, int* fetch, int* err, Load load,
+                                                     Store store)
 {
     const int lane = threadIdx.x & 31;
-    Bvh2Walk<ANY, Stack> w;
+    Walk w;
     w.stack.init();
     int item = -1, scene = 0;
     bool exhausted = false;
@@ -400,6 +458,21 @@ __device__ __forceinline__ uint32_t trace_items_bvh2_views(const Views& views, i
         }
     }
     return rays;
+}
+
+template <bool ANY, typename Stack, typename Views, typename Load, typename Store>
+__device__ __forceinline__ uint32_t trace_items_bvh2_views(const Views& views, int n, int* fetch, int* err, Load load,
+                                                           Store store)
+{
+    return trace_items_walk<Bvh2Walk<ANY, Stack>>(views, n, fetch, err, load, store);
+}
+
+// Dynamic fetching over the 8-wide BVH (the same refill policy).
+template <bool ANY, typename Stack64, typename Views, typename Load, typename Store>
+__device__ __forceinline__ uint32_t trace_items_wide_views(const Views& views, int n, int* fetch, int* err, Load load,
+                                                           Store store)
+{
+    return trace_items_walk<WideWalk<ANY, Stack64>>(views, n, fetch, err, load, store);
 }
 
 // The same over one scene.

@@ -41,6 +41,25 @@ __global__ void __launch_bounds__(128) k_trace_dyn(SceneView s, const float4* __
         });
 }
 
+// The same over the 8-wide BVH, with the group-entry stack's bottom entries in shared memory.
+__global__ void __launch_bounds__(128) k_trace_dyn_wide(SceneView s, const float4* __restrict__ rays, int n,
+                                                        float4* __restrict__ hits, int* err, int* fetch)
+{
+    trace_items_wide_views<false, ShortStack64<CPT_WIDE_SHORT_STACK>>(
+        [&](int) -> const SceneView& { return s; }, n, fetch, err,
+        [&](int i, float3& o, float3& d, float& tmn, float& tmx, int&, int&) {
+            float4 a = __ldg(rays + 2 * (size_t)i), b = __ldg(rays + 2 * (size_t)i + 1);
+            o = f3(a.x, a.y, a.z);
+            d = f3(b.x, b.y, b.z);
+            tmn = a.w;
+            tmx = b.w;
+        },
+        [&](int i, const Hit& h, int) {
+            int prim = h.leaf >= 0 ? __float_as_int(ldg4(s.leaf_rec + 3 * (size_t)h.leaf).w) : -1;
+            hits[i] = make_float4(h.leaf >= 0 ? h.t : -1.0f, __int_as_float(prim), h.u, h.v);
+        });
+}
+
 }  // namespace
 
 cpt_status launch_trace(const SceneView& view, const cpt_ray* rays, uint64_t n, cpt_hit* hits, int* d_err,
@@ -62,6 +81,16 @@ cpt_status launch_trace(const SceneView& view, const cpt_ray* rays, uint64_t n, 
         CPT_CUDA(cudaMemsetAsync(fetch, 0, sizeof(int), stream));
         k_trace_dyn<<<std::max(1, per_sm) * sms, T, smem, stream>>>(view, (const float4*)rays, (int)n, (float4*)hits,
                                                                     d_err, fetch);
+    } else if (view.wide && view.n_internal > 0 && n < 0x7fffffffull) {
+        const size_t wsmem = wide_short_stack_bytes(T);
+        int dev = 0, sms = 0, per_sm = 0;
+        CPT_CUDA(cudaGetDevice(&dev));
+        CPT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        CPT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_dyn_wide, T, wsmem));
+        int* fetch = d_err + 1;
+        CPT_CUDA(cudaMemsetAsync(fetch, 0, sizeof(int), stream));
+        k_trace_dyn_wide<<<std::max(1, per_sm) * sms, T, wsmem, stream>>>(view, (const float4*)rays, (int)n,
+                                                                          (float4*)hits, d_err, fetch);
     } else if (view.wide)
         k_trace<true><<<(unsigned)blocks, T, smem, stream>>>(view, (const float4*)rays, n, (float4*)hits, d_err);
     else

@@ -1,8 +1,11 @@
 // wide.cu — collapses the binary LBVH into a compressed 8-wide BVH for traversal.
 //
-// Each wide node stands for one binary node b and is stored at index b, so wide nodes keep the
-// Morton order of the Karras tree (a subtree's nodes sit close together in memory), the layout
-// is deterministic, and leaves stay in sorted Morton order.  Starting from b's two children,
+// The collapse runs level by level from the root.  Wide nodes are numbered compactly in that
+// breadth-first order: level l occupies [base_l, base_l + n_l), and the internal children of a node
+// are numbered consecutively (one atomic per node reserves their block in the next level), so the
+// reachable nodes fill [0, num_wide) with siblings side by side and the top levels packed together
+// (the hot part of the tree stays within a few megabytes).  Leaves stay in sorted Morton order in the
+// leaf records.  Each wide node stands for one binary node b; starting from b's two children,
 // the child with the largest surface area that is an internal binary node is replaced by its two
 // children until there are 8 children or only leaves remain.  Children are then placed in slots
 // by direction: slot s (bits: negative x, y, z) holds the child whose centroid offset from the
@@ -67,14 +70,18 @@ __device__ __forceinline__ uint32_t q_hi(float v, float p, float inv_scale)
 
 __device__ __forceinline__ float inv_grid(uint32_t e) { return __int_as_float((int)((254u - e) << 23)); }
 
+// One level: task t is binary node tasks_in[t], whose wide node is number base + t (base = the
+// nodes of the finished levels).  Internal children are queued for the next level, whose nodes
+// start at base + n.
 __global__ void k_collapse_level(const int2* __restrict__ child, const float4* __restrict__ node_box,
                                  const float4* __restrict__ leaf_box, const int* __restrict__ tasks_in,
-                                 const int* __restrict__ n_in, int* __restrict__ tasks_out, int* __restrict__ n_out,
-                                 float4* __restrict__ wide)
+                                 const int* __restrict__ n_in, const int* __restrict__ done_levels,
+                                 int* __restrict__ tasks_out, int* __restrict__ n_out, float4* __restrict__ wide)
 {
     const int n = *n_in;
+    const int base = *done_levels;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-        const int b = tasks_in[t];   // binary node; its wide node has the same index
+        const int b = tasks_in[t];   // binary node
         int refs[8];
         int2 c = child[b];
         refs[0] = c.x;
@@ -134,6 +141,11 @@ __global__ void k_collapse_level(const int2* __restrict__ child, const float4* _
         int at_slot[8];
         for (int s = 0; s < 8; ++s) at_slot[s] = CPT_WIDE_EMPTY;
         for (int k = 0; k < nr; ++k) at_slot[slot_of[k]] = refs[k];
+        // the internal children's block in the next level, in slot order
+        int n_int = 0;
+        for (int s = 0; s < 8; ++s) n_int += (at_slot[s] != CPT_WIDE_EMPTY && at_slot[s] >= 0) ? 1 : 0;
+        const int first_child = n_int ? atomicAdd(n_out, n_int) : 0;
+        int next_child = first_child;
         uint32_t ex = grid_exponent(nmn.x, nmx.x), ey = grid_exponent(nmn.y, nmx.y), ez = grid_exponent(nmn.z, nmx.z);
         float isx = inv_grid(ex), isy = inv_grid(ey), isz = inv_grid(ez);
         uint32_t q[6][2];
@@ -146,7 +158,9 @@ __global__ void k_collapse_level(const int2* __restrict__ child, const float4* _
             ref_box(ref, node_box, leaf_box, mn, mx);
             if (ref >= 0) {
                 imask |= 1u << s;
-                tasks_out[atomicAdd(n_out, 1)] = ref;
+                tasks_out[next_child] = ref;
+                at_slot[s] = base + n + next_child;   // the child's wide node number
+                ++next_child;
             }
             int qw = s >> 2, qs = (s & 3) * 8;
             q[0][qw] |= q_lo(mn.x, nmn.x, isx) << qs;
@@ -156,7 +170,7 @@ __global__ void k_collapse_level(const int2* __restrict__ child, const float4* _
             q[4][qw] |= q_lo(mn.z, nmn.z, isz) << qs;
             q[5][qw] |= q_hi(mx.z, nmn.z, isz) << qs;
         }
-        float4* dst = wide + CPT_WIDE_F4 * (size_t)b;
+        float4* dst = wide + CPT_WIDE_F4 * (size_t)(base + t);
         dst[0] = make_float4(nmn.x, nmn.y, nmn.z, __int_as_float((int)(ex | (ey << 8) | (ez << 16) | (imask << 24))));
         dst[1] = make_float4(__int_as_float(at_slot[0]), __int_as_float(at_slot[1]), __int_as_float(at_slot[2]),
                              __int_as_float(at_slot[3]));
@@ -170,7 +184,7 @@ __global__ void k_collapse_level(const int2* __restrict__ child, const float4* _
 
 __global__ void k_collapse_init(int* tasks, int* n_tasks)
 {
-    tasks[0] = 0;   // the binary root is wide node 0
+    tasks[0] = 0;   // the binary root is task 0 of level 0: wide node 0
     n_tasks[0] = 1;
     n_tasks[1] = 0;
     n_tasks[2] = 0;   // wide nodes written by finished levels
@@ -215,7 +229,7 @@ cpt_status build_wide(uint32_t n, const int2* child, const float4* node_box, con
     for (int level = 0; level < 72; ++level) {
         k_next_level<<<1, 1, 0, stream>>>(n_tasks + (cur ^ 1), n_tasks + 2);
         k_collapse_level<<<std::max(1u, std::min((n + 255) / 256, 4096u)), 256, 0, stream>>>(
-            child, node_box, leaf_box, tasks[cur], n_tasks + cur, tasks[cur ^ 1], n_tasks + (cur ^ 1), wide);
+            child, node_box, leaf_box, tasks[cur], n_tasks + cur, n_tasks + 2, tasks[cur ^ 1], n_tasks + (cur ^ 1), wide);
         add_launches(2);
         cur ^= 1;
         if ((level & 7) == 7) {

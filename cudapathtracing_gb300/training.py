@@ -88,21 +88,27 @@ def train(net: Denoiser, data, steps: int, batch: int = 8, lr: float = 1e-3, lr_
     return hist
 
 
-LADDER = (1, 2, 3, 4, 6, 8, 12, 16, 24, 32, 48, 64, 96, 128, 192, 256, 384, 512, 768, 1024, 1536, 2048)
+# spp ladder of the wall-time-to-RMSE comparison: geometric, ratio 2^(1/4) (about 1.19), so the
+# spp at which a method first reaches the target is resolved to within 19 %.
+LADDER = tuple(sorted({max(1, int(round(2 ** (k / 4)))) for k in range(0, 45)}))
 
 
-def evaluate(ctx, net: Denoiser, desc, ref_spp: int = 8192, plain_spps=LADDER,
+def evaluate(ctx, net: Denoiser, desc, ref_spp: int = 16384, plain_spps=LADDER,
              denoise_spps=tuple(x for x in LADDER if x <= 512), target_rmse: float = 0.01, seed: int = 17):
     """RMSE and wall time of plain, bilateral-filtered and denoised renders against a high-spp
     reference (another seed), and the time each needs to reach target_rmse (None if it does not):
-    the smallest spp of a geometric ladder (ratio ~1.5) at which it does.
-    Times are device milliseconds of the render (and of the filter / denoiser) at that spp."""
+    the smallest spp of the geometric ladder at which it does.  The ladder stops once both the
+    plain and the denoised render have reached the target.  Times are device milliseconds of the
+    render (and of the filter / denoiser) at that spp."""
     import torch
     sc = api.Scene(ctx, desc).init()
     ref, _, ref_ms = render(ctx, sc, ref_spp, seed=seed + 1, gbuf=False)
     rows = []
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    plain_done = den_done = False
     for spp in sorted(set(plain_spps) | set(denoise_spps)):
+        if plain_done and (den_done or spp > max(denoise_spps)):
+            break
         rgb, gb, ms = render(ctx, sc, spp, seed=seed)
         row = {"spp": spp, "render_ms": ms, "plain": rmse(rgb, ref)}
         ev0.record()
@@ -118,6 +124,8 @@ def evaluate(ctx, net: Denoiser, desc, ref_spp: int = 8192, plain_spps=LADDER,
             ev1.record()
             torch.cuda.synchronize()
             row["denoised"], row["denoise_ms"] = rmse(den[0], ref), ev0.elapsed_time(ev1)
+            den_done = den_done or row["denoised"] <= target_rmse
+        plain_done = plain_done or row["plain"] <= target_rmse
         rows.append(row)
     sc.close()
 
@@ -145,23 +153,30 @@ def main():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--out", default=DEFAULT_WEIGHTS)
     ap.add_argument("--eval-size", type=int, default=512)
+    ap.add_argument("--eval-scenes", type=int, default=8)
+    ap.add_argument("--eval-ref-spp", type=int, default=16384)
+    ap.add_argument("--eval-only", action="store_true", help="evaluate the weights in --out, no training")
     args = ap.parse_args()
     import torch
     ctx = api.Context()
-    t0 = time.time()
-    data = make_dataset(ctx, args.scenes, args.size, spp_ref=args.spp_ref)
-    torch.cuda.synchronize()
-    print(f"dataset {tuple(data[0].shape)} in {time.time() - t0:.1f} s", flush=True)
     net = Denoiser(seed=args.seed)
-    t1 = time.time()
-    hist = train(net, data, args.steps, args.batch, args.lr, seed=args.seed)
-    torch.cuda.synchronize()
-    print(f"trained {args.steps} steps in {time.time() - t1:.1f} s; final loss {np.mean(hist[-100:]):.5f}",
-          flush=True)
-    os.makedirs(os.path.dirname(os.path.abspath(args.out)), exist_ok=True)
-    net.save(args.out)
-    for k in range(3):
-        res = evaluate(ctx, net, P.random_scene(EVAL_SEED0 + k, width=args.eval_size))
+    if args.eval_only:
+        net.load(args.out)
+    else:
+        t0 = time.time()
+        data = make_dataset(ctx, args.scenes, args.size, spp_ref=args.spp_ref)
+        torch.cuda.synchronize()
+        print(f"dataset {tuple(data[0].shape)} in {time.time() - t0:.1f} s", flush=True)
+        t1 = time.time()
+        hist = train(net, data, args.steps, args.batch, args.lr, seed=args.seed)
+        torch.cuda.synchronize()
+        print(f"trained {args.steps} steps in {time.time() - t1:.1f} s; final loss {np.mean(hist[-100:]):.5f}",
+              flush=True)
+        del data
+        os.makedirs(os.path.dirname(os.path.abspath(args.out)), exist_ok=True)
+        net.save(args.out)
+    for k in range(args.eval_scenes):
+        res = evaluate(ctx, net, P.random_scene(EVAL_SEED0 + k, width=args.eval_size), ref_spp=args.eval_ref_spp)
         print(f"held-out scene {k}: plain reaches {res['target_rmse']} at {res['plain_spp']} spp "
               f"({res['plain_ms']} ms), denoised at {res['denoised_spp']} spp ({res['denoised_ms']} ms), "
               f"speedup {res['speedup']}", flush=True)
