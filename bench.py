@@ -223,8 +223,9 @@ def microbench_c2(ctx, steps: int = 5) -> dict:
     hits = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
     stream = torch.cuda.current_stream()
     out = {"triangles": d.num_triangles, "rays": n}
-    for width in (2, 8):
+    for width, comp in ((2, False), (2, True), (8, False)):
         ctx.set_bvh_width(width)
+        ctx.set_bvh_compression(comp)
         sc = api.Scene(ctx, d)
         builds, trace = [], []
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -238,13 +239,14 @@ def microbench_c2(ctx, steps: int = 5) -> dict:
                 builds.append([st.ms_prep, st.ms_sort, st.ms_emit, st.ms_refit, st.ms_collapse, st.ms_total])
                 trace.append(e0.elapsed_time(e1))
         b = np.median(np.array(builds), 0)
-        out[f"bvh{width}"] = {"build_ms": round(float(b[5]), 3),
+        out[f"bvh{width}" + ("_compressed" if comp else "")] = {"build_ms": round(float(b[5]), 3),
                               "build_split_ms": {k: round(float(v), 3) for k, v in
                                                  zip(("prep", "sort", "emit", "refit", "layout"), b[:5])},
                               "trace_ms": round(float(np.median(trace)), 3),
                               "mrays_per_s": round(n / (float(np.median(trace)) / 1e3) / 1e6, 1)}
         sc.close()
     ctx.set_bvh_width(2)
+    ctx.set_bvh_compression(False)
     return out
 
 
@@ -263,6 +265,8 @@ def main():
     ap.add_argument("--spp", type=int, default=0, help="override the workload's spp (profiling captures)")
     ap.add_argument("--e2e-steps", type=int, default=2, help="steps of the end-to-end leg (0: skip)")
     ap.add_argument("--bvh-width", type=int, default=2, choices=[2, 8], help="traversal layout")
+    ap.add_argument("--bvh-compression", type=int, default=-1, choices=[-1, 0, 1],
+                    help="BVH2 nodes: 0 = 64-byte FP32, 1 = 32-byte quantised; -1: the tuned / default choice")
     ap.add_argument("--no-autotune", action="store_true", help="use the library defaults (no autotuner)")
     ap.add_argument("--material-sort", type=int, default=-1, choices=[-1, 0, 1],
                     help="force the wavefront's material sort off (0) or on (1); -1: the tuned / default choice")
@@ -290,6 +294,8 @@ def main():
     W, H = desc.camera.width, desc.camera.height
     ctx = api.Context(local)
     ctx.set_bvh_width(args.bvh_width)
+    if args.bvh_compression >= 0:
+        ctx.set_bvh_compression(bool(args.bvh_compression))
     stream = torch.cuda.current_stream()
     scene = api.Scene(ctx, desc)
     scene.buildBVH(stream.cuda_stream)
@@ -308,6 +314,9 @@ def main():
         tuned = tuner.tune(scene, dict(wl, seed=seed), integ)
     if args.material_sort >= 0:
         ctx.set_material_sort(bool(args.material_sort))
+    if args.bvh_compression >= 0:
+        ctx.set_bvh_compression(bool(args.bvh_compression))
+        scene.buildBVH(stream.cuda_stream)
     if trace_only:
         from cudapathtracing_gb300 import procedural as P
         n_rays = 10_000_000
@@ -380,6 +389,9 @@ def main():
             tuner.tune(scene, dict(wl, seed=seed), integ)
         if args.material_sort >= 0:
             ctx.set_material_sort(bool(args.material_sort))
+        if args.bvh_compression >= 0:
+            ctx.set_bvh_compression(bool(args.bvh_compression))
+            scene.buildBVH(stream.cuda_stream)
     if world > 1:
         import torch.distributed as dist
         t = torch.tensor([elapsed, float(rays)], device="cuda", dtype=torch.float64)
@@ -472,6 +484,8 @@ def main():
         "config": {"workload": args.workload, "width": W, "height": H, "spp": wl["spp"],
                    "triangles": desc.num_triangles, "integrator": args.integrator,
                    "bvh_width": int(tuned.knobs["bvh_width"]) if tuned else args.bvh_width,
+                   "bvh_compression": (bool(args.bvh_compression) if args.bvh_compression >= 0 else
+                                       bool(tuned.knobs.get("bvh_compression", 0)) if tuned else False),
                    "material_sort": (bool(args.material_sort) if args.material_sort >= 0 else
                                      bool(tuned.knobs.get("material_sort", 0)) if tuned else False),
                    "estimator": "config" if wl["estimator"] == 1 else "reference",

@@ -44,6 +44,7 @@ def lib():
             "cpt_context_set_short_stack": (S, [P, C.c_int]),
             "cpt_context_set_loop_limits": (S, [P, C.c_int32, C.c_int32]),
             "cpt_context_set_material_sort": (S, [P, C.c_int]),
+            "cpt_context_set_bvh_compression": (S, [P, C.c_int]),
             "cpt_filter_bilateral": (S, [P, P, P, P, C.c_int32, C.c_int32, C.POINTER(abi.cpt_filter_params), P]),
             "cpt_pick": (S, [P, C.c_int32, C.c_int32, C.POINTER(C.c_int32)]),
             "cpt_scene_set_material": (S, [P, C.c_uint32, C.c_uint32, C.c_double, C.c_double, C.c_int32]),

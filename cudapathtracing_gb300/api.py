@@ -51,6 +51,10 @@ class Context:
         check(lib().cpt_context_set_wavefront(self.h, slots, block_trace, block_shade, use_graph),
               "cpt_context_set_wavefront")
 
+    def set_bvh_compression(self, on: bool) -> None:
+        """32-byte quantised BVH2 nodes for later builds (cpt_context_set_bvh_compression)."""
+        check(lib().cpt_context_set_bvh_compression(self.h, 1 if on else 0), "cpt_context_set_bvh_compression")
+
     def set_material_sort(self, on: bool) -> None:
         """Wavefront shade queue binned by material (cpt_context_set_material_sort)."""
         check(lib().cpt_context_set_material_sort(self.h, 1 if on else 0), "cpt_context_set_material_sort")

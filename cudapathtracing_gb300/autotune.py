@@ -4,7 +4,8 @@ Knobs (all set through the C ABI on the context):
   megakernel   thread-block shape (block_x, block_y)
   wavefront    path slots (the wavefront size), trace / shade block sizes, traversal short-stack
                depth (entries kept in shared memory), material sort of the shade queue
-  both         BVH layout width (2 or 8; changing it rebuilds the scene's trace layout)
+  both         BVH layout width (2 or 8) and BVH2 node compression (64-byte FP32 or 32-byte
+               quantised nodes); changing either rebuilds the scene's trace layout
 
 Tuning is coordinate descent from the defaults: each knob in turn is swept with the others held
 at their best values so far, every candidate is rendered `repeats` times on the caller's own
@@ -32,6 +33,7 @@ DEFAULTS = {
     "block_shade": 128,
     "short_stack": 16,
     "bvh_width": 2,
+    "bvh_compression": 0,
     "material_sort": 0,
 }
 
@@ -42,12 +44,14 @@ CANDIDATES = {
     "block_shade": [64, 128, 256],
     "short_stack": [8, 16, 24, 32],
     "bvh_width": [2, 8],
+    "bvh_compression": [0, 1],
     "material_sort": [0, 1],
 }
 
 KNOBS = {
-    abi.INTEGRATOR_MEGAKERNEL: ["bvh_width", "render_block"],
-    abi.INTEGRATOR_WAVEFRONT: ["bvh_width", "slots", "block_trace", "short_stack", "block_shade", "material_sort"],
+    abi.INTEGRATOR_MEGAKERNEL: ["bvh_width", "bvh_compression", "render_block"],
+    abi.INTEGRATOR_WAVEFRONT: ["bvh_width", "bvh_compression", "slots", "block_trace", "short_stack", "block_shade",
+                               "material_sort"],
 }
 
 
@@ -155,12 +159,12 @@ class Autotuner:
         c.set_wavefront(int(knobs["slots"]), int(knobs["block_trace"]), int(knobs["block_shade"]), 1)
         c.set_short_stack(int(knobs["short_stack"]))
         c.set_material_sort(bool(knobs.get("material_sort", 0)))
-        if scene is not None and getattr(scene, "_tuned_width", None) != knobs["bvh_width"]:
-            c.set_bvh_width(int(knobs["bvh_width"]))
+        layout = (int(knobs["bvh_width"]), int(knobs.get("bvh_compression", 0)))
+        c.set_bvh_width(layout[0])
+        c.set_bvh_compression(bool(layout[1]))
+        if scene is not None and getattr(scene, "_tuned_layout", None) != layout:
             scene.buildBVH()
-            scene._tuned_width = knobs["bvh_width"]
-        else:
-            c.set_bvh_width(int(knobs["bvh_width"]))
+            scene._tuned_layout = layout
 
     def _measure(self, scene, params: dict, integrator: int, knobs: dict) -> float:
         import torch

@@ -51,6 +51,7 @@ struct cpt_context {
     bool wf_grids_ready;
     int bvh_width;             // traversal layout built by cpt_lbvh_build: 8 (compressed wide) or 2
     int iter_limit;            // loop trips per sample of the render loops (cpt_context_set_loop_limits)
+    bool bvh2_compressed;      // BVH2 nodes of later builds: 32-byte quantised (cpt_context_set_bvh_compression)
 };
 
 namespace cpt {
@@ -93,6 +94,7 @@ struct cpt_scene {
     size_t scratch_bytes;
     // traversal layout
     int width;          // layout of the last build: 2 or 8
+    bool node_q;        // the BVH2 nodes of the last build are compressed
     float4* nodes;      // BVH2 nodes (width 2)
     float4* wide;       // compressed 8-wide nodes (width 8)
     float4* leaf_rec;
@@ -413,6 +415,7 @@ SceneView view_of(const cpt_scene* s)
     v.n_tris = (int)s->n_tris;
     v.n_internal = s->n > 1 ? (int)s->n - 1 : 0;
     v.nodes = s->nodes;
+    v.node_q = s->node_q ? 1 : 0;
     v.wide = s->width == 8 ? s->wide : nullptr;
     v.leaf_rec = s->leaf_rec;
     v.tri_mat = s->tri_mat;
@@ -455,9 +458,10 @@ cpt_status make_layout(cpt_scene* s, cudaStream_t stream, uint32_t* num_wide)
         if (st != CPT_OK) return st;
     }
     s->width = 2;
+    s->node_q = s->ctx->bvh2_compressed;
     if (num_wide) *num_wide = 0;
     return build_trace_layout(n, s->n_lights, s->n_spheres, s->child, s->node_box, s->leaf_box, s->order, s->tri_f32,
-                              s->tri_f64, s->spheres, s->nodes, s->leaf_rec, stream);
+                              s->tri_f64, s->spheres, s->nodes, s->leaf_rec, stream, s->node_q);
 }
 
 LbvhBuffers buffers_of(cpt_scene* s)
@@ -521,6 +525,7 @@ CPT_EXPORT cpt_status cpt_context_create(int device, cpt_context** out)
     c->wf_grids_ready = false;
     c->bvh_width = 2;   // the faster of the two layouts as measured on GB300
     c->iter_limit = CPT_ITER_LIMIT;
+    c->bvh2_compressed = false;
     c->wf.max_replays = CPT_MAX_REPLAYS;
     CPT_CUDA(cudaStreamCreateWithFlags(&c->wf.capture_stream, cudaStreamNonBlocking));
     CPT_CUDA(cudaStreamCreateWithFlags(&c->wf.side_stream, cudaStreamNonBlocking));
@@ -552,6 +557,13 @@ CPT_EXPORT cpt_status cpt_context_set_wavefront(cpt_context* ctx, int slots, int
     ctx->wf.block_shade = block_shade;
     ctx->wf.use_graph = use_graph != 0;
     ctx->wf_grids_ready = false;
+    return CPT_OK;
+}
+
+CPT_EXPORT cpt_status cpt_context_set_bvh_compression(cpt_context* ctx, int on)
+{
+    if (!ctx) return fail(CPT_ERR_INVALID_ARGUMENT, "cpt_context_set_bvh_compression: null context");
+    ctx->bvh2_compressed = on != 0;
     return CPT_OK;
 }
 

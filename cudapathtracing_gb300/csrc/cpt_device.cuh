@@ -73,7 +73,8 @@ struct DevCamera {     // Camera (Camera.cu:5-40), derived in double on the host
 // Read-only view of a built scene passed to trace/render kernels by value.
 struct SceneView {
     int n_prims, n_lights, n_spheres, n_tris, n_internal;
-    const float4* __restrict__ nodes;      // BVH2: 4 float4 per internal node (Aila-Laine layout)
+    const float4* __restrict__ nodes;      // BVH2: 4 float4 per internal node (Aila-Laine layout), or 2 (node_q)
+    int node_q;                            // BVH2 nodes are compressed (quantised child boxes, 32 bytes)
     const float4* __restrict__ wide;       // BVH8: CPT_WIDE_F4 float4 per wide node, or NULL (use BVH2)
     const float4* __restrict__ leaf_rec;   // 3 float4 per leaf (sorted order, or wide slot order)
     const uint32_t* __restrict__ tri_mat;  // per triangle

@@ -61,11 +61,12 @@ cpt_status lbvh_leaf_boxes(uint32_t n_extra, const float4* extra_box, uint32_t n
                            cudaStream_t stream);
 
 // ---- traversal layout (lbvh.cu)
-// BVH2 nodes (4 float4 per internal node) and leaf records (3 float4 per leaf).
+// BVH2 nodes (4 float4 per internal node, or 2 when compressed: 8-bit quantised child boxes) and
+// leaf records (3 float4 per leaf).
 cpt_status build_trace_layout(uint32_t n, uint32_t n_lights, uint32_t n_spheres, const int2* child,
                               const float4* node_box, const float4* leaf_box, const uint32_t* order,
                               const float* tri_f32, const double* tri_f64, const float4* spheres, float4* nodes,
-                              float4* leaf_rec, cudaStream_t stream);
+                              float4* leaf_rec, cudaStream_t stream, bool compressed = false);
 
 // ---- trace / render launchers (trace.cu, render.cu)
 cpt_status launch_trace(const SceneView& view, const cpt_ray* rays, uint64_t n, cpt_hit* hits, int* d_err,

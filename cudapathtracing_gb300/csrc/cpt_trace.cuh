@@ -280,6 +280,50 @@ __device__ __forceinline__ bool trace_closest_wide(const SceneView& s, float3 o,
     return hit.leaf >= 0;
 }
 
+// Slab distances of both children of BVH2 node `node` (t = box * idir - o * idir per axis) and
+// their references, from the full 64-byte node or the compressed 32-byte one (s.node_q).
+struct Bvh2Slabs {
+    float ax0, ax1, ay0, ay1, az0, az1, bx0, bx1, by0, by1, bz0, bz1;
+    int ca, cb;
+};
+
+__device__ __forceinline__ float u8f(uint32_t w, int k) { return (float)((w >> (8 * k)) & 0xFFu); }
+
+__device__ __forceinline__ void bvh2_slabs(const SceneView& s, int node, float3 o, float3 idir, float3 ood,
+                                           Bvh2Slabs& r)
+{
+    if (s.node_q) {
+        const float4* np = s.nodes + 2 * (size_t)node;
+        const float4 q0 = ldg4(np), q1 = ldg4(np + 1);
+        const uint32_t e = __float_as_uint(q0.w);
+        const float sx = __uint_as_float((e & 0xFFu) << 23) * idir.x;
+        const float sy = __uint_as_float(((e >> 8) & 0xFFu) << 23) * idir.y;
+        const float sz = __uint_as_float(((e >> 16) & 0xFFu) << 23) * idir.z;
+        const float bx = (q0.x - o.x) * idir.x, by = (q0.y - o.y) * idir.y, bz = (q0.z - o.z) * idir.z;
+        const uint32_t w0 = __float_as_uint(q1.x), w1 = __float_as_uint(q1.y), w2 = __float_as_uint(q1.z);
+        const int split = __float_as_int(q1.w);
+        r.ax0 = fmaf(u8f(w0, 0), sx, bx); r.ax1 = fmaf(u8f(w0, 3), sx, bx);
+        r.ay0 = fmaf(u8f(w0, 1), sy, by); r.ay1 = fmaf(u8f(w1, 0), sy, by);
+        r.az0 = fmaf(u8f(w0, 2), sz, bz); r.az1 = fmaf(u8f(w1, 1), sz, bz);
+        r.bx0 = fmaf(u8f(w1, 2), sx, bx); r.bx1 = fmaf(u8f(w2, 1), sx, bx);
+        r.by0 = fmaf(u8f(w1, 3), sy, by); r.by1 = fmaf(u8f(w2, 2), sy, by);
+        r.bz0 = fmaf(u8f(w2, 0), sz, bz); r.bz1 = fmaf(u8f(w2, 3), sz, bz);
+        r.ca = ((e >> 24) & 1u) ? ~split : split;
+        r.cb = ((e >> 25) & 1u) ? ~(split + 1) : split + 1;
+        return;
+    }
+    const float4* np = s.nodes + 4 * (size_t)node;
+    const float4 n0 = ldg4(np), n1 = ldg4(np + 1), n2 = ldg4(np + 2), n3 = ldg4(np + 3);
+    r.ax0 = fmaf(n0.x, idir.x, -ood.x); r.ax1 = fmaf(n0.y, idir.x, -ood.x);
+    r.ay0 = fmaf(n0.z, idir.y, -ood.y); r.ay1 = fmaf(n0.w, idir.y, -ood.y);
+    r.az0 = fmaf(n2.x, idir.z, -ood.z); r.az1 = fmaf(n2.y, idir.z, -ood.z);
+    r.bx0 = fmaf(n1.x, idir.x, -ood.x); r.bx1 = fmaf(n1.y, idir.x, -ood.x);
+    r.by0 = fmaf(n1.z, idir.y, -ood.y); r.by1 = fmaf(n1.w, idir.y, -ood.y);
+    r.bz0 = fmaf(n2.z, idir.z, -ood.z); r.bz1 = fmaf(n2.w, idir.z, -ood.z);
+    r.ca = __float_as_int(n3.x);
+    r.cb = __float_as_int(n3.y);
+}
+
 // Binary-node traversal (Aila–Laine node layout): near child first, far child pushed.  The
 // stack (ShortStack: shared memory, then local memory) holds at most one entry per level.  ANY as in
 // trace_closest_wide.
@@ -295,21 +339,13 @@ __device__ __forceinline__ bool trace_closest_bvh2(const SceneView& s, float3 o,
     int node = 0;
     float best = tmax;
     for (;;) {
-        const float4* np = s.nodes + 4 * (size_t)node;
-        float4 n0 = ldg4(np), n1 = ldg4(np + 1), n2 = ldg4(np + 2), n3 = ldg4(np + 3);
-        // child A
-        float ax0 = fmaf(n0.x, idir.x, -ood.x), ax1 = fmaf(n0.y, idir.x, -ood.x);
-        float ay0 = fmaf(n0.z, idir.y, -ood.y), ay1 = fmaf(n0.w, idir.y, -ood.y);
-        float az0 = fmaf(n2.x, idir.z, -ood.z), az1 = fmaf(n2.y, idir.z, -ood.z);
-        float an = fmaxf(fmaxf(fminf(ax0, ax1), fminf(ay0, ay1)), fmaxf(fminf(az0, az1), tmin));
-        float af = fminf(fminf(fmaxf(ax0, ax1), fmaxf(ay0, ay1)), fminf(fmaxf(az0, az1), best));
-        // child B
-        float bx0 = fmaf(n1.x, idir.x, -ood.x), bx1 = fmaf(n1.y, idir.x, -ood.x);
-        float by0 = fmaf(n1.z, idir.y, -ood.y), by1 = fmaf(n1.w, idir.y, -ood.y);
-        float bz0 = fmaf(n2.z, idir.z, -ood.z), bz1 = fmaf(n2.w, idir.z, -ood.z);
-        float bn = fmaxf(fmaxf(fminf(bx0, bx1), fminf(by0, by1)), fmaxf(fminf(bz0, bz1), tmin));
-        float bf = fminf(fminf(fmaxf(bx0, bx1), fmaxf(by0, by1)), fminf(fmaxf(bz0, bz1), best));
-        int ca = __float_as_int(n3.x), cb = __float_as_int(n3.y);
+        Bvh2Slabs r;
+        bvh2_slabs(s, node, o, idir, ood, r);
+        float an = fmaxf(fmaxf(fminf(r.ax0, r.ax1), fminf(r.ay0, r.ay1)), fmaxf(fminf(r.az0, r.az1), tmin));
+        float af = fminf(fminf(fmaxf(r.ax0, r.ax1), fmaxf(r.ay0, r.ay1)), fminf(fmaxf(r.az0, r.az1), best));
+        float bn = fmaxf(fmaxf(fminf(r.bx0, r.bx1), fminf(r.by0, r.by1)), fmaxf(fminf(r.bz0, r.bz1), tmin));
+        float bf = fminf(fminf(fmaxf(r.bx0, r.bx1), fmaxf(r.by0, r.by1)), fminf(fmaxf(r.bz0, r.bz1), best));
+        int ca = r.ca, cb = r.cb;
         bool ha = an <= af, hb = bn <= bf;
         if (ha && ca < 0 && visit_leaf<ANY>(s, ~ca, o, d, best, hit, skip)) return true;
         if (hb && cb < 0 && visit_leaf<ANY>(s, ~cb, o, d, best, hit, skip)) return true;
@@ -365,19 +401,13 @@ struct Bvh2Walk {
     // Visits one node; returns true when the traversal has finished.
     __device__ __forceinline__ bool step(const SceneView& s, int* err)
     {
-        const float4* np = s.nodes + 4 * (size_t)node;
-        float4 n0 = ldg4(np), n1 = ldg4(np + 1), n2 = ldg4(np + 2), n3 = ldg4(np + 3);
-        float ax0 = fmaf(n0.x, idir.x, -ood.x), ax1 = fmaf(n0.y, idir.x, -ood.x);
-        float ay0 = fmaf(n0.z, idir.y, -ood.y), ay1 = fmaf(n0.w, idir.y, -ood.y);
-        float az0 = fmaf(n2.x, idir.z, -ood.z), az1 = fmaf(n2.y, idir.z, -ood.z);
-        float an = fmaxf(fmaxf(fminf(ax0, ax1), fminf(ay0, ay1)), fmaxf(fminf(az0, az1), tmin));
-        float af = fminf(fminf(fmaxf(ax0, ax1), fmaxf(ay0, ay1)), fminf(fmaxf(az0, az1), best));
-        float bx0 = fmaf(n1.x, idir.x, -ood.x), bx1 = fmaf(n1.y, idir.x, -ood.x);
-        float by0 = fmaf(n1.z, idir.y, -ood.y), by1 = fmaf(n1.w, idir.y, -ood.y);
-        float bz0 = fmaf(n2.z, idir.z, -ood.z), bz1 = fmaf(n2.w, idir.z, -ood.z);
-        float bn = fmaxf(fmaxf(fminf(bx0, bx1), fminf(by0, by1)), fmaxf(fminf(bz0, bz1), tmin));
-        float bf = fminf(fminf(fmaxf(bx0, bx1), fmaxf(by0, by1)), fminf(fmaxf(bz0, bz1), best));
-        int ca = __float_as_int(n3.x), cb = __float_as_int(n3.y);
+        Bvh2Slabs r;
+        bvh2_slabs(s, node, o, idir, ood, r);
+        float an = fmaxf(fmaxf(fminf(r.ax0, r.ax1), fminf(r.ay0, r.ay1)), fmaxf(fminf(r.az0, r.az1), tmin));
+        float af = fminf(fminf(fmaxf(r.ax0, r.ax1), fmaxf(r.ay0, r.ay1)), fminf(fmaxf(r.az0, r.az1), best));
+        float bn = fmaxf(fmaxf(fminf(r.bx0, r.bx1), fminf(r.by0, r.by1)), fmaxf(fminf(r.bz0, r.bz1), tmin));
+        float bf = fminf(fminf(fmaxf(r.bx0, r.bx1), fmaxf(r.by0, r.by1)), fminf(fmaxf(r.bz0, r.bz1), best));
+        int ca = r.ca, cb = r.cb;
         bool ha = an <= af, hb = bn <= bf;
         if (ha && ca < 0 && visit_leaf<ANY>(s, ~ca, o, d, best, hit, skip)) return true;
         if (hb && cb < 0 && visit_leaf<ANY>(s, ~cb, o, d, best, hit, skip)) return true;

@@ -20,6 +20,7 @@
 #include <cstring>
 
 #include "cpt_internal.h"
+#include "cpt_quant.cuh"
 
 namespace cpt {
 
@@ -131,6 +132,33 @@ __device__ __forceinline__ void tri_center_box(const double p[9], double c[3], f
     bmax = make_float4(__double2float_ru(mx[0]), __double2float_ru(mx[1]), __double2float_ru(mx[2]), 0.f);
 }
 
+// Conversions between FP32 and FP64 by bit manipulation on the integer units: on this part the
+// FP64 pipe also executes the hardware conversions, and it is the scarce resource of k_prep.
+// widen: exact float -> double.  narrow_rd / narrow_ru: double -> float rounded down / up.  Values
+// outside the normal range of the narrower type take the hardware conversion.
+__device__ __forceinline__ double widen(float f)
+{
+    const uint32_t b = __float_as_uint(f);
+    const uint32_t e = (b >> 23) & 0xFFu;
+    if (e == 0u || e == 0xFFu) return (double)f;   // zero, subnormal, infinity, NaN
+    const uint32_t hi = (b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7FFFFFu) >> 3);
+    return __hiloint2double((int)hi, (int)(b << 29));
+}
+
+template <bool UP>
+__device__ __forceinline__ float narrow(double d)
+{
+    const uint32_t hi = (uint32_t)__double2hiint(d), lo = (uint32_t)__double2loint(d);
+    const uint32_t e = (hi >> 20) & 0x7FFu;
+    if (e < 897u || e > 1150u) return UP ? __double2float_ru(d) : __double2float_rd(d);
+    uint32_t fb = (hi & 0x80000000u) | ((e - 896u) << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29);
+    const bool inexact = (lo & 0x1FFFFFFFu) != 0u;
+    const bool negative = (hi >> 31) != 0u;
+    // truncation rounds the magnitude down; moving away from zero is one step up in the bits
+    if (inexact && (UP ? !negative : negative)) fb += 1u;
+    return __uint_as_float(fb);
+}
+
 // Padded triangle box (AABB::pad, AABB.cuh:30-40) rounded outwards to FP32.  For FP32 vertices
 // the minimum and maximum are exact in FP32; the padding is the reference's FP64 operation.
 __device__ __forceinline__ void tri_box(const float p[9], float4& bmin, float4& bmax)
@@ -141,12 +169,10 @@ __device__ __forceinline__ void tri_box(const float p[9], float4& bmin, float4& 
         mn[a] = fminf(fminf(p[a], p[3 + a]), p[6 + a]);
         mx[a] = fmaxf(fmaxf(p[a], p[3 + a]), p[6 + a]);
     }
-    bmin = make_float4(__double2float_rd(__dsub_rn((double)mn[0], 0.0001)),
-                       __double2float_rd(__dsub_rn((double)mn[1], 0.0001)),
-                       __double2float_rd(__dsub_rn((double)mn[2], 0.0001)), 0.f);
-    bmax = make_float4(__double2float_ru(__dadd_rn((double)mx[0], 0.0001)),
-                       __double2float_ru(__dadd_rn((double)mx[1], 0.0001)),
-                       __double2float_ru(__dadd_rn((double)mx[2], 0.0001)), 0.f);
+    bmin = make_float4(narrow<false>(__dsub_rn(widen(mn[0]), 0.0001)), narrow<false>(__dsub_rn(widen(mn[1]), 0.0001)),
+                       narrow<false>(__dsub_rn(widen(mn[2]), 0.0001)), 0.f);
+    bmax = make_float4(narrow<true>(__dadd_rn(widen(mx[0]), 0.0001)), narrow<true>(__dadd_rn(widen(mx[1]), 0.0001)),
+                       narrow<true>(__dadd_rn(widen(mx[2]), 0.0001)), 0.f);
 }
 
 template <typename VT>
@@ -519,15 +545,72 @@ __device__ __forceinline__ void range_union(const Levels& L, uint32_t lo, uint32
     }
 }
 
+// The same union computed by a whole warp for one range (lo and hi equal in every lane): at each
+// level the lanes load the partial blocks' boxes side by side, then one butterfly reduction.
+__device__ __forceinline__ void warp_range_union(const Levels& L, uint32_t lo, uint32_t hi, int lane, float4& mn,
+                                                 float4& mx)
+{
+    mn = make_float4(INFINITY, INFINITY, INFINITY, 0.f);
+    mx = make_float4(-INFINITY, -INFINITY, -INFINITY, 0.f);
+    for (int l = 0; l < L.count; ++l) {
+        const float4* a = L.lv[l];
+        const uint32_t lo_up = (lo + 31u) & ~31u, hi_dn = hi & ~31u;
+        const bool last = l == L.count - 1 || lo_up >= hi_dn;
+        const uint32_t lend = last ? hi : lo_up;
+        for (uint32_t x = lo + lane; x < lend; x += 32) box_union(mn, mx, a[2ull * x], a[2ull * x + 1]);
+        if (last) break;
+        for (uint32_t x = hi_dn + lane; x < hi; x += 32) box_union(mn, mx, a[2ull * x], a[2ull * x + 1]);
+        lo = lo_up >> 5;
+        hi = hi_dn >> 5;
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        mn.x = fminf(mn.x, __shfl_xor_sync(0xffffffffu, mn.x, o));
+        mn.y = fminf(mn.y, __shfl_xor_sync(0xffffffffu, mn.y, o));
+        mn.z = fminf(mn.z, __shfl_xor_sync(0xffffffffu, mn.z, o));
+        mx.x = fmaxf(mx.x, __shfl_xor_sync(0xffffffffu, mx.x, o));
+        mx.y = fmaxf(mx.y, __shfl_xor_sync(0xffffffffu, mx.y, o));
+        mx.z = fmaxf(mx.z, __shfl_xor_sync(0xffffffffu, mx.z, o));
+    }
+}
+
+// Node i's box = union of its sorted leaf range.  Ranges of up to SMALL_RANGE leaves are summed by
+// their own thread; longer ones (whose lengths differ widely between neighbouring node indices,
+// which made per-thread loops diverge) are taken one at a time by the whole warp.  Min and max
+// are exact, so the result does not depend on the grouping.
+constexpr uint32_t SMALL_RANGE = 8;
+
 __global__ void k_node_boxes(Levels L, const int2* __restrict__ range, uint32_t n_internal, float4* __restrict__ node_box)
 {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n_internal) return;
-    int2 r = range[i];
-    float4 mn, mx;
-    range_union(L, (uint32_t)r.x, (uint32_t)r.y + 1u, mn, mx);
-    node_box[2ull * i] = mn;
-    node_box[2ull * i + 1] = mx;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const bool valid = i < n_internal;
+    uint32_t lo = 0, hi = 0;
+    if (valid) {
+        const int2 r = range[i];
+        lo = (uint32_t)r.x;
+        hi = (uint32_t)r.y + 1u;
+    }
+    const bool small = hi - lo <= SMALL_RANGE;
+    if (valid && small) {
+        float4 mn = make_float4(INFINITY, INFINITY, INFINITY, 0.f), mx = make_float4(-INFINITY, -INFINITY, -INFINITY, 0.f);
+        const float4* a = L.lv[0];
+        for (uint32_t x = lo; x < hi; ++x) box_union(mn, mx, a[2ull * x], a[2ull * x + 1]);
+        node_box[2ull * i] = mn;
+        node_box[2ull * i + 1] = mx;
+    }
+    uint32_t big = __ballot_sync(0xffffffffu, valid && !small);
+    while (big) {
+        const int src = __ffs(big) - 1;
+        big &= big - 1;
+        const uint32_t blo = __shfl_sync(0xffffffffu, lo, src), bhi = __shfl_sync(0xffffffffu, hi, src);
+        float4 mn, mx;
+        warp_range_union(L, blo, bhi, lane, mn, mx);
+        if (lane == src) {
+            node_box[2ull * i] = mn;
+            node_box[2ull * i + 1] = mx;
+        }
+    }
 }
 
 // ---------------------------------------------------------------- traversal layout
@@ -546,6 +629,37 @@ __global__ void k_bvh2_nodes(const int2* __restrict__ child, const float4* __res
     nodes[4ull * i + 1] = make_float4(bmn.x, bmx.x, bmn.y, bmx.y);
     nodes[4ull * i + 2] = make_float4(amn.z, amx.z, bmn.z, bmx.z);
     nodes[4ull * i + 3] = make_float4(__int_as_float(c.x), __int_as_float(c.y), 0.f, 0.f);
+}
+
+// Compressed BVH2 node i (32 bytes, one memory sector per visit instead of two): both child boxes
+// quantised outwards to 8 bits on a grid anchored at the node box's minimum (cpt_quant.cuh), and
+// the split index of the Karras tree, whose children are always split and split + 1 (each a leaf
+// or an internal node, as two flags say):
+//   float4 q0: origin xyz; w = ex | ey << 8 | ez << 16 | leaf(A) << 24 | leaf(B) << 25
+//   uint4  q1: x = A.lo.x | A.lo.y << 8 | A.lo.z << 16 | A.hi.x << 24
+//              y = A.hi.y | A.hi.z << 8 | B.lo.x << 16 | B.lo.y << 24
+//              z = B.lo.z | B.hi.x << 8 | B.hi.y << 16 | B.hi.z << 24
+//              w = split
+__global__ void k_bvh2_qnodes(const int2* __restrict__ child, const float4* __restrict__ node_box,
+                              const float4* __restrict__ leaf_box, uint32_t n_internal, float4* __restrict__ nodes)
+{
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_internal) return;
+    int2 c = child[i];
+    const float4* ba = c.x < 0 ? leaf_box + 2ull * (uint32_t)(~c.x) : node_box + 2ull * (uint32_t)c.x;
+    const float4* bb = c.y < 0 ? leaf_box + 2ull * (uint32_t)(~c.y) : node_box + 2ull * (uint32_t)c.y;
+    const float4 amn = ba[0], amx = ba[1], bmn = bb[0], bmx = bb[1];
+    const float ox = fminf(amn.x, bmn.x), oy = fminf(amn.y, bmn.y), oz = fminf(amn.z, bmn.z);
+    const uint32_t ex = grid_exponent(ox, fmaxf(amx.x, bmx.x)), ey = grid_exponent(oy, fmaxf(amx.y, bmx.y)),
+                   ez = grid_exponent(oz, fmaxf(amx.z, bmx.z));
+    const float sx = inv_grid(ex), sy = inv_grid(ey), sz = inv_grid(ez);
+    const uint32_t split = (uint32_t)(c.x < 0 ? ~c.x : c.x);
+    const uint32_t flags = (c.x < 0 ? 1u : 0u) | (c.y < 0 ? 2u : 0u);
+    const uint32_t w0 = q_lo(amn.x, ox, sx) | q_lo(amn.y, oy, sy) << 8 | q_lo(amn.z, oz, sz) << 16 | q_hi(amx.x, ox, sx) << 24;
+    const uint32_t w1 = q_hi(amx.y, oy, sy) | q_hi(amx.z, oz, sz) << 8 | q_lo(bmn.x, ox, sx) << 16 | q_lo(bmn.y, oy, sy) << 24;
+    const uint32_t w2 = q_lo(bmn.z, oz, sz) | q_hi(bmx.x, ox, sx) << 8 | q_hi(bmx.y, oy, sy) << 16 | q_hi(bmx.z, oz, sz) << 24;
+    nodes[2ull * i] = make_float4(ox, oy, oz, __uint_as_float(ex | ey << 8 | ez << 16 | flags << 24));
+    nodes[2ull * i + 1] = make_float4(__uint_as_float(w0), __uint_as_float(w1), __uint_as_float(w2), __uint_as_float(split));
 }
 
 // Leaf record k (48 bytes) for primitive order[k]:
@@ -769,10 +883,13 @@ cpt_status lbvh_refit(uint32_t n, const LbvhBuffers& out, void* scratch, size_t 
 cpt_status build_trace_layout(uint32_t n, uint32_t n_lights, uint32_t n_spheres, const int2* child,
                               const float4* node_box, const float4* leaf_box, const uint32_t* order,
                               const float* tri_f32, const double* tri_f64, const float4* spheres, float4* nodes,
-                              float4* leaf_rec, cudaStream_t stream)
+                              float4* leaf_rec, cudaStream_t stream, bool compressed)
 {
     if (n == 0) return CPT_OK;
-    if (n > 1 && nodes) k_bvh2_nodes<<<blocks_for(n - 1, 256), 256, 0, stream>>>(child, node_box, leaf_box, n - 1, nodes);
+    if (n > 1 && nodes && compressed)
+        k_bvh2_qnodes<<<blocks_for(n - 1, 256), 256, 0, stream>>>(child, node_box, leaf_box, n - 1, nodes);
+    else if (n > 1 && nodes)
+        k_bvh2_nodes<<<blocks_for(n - 1, 256), 256, 0, stream>>>(child, node_box, leaf_box, n - 1, nodes);
     if (tri_f64)
         k_leaf_records<double><<<blocks_for(n, 256), 256, 0, stream>>>(order, n, n_lights, n_spheres, tri_f64, spheres,
                                                                        leaf_rec);

@@ -245,6 +245,12 @@ cpt_status cpt_context_set_short_stack(cpt_context* ctx, int entries);
  * both child boxes per 64-byte node (the default), 8 = the compressed 8-wide BVH (96-byte nodes,
  * 8-bit quantised child boxes, direction-ordered slots). */
 cpt_status cpt_context_set_bvh_width(cpt_context* ctx, int width);
+/* BVH2 node format of later cpt_lbvh_build / cpt_lbvh_refit calls: 0 = 64-byte nodes with both
+ * child boxes in FP32 (the default), 1 = 32-byte nodes (one memory sector per visit) with both
+ * child boxes quantised outwards to 8 bits on a grid spanning the node, and the children as the
+ * Karras split index.  Closest hits are the same up to exact ties; the quantised boxes are larger,
+ * so a traversal may test a few more nodes. */
+cpt_status cpt_context_set_bvh_compression(cpt_context* ctx, int on);
 /* Wavefront integrator: when on, every iteration files the traced paths into bins by the material
  * their ray hit (miss / light / medium, Opaque and Lambertian, specular dielectric, rough
  * dielectric) and shades the bins in order, so that a warp's lanes run one BSDF.  The image is

@@ -55,17 +55,21 @@ def spheres(ctx, oracle_mod):
         s.close()
 
 
-@pytest.mark.parametrize("width", [2, 8])
+@pytest.mark.parametrize("width", [2, 8, "2q"])
 @pytest.mark.parametrize("integrator", [abi.INTEGRATOR_MEGAKERNEL, abi.INTEGRATOR_WAVEFRONT],
                          ids=["megakernel", "wavefront"])
 def test_spheres_1080p_band_vs_oracle(ctx, spheres, integrator, width):
+    """Traversal layouts: BVH2 (64-byte nodes), the 8-wide BVH, and BVH2 with 32-byte quantised
+    nodes ("2q")."""
     d, ref, scenes = spheres
     if width not in scenes:
-        ctx.set_bvh_width(width)
+        ctx.set_bvh_width(2 if width == "2q" else width)
+        ctx.set_bvh_compression(width == "2q")
         try:
             scenes[width] = api.Scene(ctx, d).init()
         finally:
             ctx.set_bvh_width(2)
+            ctx.set_bvh_compression(False)
     s = scenes[width]
     assert s.num_prims == d.num_prims == 4096016   # 4,096,014 triangles + 2 lights
     r = s.render(integrator=integrator, rows=BAND, **SPHERES_PRM)

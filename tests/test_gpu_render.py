@@ -88,18 +88,21 @@ def test_config_estimator_vs_oracle(ctx, oracle_mod, name, integrator):
     assert abs(r["rays"] - o["rays"]) / o["rays"] < 0.01
 
 
-@pytest.mark.parametrize("width", [2, 8])
+@pytest.mark.parametrize("width", [2, 8, "2q"])
 @pytest.mark.parametrize("slots,graph", [(1 << 20, 1), (1024, 1), (1536, 0)])
 @pytest.mark.parametrize("name", ["cornell", "volume_glass", "spheres"])
 def test_wavefront_matches_megakernel(ctx, name, slots, graph, width):
     """Same estimator, same PCG32 streams and draw order: the two integrators trace the same
-    paths.  With fewer slots than pixels the slots take new pixels as they finish."""
+    paths.  With fewer slots than pixels the slots take new pixels as they finish.  "2q": BVH2 with
+    32-byte quantised nodes."""
     d = config_scene(name)
-    ctx.set_bvh_width(width)
+    ctx.set_bvh_width(2 if width == "2q" else width)
+    ctx.set_bvh_compression(width == "2q")
     try:
         s = api.Scene(ctx, d).init()
     finally:
         ctx.set_bvh_width(2)
+        ctx.set_bvh_compression(False)
     prm = config_params(name, spp=6)
     mk = s.render(integrator=abi.INTEGRATOR_MEGAKERNEL, **prm)
     ctx.set_wavefront(slots, 128, 128, graph)

@@ -55,11 +55,14 @@ def check_t(gpu, ref_ids, ref_t):
     assert rel.max(initial=0) < 2e-5
 
 
-@pytest.fixture(params=[8, 2], ids=["bvh8", "bvh2"])
+@pytest.fixture(params=[8, 2, "2q"], ids=["bvh8", "bvh2", "bvh2_compressed"])
 def width(request, ctx):
-    ctx.set_bvh_width(request.param)
-    yield request.param
+    w = 2 if request.param == "2q" else request.param
+    ctx.set_bvh_width(w)
+    ctx.set_bvh_compression(request.param == "2q")
+    yield w
     ctx.set_bvh_width(2)
+    ctx.set_bvh_compression(False)
 
 
 def test_axis_parallel_rays(ctx, oracle_mod, width):
