@@ -157,7 +157,26 @@ def cpu_reference_sample(desc, seconds: float = 15.0):
     c = CpuReference(desc)
     c.calibrate(seconds)
     v = c.run()
-    return v, c.info(v)
+    info = c.info(v)
+    info["rows"] = [c.r0, c.r0 + c.rows]
+    return v, info
+
+
+def same_sample_on_gpu(scene, rows, stream, reps: int = 5) -> dict:
+    """The CPU baseline's exact sample on the GPU: the same band of rows, 1 spp, PCG32 seed 0, the
+    reference's STATIC estimator (megakernel), so the two Mrays/s figures trace the same paths."""
+    from cudapathtracing_gb300 import abi
+    r = None
+    rays, ms = 0, 0.0
+    for i in range(reps + 1):
+        r = scene.render(spp=1, seed=0, estimator=abi.ESTIMATOR_REFERENCE, integrator=abi.INTEGRATOR_MEGAKERNEL,
+                         rows=tuple(rows), stream=stream, want_rgba8=False)
+        if i:
+            rays += r["rays"]
+            ms += r["ms"]
+    return {"value": round(rays / (ms / 1e3) / 1e6, 2), "unit": "Mrays/s", "rows": list(rows),
+            "rays_per_run": rays // reps, "estimator": "reference (STATIC)", "integrator": "megakernel",
+            "timing": "device time of the render, scene resident"}
 
 
 def run_reference_arm(args):
@@ -470,9 +489,11 @@ def main():
             micro = {"error": str(e)}
 
     cpu = None
+    same_gpu = None
     if not args.no_cpu_baseline:
         try:
             _, cpu = cpu_reference_sample(desc, seconds=15.0)
+            same_gpu = same_sample_on_gpu(scene, cpu["rows"], stream.cuda_stream)
         except Exception as e:  # the baseline is reported, never required
             cpu = {"value": None, "unit": "Mrays/s", "cores": 0, "kind": "port", "sample": f"failed: {e}"}
 
@@ -503,6 +524,7 @@ def main():
                          "k_wf_* (every launch of one render)" if args.integrator == "wavefront" else "k_render"),
                      "kernel_ms": round(k_ms, 3), "bytes_per_ray": round(bpr, 1), "peak_source": peak_src},
         "cpu_baseline": cpu,
+        "cpu_sample_on_gpu": same_gpu,
         "megakernel_same_run": compare,
         "lbvh_traversal_microbench": micro,
         "denoise": denoise,
