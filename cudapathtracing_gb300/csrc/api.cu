@@ -56,7 +56,7 @@ struct cpt_context {
 
 namespace cpt {
 cpt_status wavefront_grids(int sm_count, int block_trace, int block_shade, int short_entries, int* grid_trace,
-                           int* grid_shade);
+                           int* grid_trace_wide, int* grid_shade);
 size_t wide_scratch_bytes(uint32_t n);
 cpt_status build_wide(uint32_t n, const int2* child, const float4* node_box, const float4* leaf_box, float4* wide,
                       void* scratch, size_t scratch_bytes, cudaStream_t stream, uint32_t* num_wide);
@@ -1002,7 +1002,7 @@ CPT_EXPORT cpt_status cpt_render(cpt_scene* s, const cpt_render_params* p, const
     if (p->integrator == CPT_INTEGRATOR_WAVEFRONT) {
         cpt_context* c = s->ctx;
         if (!c->wf_grids_ready) {
-            st = wavefront_grids(c->sm_count, c->wf.block_trace, c->wf.block_shade, c->wf.short_stack, &c->wf.grid_trace,
+            st = wavefront_grids(c->sm_count, c->wf.block_trace, c->wf.block_shade, c->wf.short_stack, &c->wf.grid_trace, &c->wf.grid_trace_wide,
                                  &c->wf.grid_shade);
             c->wf_grids_ready = st == CPT_OK;
         }
@@ -1125,7 +1125,7 @@ CPT_EXPORT cpt_status cpt_render_batch(cpt_context* ctx, const cpt_render_job* j
     }
     if (!ctx->wf_grids_ready) {
         st = wavefront_grids(ctx->sm_count, ctx->wf.block_trace, ctx->wf.block_shade, ctx->wf.short_stack,
-                             &ctx->wf.grid_trace, &ctx->wf.grid_shade);
+                             &ctx->wf.grid_trace, &ctx->wf.grid_trace_wide, &ctx->wf.grid_shade);
         ctx->wf_grids_ready = st == CPT_OK;
         if (st != CPT_OK) {
             release();

@@ -97,7 +97,8 @@ cpt_status launch_render_megakernel(const SceneView& view, const RenderArgs& arg
 // Wavefront integrator launch shape (the autotuner's knobs) and graph-capture resources.
 struct WavefrontTuning {
     int slots;                   // path slots (the wavefront size)
-    int grid_trace, block_trace; // persistent grids
+    int grid_trace, block_trace; // persistent grids (grid_trace_wide: the 8-wide trace kernels)
+    int grid_trace_wide;
     int grid_shade, block_shade;
     int short_stack;             // traversal stack entries kept in shared memory (8, 16, 24, 32)
     bool use_graph;

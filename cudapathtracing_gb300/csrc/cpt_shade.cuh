@@ -30,6 +30,21 @@ __device__ __forceinline__ void set_face_normal(Surf& sf, float3 d, float3 outwa
     sf.normal = sf.front ? outward : -outward;
 }
 
+// Luminance of a radiance sample (Rec. 709 weights).
+__device__ __forceinline__ float luminance(float3 c) { return 0.2126f * c.x + 0.7152f * c.y + 0.0722f * c.z; }
+
+// G-buffer channel 7 of the config estimator: the variance of the pixel mean's luminance, from the
+// sum of the samples' radiance and the sum of their squared luminances (spp samples).  With one
+// sample the squared luminance stands in for it.  Both integrators add the same samples in the same
+// order (groups in group order), so they write the same value.
+__device__ __forceinline__ float mean_variance(float3 sum, float sum_y2, int spp)
+{
+    if (spp <= 1) return sum_y2;
+    const float ys = luminance(sum);
+    const float v = (sum_y2 - ys * ys / (float)spp) / ((float)(spp - 1) * (float)spp);
+    return fmaxf(v, 0.f);
+}
+
 // Nearest texel of an 8-bit RGB image at (u, v) (HitRecord::sampleTexture, HitRecord.cuh:38-49;
 // the same rule in Camera::getSkyBox, Camera.cuh:56-61): x = clamp(int(u * w), 0, w - 1), y likewise,
 // texels / 255.  The float-to-int conversion saturates, so far-out coordinates clamp too.

@@ -20,9 +20,10 @@
 // poolings); the feature kernel writes zeros in the padding and the kernel apply clamps its
 // gather to the real image.
 //
-// Input features (10 channels, padded to 32 with zeros): log(1 + radiance) (3), albedo (3),
-// octahedral normal (2), depth / (1 + depth) (1, 1 on a miss), and the 3x3 variance of
-// log(1 + luminance) around the pixel (1).
+// Input features (11 channels, padded to 32 with zeros): log(1 + radiance) (3), albedo (3),
+// octahedral normal (2), depth / (1 + depth) (1, 1 on a miss), the 3x3 variance of
+// log(1 + luminance) around the pixel (1), and log(1 + the standard deviation of the pixel mean's
+// luminance) from the renderer's own samples (G-buffer channel 7) (1).
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
@@ -42,7 +43,7 @@ constexpr int KSIZE = 5;           // predicted filter: 5 x 5
 constexpr int KTAPS = KSIZE * KSIZE;
 constexpr int IN_CH = 32;          // input features padded from 10 to 32 channels
 constexpr int OUT_CH = 32;         // logits padded from 25 to 32 channels
-constexpr int NUM_FEATURES = 10;   // written by k_features; the rest of IN_CH is zero
+constexpr int NUM_FEATURES = 11;   // written by k_features; the rest of IN_CH is zero
 static_assert(NUM_FEATURES <= IN_CH && IN_CH % 32 == 0, "feature padding");
 
 struct View {                      // NHWC tensor slice: element (p, c) at ptr[p * cs + co + c]
@@ -494,6 +495,8 @@ __global__ void k_features(Geo g, int Hr, int Wr, const float* __restrict__ rgb,
             float var = 0.f;
             for (int k = 0; k < 9; ++k) var += (l9[k] - m) * (l9[k] - m);
             f[9] = var / 9.f;
+            // standard deviation of the pixel mean (G-buffer channel 7: variance of its luminance)
+            f[10] = log1pf(sqrtf(fmaxf(g1.w, 0.f)));
         }
         uint4* fo = reinterpret_cast<uint4*>(feat + p * IN_CH);
 #pragma unroll

@@ -34,6 +34,7 @@ struct PixelResult {
     float3 gn;
     float gdepth;
     float3 galb;
+    float gvar;   // variance of the pixel mean's luminance (config estimator), 0 otherwise
     uint32_t rays;
 };
 
@@ -47,6 +48,7 @@ __device__ PixelResult pixel_reference(const SceneView& s, int i, int j, const R
 {
     PixelResult out;
     out.rays = 0;
+    out.gvar = 0.f;
     const DevCamera& cam = s.cam;
     Pcg32 rng;
     rng.init(a.seed, (uint64_t)j * cam.width + i);
@@ -167,6 +169,7 @@ __device__ PixelResult pixel_config(const SceneView& s, int i, int j, const Rend
     const uint64_t stream = (uint64_t)j * cam.width + i;
     const int group = sample_group(a.spp);
     float3 pix = f3(0.f, 0.f, 0.f), gsum = f3(0.f, 0.f, 0.f);
+    float pix_y2 = 0.f, gsum_y2 = 0.f;   // sums of the samples' squared luminances
     for (int sample = 0; sample < a.spp; ++sample) {
         Pcg32 rng;
         rng.init_sample(a.seed, stream, (uint32_t)sample);
@@ -273,12 +276,17 @@ __device__ PixelResult pixel_config(const SceneView& s, int i, int j, const Rend
             d = dir;
         }
         gsum = gsum + rad;
+        const float y = luminance(rad);
+        gsum_y2 += y * y;
         if ((sample + 1) % group == 0 || sample + 1 == a.spp) {
             pix = pix + gsum;
             gsum = f3(0.f, 0.f, 0.f);
+            pix_y2 += gsum_y2;
+            gsum_y2 = 0.f;
         }
     }
     out.rgb = pix / (float)a.spp;
+    out.gvar = mean_variance(pix, pix_y2, a.spp);
     return out;
 }
 
@@ -317,7 +325,7 @@ __global__ void __maxnreg__(72) k_render(SceneView s, RenderArgs a)
         if (a.gbuf) {
             float4* g = reinterpret_cast<float4*>(a.gbuf) + 2 * off;
             g[0] = make_float4(r.gn.x, r.gn.y, r.gn.z, r.gdepth);
-            g[1] = make_float4(r.galb.x, r.galb.y, r.galb.z, 0.f);
+            g[1] = make_float4(r.galb.x, r.galb.y, r.galb.z, r.gvar);
         }
         rays = r.rays;
     }

@@ -97,7 +97,7 @@ struct Wf {
     const WfJob* jobs;      // device array of n_jobs, NULL for a single render
     int n_jobs;
     int* job;               // job of the slot's item
-    int all_bvh2;           // every job's scene has a BVH2 with internal nodes (dynamic fetching)
+    int all_bvh2;           // every job's scene has internal nodes (dynamic fetching)
 };
 
 // One render of a batch: its scene and parameters, and its share of the items and group sums.
@@ -184,6 +184,14 @@ __device__ __forceinline__ void count_rays(unsigned long long* counter, uint32_t
 
 __device__ __forceinline__ float3 xyz(float4 v) { return f3(v.x, v.y, v.z); }
 __device__ __forceinline__ float4 w0(float3 v) { return make_float4(v.x, v.y, v.z, 0.f); }
+
+// A finished sample's radiance added to its item's sum: radiance in xyz, squared luminance in w
+// (G-buffer channel 7, mean_variance).
+__device__ __forceinline__ float4 add_sample(float4 sum, float3 r)
+{
+    const float y = luminance(r);
+    return make_float4(sum.x + r.x, sum.y + r.y, sum.z + r.z, sum.w + y * y);
+}
 
 __device__ __forceinline__ float3 camera_dir(const DevCamera& c, int i, int j, float rx, float ry)   // Camera.cuh:37-43
 {
@@ -293,9 +301,15 @@ __global__ void k_wf_finish(JobGeo jg, RenderArgs a, int groups)
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= jg.npix) return;
     float3 sum = f3(0.f, 0.f, 0.f);
-    for (int g = 0; g < groups; ++g) sum = sum + xyz(jg.part[(size_t)g * jg.npix + p]);
+    float sum_y2 = 0.f;
+    for (int g = 0; g < groups; ++g) {
+        const float4 part = jg.part[(size_t)g * jg.npix + p];
+        sum = sum + xyz(part);
+        sum_y2 += part.w;
+    }
     float3 v = sum / (float)a.spp;
     size_t off = (size_t)(jg.first_pix + p);
+    if (a.gbuf) a.gbuf[8 * off + 7] = mean_variance(sum, sum_y2, a.spp);
     if (a.flags & CPT_RENDER_ACCUMULATE) {
         a.rgb[3 * off] += v.x;
         a.rgb[3 * off + 1] += v.y;
@@ -311,7 +325,7 @@ __global__ void k_wf_finish(JobGeo jg, RenderArgs a, int groups)
 // At most 48 registers (5 blocks of 256 per SM): 62 % occupancy instead of 50 % for a few spilled
 // values, +5.7 % on the 1080p spheres render (the shadow kernel is faster uncapped).
 template <bool WIDE, int SHORT, bool SORT, bool MULTI>
-__global__ void __launch_bounds__(256, 5) k_wf_trace(const __grid_constant__ SceneView s, Wf w, int par)
+__global__ void __launch_bounds__(256, WIDE ? 3 : 5) k_wf_trace(const __grid_constant__ SceneView s, Wf w, int par)
 {
     const int n = w.cnt[par];
     const int nq = par ^ 1;
@@ -328,22 +342,26 @@ __global__ void __launch_bounds__(256, 5) k_wf_trace(const __grid_constant__ Sce
     int* const bin_cnt = w.cnt + CNT_BIN + par * NBIN;
     const auto views = [&](int j) -> const SceneView& { return MULTI ? w.jobs[j].view : s; };
     uint32_t rays = 0;
-    if (!WIDE && (MULTI ? w.all_bvh2 != 0 : s.n_internal > 0)) {
-        rays = trace_items_bvh2_views<false, ShortStackN<SHORT>>(
-            views, n, &w.cnt[8 + 2 * par], w.err,
-            [&](int i, float3& o, float3& d, float& tmn, float& tmx, int&, int& j) {
-                int slot = q[i];
-                o = xyz(w.o[slot]);
-                d = xyz(w.d[slot]);
-                tmn = 0.001f;
-                tmx = CPT_INF_F;
-                j = MULTI ? w.job[slot] : 0;
-            },
-            [&](int i, const Hit& h, int j) {
-                const int slot = q[i];
-                w.hit[slot] = make_float4(h.t, __int_as_float(h.leaf), h.u, h.v);
-                if (SORT) append_binned(bins, bin_cnt, w.M, shade_bin(views(j), h.leaf), slot);
-            });
+    const auto load = [&](int i, float3& o, float3& d, float& tmn, float& tmx, int&, int& j) {
+        int slot = q[i];
+        o = xyz(w.o[slot]);
+        d = xyz(w.d[slot]);
+        tmn = 0.001f;
+        tmx = CPT_INF_F;
+        j = MULTI ? w.job[slot] : 0;
+    };
+    const auto store = [&](int i, const Hit& h, int j) {
+        const int slot = q[i];
+        w.hit[slot] = make_float4(h.t, __int_as_float(h.leaf), h.u, h.v);
+        if (SORT) append_binned(bins, bin_cnt, w.M, shade_bin(views(j), h.leaf), slot);
+    };
+    if (MULTI ? w.all_bvh2 != 0 : s.n_internal > 0) {
+        if (WIDE)
+            rays = trace_items_wide_views<false, ShortStack64<CPT_WIDE_SHORT_STACK>>(views, n, &w.cnt[8 + 2 * par],
+                                                                                     w.err, load, store);
+        else
+            rays = trace_items_bvh2_views<false, ShortStackN<SHORT>>(views, n, &w.cnt[8 + 2 * par], w.err, load,
+                                                                    store);
     } else {
         for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
             int slot = q[idx];
@@ -366,20 +384,24 @@ __global__ void __launch_bounds__(256) k_wf_shadow(const __grid_constant__ Scene
     const int* sq = w.sq + (size_t)par * w.M * w.L;
     const auto views = [&](int j) -> const SceneView& { return MULTI ? w.jobs[j].view : s; };
     uint32_t rays = 0;
-    if (!WIDE && (MULTI ? w.all_bvh2 != 0 : s.n_internal > 0)) {
-        rays = trace_items_bvh2_views<true, ShortStackN<SHORT>>(
-            views, n, &w.cnt[9 + 2 * par], w.err,
-            [&](int i, float3& o, float3& d, float& tmn, float& tmx, int& skip, int& j) {
-                int e = sq[i];
-                float4 dd = w.sd[e];
-                o = xyz(w.so[e]);
-                d = xyz(dd);
-                tmn = 0.001f;
-                tmx = dd.w;
-                skip = e % w.L;
-                j = MULTI ? w.job[e / w.L] : 0;
-            },
-            [&](int i, const Hit& h, int) { w.svis[sq[i]] = h.leaf < 0 ? 1 : 0; });
+    const auto load = [&](int i, float3& o, float3& d, float& tmn, float& tmx, int& skip, int& j) {
+        int e = sq[i];
+        float4 dd = w.sd[e];
+        o = xyz(w.so[e]);
+        d = xyz(dd);
+        tmn = 0.001f;
+        tmx = dd.w;
+        skip = e % w.L;
+        j = MULTI ? w.job[e / w.L] : 0;
+    };
+    const auto store = [&](int i, const Hit& h, int) { w.svis[sq[i]] = h.leaf < 0 ? 1 : 0; };
+    if (MULTI ? w.all_bvh2 != 0 : s.n_internal > 0) {
+        if (WIDE)
+            rays = trace_items_wide_views<true, ShortStack64<CPT_WIDE_SHORT_STACK>>(views, n, &w.cnt[9 + 2 * par],
+                                                                                    w.err, load, store);
+        else
+            rays = trace_items_bvh2_views<true, ShortStackN<SHORT>>(views, n, &w.cnt[9 + 2 * par], w.err, load,
+                                                                   store);
     } else {
         for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
             int e = sq[idx];
@@ -413,7 +435,7 @@ __global__ void __launch_bounds__(256) k_wf_resolve(const __grid_constant__ Scen
     for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
         int slot = rq[idx];
         float3 acc = add_visible(w, slot, w.nee[slot], xyz(w.radp[slot]));
-        w.pix[slot] = w0(xyz(w.pix[slot]) + acc);
+        w.pix[slot] = add_sample(w.pix[slot], acc);
         w.nee[slot] = 0;
         if (MULTI) {
             const WfJob& J = w.jobs[w.job[slot]];
@@ -463,7 +485,7 @@ __global__ void __launch_bounds__(256, 4) k_wf_shade(const __grid_constant__ Sce
         if (pend) {
             if (fl & F_NEE_PREV) {
                 float3 accp = add_visible(w, slot, pend, xyz(w.radp[slot]));
-                w.pix[slot] = w0(xyz(w.pix[slot]) + accp);
+                w.pix[slot] = add_sample(w.pix[slot], accp);
             } else {
                 rad = add_visible(w, slot, pend, rad);
             }
@@ -604,7 +626,7 @@ __global__ void __launch_bounds__(256, 4) k_wf_shade(const __grid_constant__ Sce
                 w.radp[slot] = w0(rad);
                 fl |= F_NEE_PREV;
             } else {
-                w.pix[slot] = w0(xyz(w.pix[slot]) + rad);
+                w.pix[slot] = add_sample(w.pix[slot], rad);
             }
             const JobGeo jg = MULTI ? geo_of(w, w.jobs[job]) : geo_of(w);
             if (k % jg.S != 0 && k < a.spp) {   // the item's group has samples left
@@ -661,7 +683,7 @@ void enqueue_chunk(const SceneView& view, const Wf& w, const RenderArgs& args, i
                    int short_entries, cudaStream_t st, const WavefrontTuning* fork)
 {
     const TracePair kp = trace_pair(view.wide != nullptr, short_entries, w.bins != nullptr, MULTI);
-    const size_t smem = short_stack_bytes(bt, short_entries);
+    const size_t smem = view.wide ? wide_short_stack_bytes(bt) : short_stack_bytes(bt, short_entries);
     for (int it = 0; it < CHUNK; ++it) {
         int par = it & 1;
         cudaStream_t ss = st;
@@ -741,9 +763,9 @@ cpt_status run_wavefront(const SceneView& view, const RenderArgs& args, const st
             n_parts += items;
             L = std::max(L, j.view.n_lights);
         }
-        w.all_bvh2 = 1;
+        w.all_bvh2 = 1;   // every job has internal nodes (all share one layout): dynamic fetching
         for (const WfJob& j : J)
-            if (j.view.wide != nullptr || j.view.n_internal <= 0) w.all_bvh2 = 0;
+            if (j.view.n_internal <= 0) w.all_bvh2 = 0;
         if (n_items == 0) return CPT_OK;
     }
     if (n_items > (size_t)INT32_MAX / 2) return fail(CPT_ERR_UNSUPPORTED, "wavefront integrator: too many pixel groups");
@@ -787,7 +809,7 @@ cpt_status run_wavefront(const SceneView& view, const RenderArgs& args, const st
     // Q_0 = all M slots
     k_wf_init<MULTI><<<(M + 255) / 256, 256, 0, stream>>>(view, w, args);
     add_launches(1);
-    const int gt = tune.grid_trace, gs = tune.grid_shade;
+    const int gt = view.wide ? tune.grid_trace_wide : tune.grid_trace, gs = tune.grid_shade;
     const int bt = tune.block_trace, bs = tune.block_shade;
     cudaGraphExec_t exec = nullptr;
     cudaGraph_t graph = nullptr;
@@ -874,13 +896,12 @@ cpt_status launch_render_wavefront_batch(const SceneView* views, const RenderArg
 
 namespace cpt {
 
-// Persistent grid sizes: resident blocks per SM (occupancy) x SMs, for the given block sizes.
+// Persistent grid sizes: resident blocks per SM (occupancy) x SMs, for the given block sizes; the
+// binary and the 8-wide trace kernels have their own register caps and shared stacks.
 cpt_status wavefront_grids(int sm_count, int block_trace, int block_shade, int short_entries, int* grid_trace,
-                           int* grid_shade)
+                           int* grid_trace_wide, int* grid_shade)
 {
-    int bt = 0, bs = 0;
-    int bt2 = 0;
-    const size_t smem = short_stack_bytes(block_trace, short_entries);
+    int bw = 0, bb = 0, bs = 0;
     const TracePair wide = trace_pair(true, short_entries), bin = trace_pair(false, short_entries);
     cudaFuncAttributes fa[3];
     CPT_CUDA(cudaFuncGetAttributes(&fa[0], wide.trace));
@@ -889,11 +910,13 @@ cpt_status wavefront_grids(int sm_count, int block_trace, int block_shade, int s
     if (block_trace > std::min(fa[0].maxThreadsPerBlock, fa[1].maxThreadsPerBlock) ||
         block_shade > fa[2].maxThreadsPerBlock)
         return fail(CPT_ERR_INVALID_ARGUMENT, "wavefront block size above the kernels' limit");
-    CPT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bt, wide.trace, block_trace, smem));
-    CPT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bt2, bin.trace, block_trace, smem));
-    bt = std::min(bt, bt2);
+    CPT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bw, wide.trace, block_trace,
+                                                           wide_short_stack_bytes(block_trace)));
+    CPT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bb, bin.trace, block_trace,
+                                                           short_stack_bytes(block_trace, short_entries)));
     CPT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bs, k_wf_shade<false>, block_shade, 0));
-    *grid_trace = std::max(1, bt) * sm_count;
+    *grid_trace = std::max(1, bb) * sm_count;
+    *grid_trace_wide = std::max(1, bw) * sm_count;
     *grid_shade = std::max(1, bs) * sm_count;
     return CPT_OK;
 }

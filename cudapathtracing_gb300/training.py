@@ -1,13 +1,14 @@
 """Training data, training loop and evaluation for the kernel-predicting denoiser.
 
-Data: seeded random scenes (procedural.random_scene), each rendered by the library at 1, 4, 16, 64
-and 256 spp (the inputs, with their G-buffers) and at 2048 spp with another seed (the target).
+Data: seeded random scenes (procedural.random_scene), each rendered by the library at 1, 4, 16, 64,
+128, 256 and 512 spp (the inputs, with their G-buffers, whose channel 7 is the renderer's own
+variance of the pixel mean) and at 4096 spp with another seed (the target).
 Training: Adam on random batches of crops through cpt_denoiser_train_step.  Evaluation: RMSE in
 display space (sqrt, clamped to [0, 1], per channel over all pixels, as pic2RGBW shows images,
 Render.cu:462-481) against a high-spp render of a held-out scene, for the plain render, the
 reference's bilateral filter and the denoiser, and the wall time each needs to reach a target RMSE.
 
-    python -m cudapathtracing_gb300.training --scenes 1024 --steps 10000 --out weights.npz
+    python -m cudapathtracing_gb300.training --scenes 2000 --steps 20000 --out weights.npz
 """
 from __future__ import annotations
 
@@ -37,7 +38,7 @@ def render(ctx, scene, spp: int, seed: int, integrator=abi.INTEGRATOR_WAVEFRONT,
     return rgb, gb, r["ms"]
 
 
-def make_dataset(ctx, n_scenes: int, size: int = 256, spp_in=(1, 4, 16, 64, 256), spp_ref: int = 2048,
+def make_dataset(ctx, n_scenes: int, size: int = 256, spp_in=(1, 4, 16, 64, 128, 256, 512), spp_ref: int = 4096,
                  seed0: int = TRAIN_SEED0, log=print):
     """Stacked device tensors noisy [M, S, S, 3], gbuf [M, S, S, 8], target [M, S, S, 3] with
     M = n_scenes * len(spp_in) (one target per scene, shared by its inputs)."""
@@ -144,10 +145,10 @@ def evaluate(ctx, net: Denoiser, desc, ref_spp: int = 16384, plain_spps=LADDER,
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--scenes", type=int, default=1024)
+    ap.add_argument("--scenes", type=int, default=2000)
     ap.add_argument("--size", type=int, default=256)
-    ap.add_argument("--spp-ref", type=int, default=2048)
-    ap.add_argument("--steps", type=int, default=10000)
+    ap.add_argument("--spp-ref", type=int, default=4096)
+    ap.add_argument("--steps", type=int, default=20000)
     ap.add_argument("--batch", type=int, default=8)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--seed", type=int, default=0)

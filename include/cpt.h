@@ -198,7 +198,9 @@ typedef struct cpt_render_params {
 typedef struct cpt_render_output {
     float* rgb;        /* W*H*3 mean radiance per pixel (pic, Render.cu:222-225); required */
     uint8_t* rgba8;    /* optional W*H*4: sqrt gamma, x254.99, clamp (Render.cu:229-260) */
-    float* gbuffer;    /* optional W*H*8: first-hit normal xyz, distance, albedo rgb, 0 */
+    float* gbuffer;    /* optional W*H*8: first-hit normal xyz, distance, albedo rgb, and (config
+                          estimator) the variance of the pixel mean's luminance over its samples
+                          (one sample: its squared luminance); 0 under the reference estimator */
     int32_t on_device; /* 1: the pointers above are device pointers, 0: host */
     int32_t reserved;
 } cpt_render_output;

@@ -883,8 +883,11 @@ static inline Ray cameraRay(const Scene& s, int x, int y, double rx, double ry) 
 struct PixelOut {
     V3 rgb;
     V3 gN; double gDepth; V3 gAlbedo;
+    double gVar;   // config estimator: variance of the pixel mean's luminance
     uint64_t rays;
 };
+
+static inline double luminance(V3 c) { return 0.2126 * c.x + 0.7152 * c.y + 0.0722 * c.z; }
 
 // The reference's STATIC render for one pixel (Render.cu:20-227).
 static PixelOut renderPixelReference(const Scene& s, int i, int j, int spp, uint64_t seed)
@@ -901,7 +904,7 @@ static PixelOut renderPixelReference(const Scene& s, int i, int j, int spp, uint
         Ray ray = cameraRay(s, i, j, rx, ry);
         V3 thr = v3(1.0, 1.0, 1.0);
         V3 rad = v3(0.0, 0.0, 0.0);
-        out.gN = v3(0, 0, 0); out.gDepth = INF; out.gAlbedo = v3(0, 0, 0);
+        out.gN = v3(0, 0, 0); out.gDepth = INF; out.gAlbedo = v3(0, 0, 0); out.gVar = 0.0;
         bool hasSampleLight = false;
         for (;;) {
             HitRecord rec;
@@ -999,6 +1002,7 @@ static PixelOut renderPixelConfig(const Scene& s, int i, int j, const cpt_render
     int offset = j * s.width + i;
     const int group = sampleGroup(p.spp);
     V3 pix = v3(0, 0, 0), gsum = v3(0, 0, 0);
+    double sumY2 = 0.0;
     uint64_t rays = 0;
     out.gDepth = INF;
     for (int sample = 0; sample < p.spp; ++sample) {
@@ -1104,11 +1108,15 @@ static PixelOut renderPixelConfig(const Scene& s, int i, int j, const cpt_render
             ray.d = dir;
         }
         gsum = gsum + rad;
+        sumY2 += luminance(rad) * luminance(rad);
         if ((sample + 1) % group == 0 || sample + 1 == p.spp) {
             pix = pix + gsum;
             gsum = v3(0, 0, 0);
         }
     }
+    // the sample variance of the luminance over the samples, divided by spp (one sample: Y^2)
+    const double ys = luminance(pix);
+    out.gVar = p.spp <= 1 ? sumY2 : std::max(0.0, (sumY2 - ys * ys / p.spp) / ((double)(p.spp - 1) * p.spp));
     pix = v3(pix.x / p.spp, pix.y / p.spp, pix.z / p.spp);
     out.rgb = pix;
     out.rays = rays;
@@ -1345,7 +1353,7 @@ ORC_API uint64_t orc_render(void* p, const cpt_render_params* prm, double* rgb, 
                 rgba8[4 * off + 3] = 255;
             }
             if (gbuf) {
-                double g[8] = {o.gN.x, o.gN.y, o.gN.z, o.gDepth, o.gAlbedo.x, o.gAlbedo.y, o.gAlbedo.z, 0.0};
+                double g[8] = {o.gN.x, o.gN.y, o.gN.z, o.gDepth, o.gAlbedo.x, o.gAlbedo.y, o.gAlbedo.z, o.gVar};
                 std::memcpy(gbuf + 8 * off, g, sizeof g);
             }
             local += o.rays;

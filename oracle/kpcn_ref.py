@@ -75,6 +75,7 @@ def features(rgb, gbuf, H, W, rnd=bf16):
             nb.append(lum[:, yy][:, :, xx])
     nb = np.stack(nb)
     X[:, :Hr, :Wr, 9] = ((nb - nb.mean(0)) ** 2).mean(0)
+    X[:, :Hr, :Wr, 10] = np.log1p(np.sqrt(np.maximum(gbuf[..., 7].astype(np.float64), 0.0)))
     return rnd(X), rad
 
 

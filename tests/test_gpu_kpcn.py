@@ -28,6 +28,7 @@ def _batch(rng, N, H, W):
     g[..., 3] = rng.uniform(1, 5, size=(N, H, W))
     g[..., 3][rng.uniform(size=(N, H, W)) < 0.1] = K.INF
     g[..., 4:7] = rng.uniform(0.1, 0.9, size=(N, H, W, 3))
+    g[..., 7] = rng.gamma(0.5, 0.02, size=(N, H, W))   # variance of the pixel mean
     tgt = rng.gamma(2.0, 0.2, size=(N, H, W, 3)).astype(np.float32)
     return rgb, g, tgt
 

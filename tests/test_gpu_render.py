@@ -460,3 +460,32 @@ def test_render_batch_arguments(ctx):
     with pytest.raises(CptError):   # bad row range
         api.render_batch(ctx, [dict(scene=a, spp=1, rows=(5, 10 ** 6))])
     assert api.render_batch(ctx, [])["rays"] == 0
+
+
+@pytest.mark.parametrize("integrator", [abi.INTEGRATOR_MEGAKERNEL, abi.INTEGRATOR_WAVEFRONT],
+                         ids=["megakernel", "wavefront"])
+@pytest.mark.parametrize("spp", [1, 6, 24])
+def test_gbuffer_sample_variance_vs_oracle(ctx, oracle_mod, integrator, spp):
+    """G-buffer channel 7 (config estimator): the variance of the pixel mean's luminance from the
+    renderer's own samples, against the FP64 oracle on the pixels whose samples follow the same paths
+    (radiance within 1e-4); FP32 cancellation in sum(Y^2) - (sum Y)^2 / spp is bounded by
+    1e-6 * mean^2."""
+    import torch
+    d = config_scene("volume_glass")
+    s = api.Scene(ctx, d).init()
+    prm = dict(spp=spp, estimator=abi.ESTIMATOR_CONFIG, max_depth=12, rr_depth=3, rr_prob=0.8, seed=6)
+    rgb = torch.zeros((s.height, s.width, 3), device="cuda")
+    gb = torch.zeros((s.height, s.width, 8), device="cuda")
+    s.render(integrator=integrator, rgb=rgb, gbuffer=gb, **prm)
+    torch.cuda.synchronize()
+    o = oracle_mod.OracleScene(d).render(abi.render_params(**prm), gbuffer=True)
+    g = gb.cpu().numpy()[..., 7].astype(np.float64)
+    r = rgb.cpu().numpy().astype(np.float64)
+    ov = o["gbuffer"][..., 7]
+    same = (np.abs(r - o["rgb"]) <= 1e-4 * np.maximum(1.0, o["rgb"])).all(-1)
+    lum = 0.2126 * o["rgb"][..., 0] + 0.7152 * o["rgb"][..., 1] + 0.0722 * o["rgb"][..., 2]
+    ok = np.abs(g - ov) <= 1e-3 * ov + 1e-6 * lum * lum + 1e-12
+    assert same.mean() > 0.9
+    assert ok[same].all(), (np.abs(g - ov)[same & ~ok][:5], ov[same & ~ok][:5])
+    assert (g >= 0).all() and np.isfinite(g).all()
+    assert (ov > 0).mean() > 0.5
