@@ -41,7 +41,7 @@ namespace kpcn {
 
 constexpr int KSIZE = 5;           // predicted filter: 5 x 5
 constexpr int KTAPS = KSIZE * KSIZE;
-constexpr int IN_CH = 32;          // input features padded from 10 to 32 channels
+constexpr int IN_CH = 32;          // input features padded from 11 to 32 channels
 constexpr int OUT_CH = 32;         // logits padded from 25 to 32 channels
 constexpr int NUM_FEATURES = 11;   // written by k_features; the rest of IN_CH is zero
 static_assert(NUM_FEATURES <= IN_CH && IN_CH % 32 == 0, "feature padding");
