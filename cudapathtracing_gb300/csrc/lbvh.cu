@@ -3,14 +3,14 @@
 //   k_prep        centroid (FP64) + Morton code + leaf box per primitive
 //                 (generateMortonCodes Device.cuh:134-142, morton3D BVH.cuh:23-41,
 //                  Hittable ctors Hittable.cuh:456-462)
-//   radix sort    stable LSD over the 30-bit codes, 8-bit digits, per-tile ranking with
+//   radix sort    stable LSD over the 30-bit codes, three 10-bit digits, per-tile ranking with
 //                 __match_any_sync (replaces thrust::sort_by_key Device.cuh:187-189: keys are
 //                 code<<32|index, so a stable sort of codes with ascending indices is the
 //                 same permutation)
 //   k_emit        Karras 2012 range/split per internal node (generateHierarchy BVH.cuh:174-241)
 //   refit         atomic-free: an internal node covers the contiguous sorted leaves
-//                 [first, last], so its box is a range union, answered from 32-ary block
-//                 unions of the leaf boxes (replaces the serial constructAABB BVH.cuh:243-280;
+//                 [first, last], so its box is a range union, answered from a 4-ary pyramid
+//                 of unions of the leaf boxes (replaces the serial constructAABB BVH.cuh:243-280;
 //                 min/max is exact, so the boxes equal the pairwise unions)
 //
 // All boxes are FP32 rounded outwards from the reference's FP64 boxes.
@@ -30,9 +30,12 @@ constexpr int RS_THREADS = 256;
 constexpr int RS_WARPS = RS_THREADS / 32;
 constexpr int RS_ITEMS = 16;
 constexpr int RS_TILE = RS_THREADS * RS_ITEMS;   // 4096 keys per tile
-constexpr int RS_BINS = 256;
-constexpr int RS_PASSES = 4;                     // bits 0-7, 8-15, 16-23, 24-29
-constexpr int MAX_LEVELS = 8;
+constexpr int RS_BITS = 10;
+constexpr int RS_BINS = 1 << RS_BITS;            // 1024 digits
+constexpr uint32_t RS_MASK = RS_BINS - 1;
+constexpr int RS_PASSES = 3;                     // bits 0-9, 10-19, 20-29: the whole 30-bit code
+constexpr int RS_DPT = RS_BINS / RS_THREADS;     // digits per thread in the per-tile scans
+static_assert(RS_BITS * RS_PASSES >= 30 && RS_BINS % RS_THREADS == 0, "radix digits");
 
 __device__ __forceinline__ uint32_t expand_bits(uint32_t v)   // BVH.cuh:12-19
 {
@@ -100,6 +103,18 @@ __device__ __forceinline__ int cell_of(double x, double tol)
     return (x - f > tol && f + 1.0 - x > tol) ? (int)f : -1;
 }
 
+// Steps 2 and 3.  Out of line, so that the compiler cannot evaluate them speculatively beside the
+// FP32 step: they run for a fraction of a percent of the coordinates.
+__device__ __noinline__ uint32_t morton_tri_axis_fp64(double a, double b, double c, MortonAxis m)
+{
+    const double s = __dadd_rn(__dadd_rn(a, b), c);   // the reference's sum
+    const double x64 = __dmul_rn(__dsub_rn(__dmul_rn(s, 1.0 / 3.0), m.mn), m.k64);
+    const double tol64 = 0x1p-48 * (m.k64 * (fabs(s) + fabs(m.mn)) + 2.0 * fabs(x64));
+    const int cell = cell_of(x64, tol64);
+    if (cell >= 0) return (uint32_t)cell;
+    return morton_axis(__ddiv_rn(s, 3.0), m.mn, m.mx);
+}
+
 template <typename VT>
 __device__ __forceinline__ uint32_t morton_tri_axis(VT a, VT b, VT c, const MortonAxis& m)
 {
@@ -107,14 +122,9 @@ __device__ __forceinline__ uint32_t morton_tri_axis(VT a, VT b, VT c, const Mort
     const float x32 = ((a32 + b32 + c32) * (1.0f / 3.0f) - m.mn32) * m.k32;
     const float mag = fabsf(a32) + fabsf(b32) + fabsf(c32) + fabsf(m.mn32);
     const float tol32 = 0x1p-20f * (m.k32 * mag + 2.0f * fabsf(x32));
-    int cell = cell_of(x32, tol32);
+    const int cell = cell_of(x32, tol32);
     if (cell >= 0) return (uint32_t)cell;
-    const double s = __dadd_rn(__dadd_rn((double)a, (double)b), (double)c);   // the reference's sum
-    const double x64 = __dmul_rn(__dsub_rn(__dmul_rn(s, 1.0 / 3.0), m.mn), m.k64);
-    const double tol64 = 0x1p-48 * (m.k64 * (fabs(s) + fabs(m.mn)) + 2.0 * fabs(x64));
-    cell = cell_of(x64, tol64);
-    if (cell >= 0) return (uint32_t)cell;
-    return morton_axis(__ddiv_rn(s, 3.0), m.mn, m.mx);
+    return morton_tri_axis_fp64((double)a, (double)b, (double)c, m);
 }
 
 // Triangle centroid and padded box (Hittable.cuh:459-461, AABB.cuh:30-40), boxes rounded
@@ -135,12 +145,17 @@ __device__ __forceinline__ void tri_center_box(const double p[9], double c[3], f
 // Conversions between FP32 and FP64 by bit manipulation on the integer units: on this part the
 // FP64 pipe also executes the hardware conversions, and it is the scarce resource of k_prep.
 // widen: exact float -> double.  narrow_rd / narrow_ru: double -> float rounded down / up.  Values
-// outside the normal range of the narrower type take the hardware conversion.
+// outside the normal range of the narrower type take the hardware conversion, out of line (an
+// inline conversion is evaluated for every value and then discarded by a select).
+__device__ __noinline__ double widen_hw(float f) { return (double)f; }
+__device__ __noinline__ float narrow_hw_rd(double d) { return __double2float_rd(d); }
+__device__ __noinline__ float narrow_hw_ru(double d) { return __double2float_ru(d); }
+
 __device__ __forceinline__ double widen(float f)
 {
     const uint32_t b = __float_as_uint(f);
     const uint32_t e = (b >> 23) & 0xFFu;
-    if (e == 0u || e == 0xFFu) return (double)f;   // zero, subnormal, infinity, NaN
+    if (e == 0u || e == 0xFFu) return widen_hw(f);   // zero, subnormal, infinity, NaN
     const uint32_t hi = (b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7FFFFFu) >> 3);
     return __hiloint2double((int)hi, (int)(b << 29));
 }
@@ -150,7 +165,7 @@ __device__ __forceinline__ float narrow(double d)
 {
     const uint32_t hi = (uint32_t)__double2hiint(d), lo = (uint32_t)__double2loint(d);
     const uint32_t e = (hi >> 20) & 0x7FFu;
-    if (e < 897u || e > 1150u) return UP ? __double2float_ru(d) : __double2float_rd(d);
+    if (e < 897u || e > 1150u) return UP ? narrow_hw_ru(d) : narrow_hw_rd(d);
     uint32_t fb = (hi & 0x80000000u) | ((e - 896u) << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29);
     const bool inexact = (lo & 0x1FFFFFFFu) != 0u;
     const bool negative = (hi >> 31) != 0u;
@@ -159,8 +174,46 @@ __device__ __forceinline__ float narrow(double d)
     return __uint_as_float(fb);
 }
 
+// The reference's padding in FP64: RD32(RN64(x - 1e-4)) (UP false) or RU32(RN64(x + 1e-4)).
+template <bool UP>
+__device__ __noinline__ float pad_fp64(float x)
+{
+    return UP ? narrow<true>(__dadd_rn(widen(x), 0.0001)) : narrow<false>(__dsub_rn(widen(x), 0.0001));
+}
+
+// The same value from FP32 operations.  c = RN64(1e-4) is split as PAD_HI + PAD_LO (PAD_HI =
+// RN32(c), PAD_LO = RN32(c - PAD_HI) = 2.53e-12, within 2^-62 of the exact remainder).  TwoSum
+// gives x -+ PAD_HI = s + e exactly, so the exact q = x -+ c is s + r with r = e -+ PAD_LO.  For
+// |s| >= 2^-10, |r| is below half the spacing of the floats next to s, so the directed rounding of
+// q is s or its neighbour, by the sign of r.  It equals the rounding of RN64(q) unless RN64 moves
+// q onto or across s, which needs |r| <= 2^-53 |q|.  The result is therefore certain when |r| >
+// 2^-50 |s| (double rounding) + 2^-23 |r| (rounding of r) + 2^-62 (PAD_LO); otherwise, and for
+// |s| outside [2^-10, 2^100) or a non-finite x, the FP64 sequence runs.  tests/test_pad_fp32.py
+// restates this in numpy float32 and compares it bit for bit with the FP64 sequence on sweeps of
+// float32 bit patterns; coordinates of magnitude 0.01 .. 4000 never take the fallback.
+constexpr float PAD_HI = 0x1.a36e2ep-14f;
+constexpr float PAD_LO = 0x1.638866p-39f;
+
+template <bool UP>
+__device__ __forceinline__ float pad_fp32(float x)
+{
+    const float h = UP ? PAD_HI : -PAD_HI;
+    const float s = __fadd_rn(x, h);
+    const float bb = __fsub_rn(s, x);
+    const float e = __fadd_rn(__fsub_rn(x, __fsub_rn(s, bb)), __fsub_rn(h, bb));
+    const float r = UP ? __fadd_rn(e, PAD_LO) : __fsub_rn(e, PAD_LO);
+    const float as = fabsf(s);
+    const float tol = 0x1p-50f * as + 0x1p-23f * fabsf(r) + 0x1p-62f;
+    if (!(as >= 0x1p-10f && as < 0x1p100f) || !(fabsf(r) > tol)) return pad_fp64<UP>(x);
+    const uint32_t sb = __float_as_uint(s);
+    const bool away = UP ? r > 0.f : r < 0.f;   // the neighbour of s in the rounding direction
+    const bool neg = (sb >> 31) != 0u;
+    return away ? __uint_as_float((UP != neg) ? sb + 1u : sb - 1u) : s;
+}
+
 // Padded triangle box (AABB::pad, AABB.cuh:30-40) rounded outwards to FP32.  For FP32 vertices
-// the minimum and maximum are exact in FP32; the padding is the reference's FP64 operation.
+// the minimum and maximum are exact in FP32; the padding is the reference's FP64 operation,
+// evaluated by pad_fp32.
 __device__ __forceinline__ void tri_box(const float p[9], float4& bmin, float4& bmax)
 {
     float mn[3], mx[3];
@@ -169,10 +222,8 @@ __device__ __forceinline__ void tri_box(const float p[9], float4& bmin, float4& 
         mn[a] = fminf(fminf(p[a], p[3 + a]), p[6 + a]);
         mx[a] = fmaxf(fmaxf(p[a], p[3 + a]), p[6 + a]);
     }
-    bmin = make_float4(narrow<false>(__dsub_rn(widen(mn[0]), 0.0001)), narrow<false>(__dsub_rn(widen(mn[1]), 0.0001)),
-                       narrow<false>(__dsub_rn(widen(mn[2]), 0.0001)), 0.f);
-    bmax = make_float4(narrow<true>(__dadd_rn(widen(mx[0]), 0.0001)), narrow<true>(__dadd_rn(widen(mx[1]), 0.0001)),
-                       narrow<true>(__dadd_rn(widen(mx[2]), 0.0001)), 0.f);
+    bmin = make_float4(pad_fp32<false>(mn[0]), pad_fp32<false>(mn[1]), pad_fp32<false>(mn[2]), 0.f);
+    bmax = make_float4(pad_fp32<true>(mx[0]), pad_fp32<true>(mx[1]), pad_fp32<true>(mx[2]), 0.f);
 }
 
 template <typename VT>
@@ -251,7 +302,7 @@ __global__ void k_digit_totals(const uint32_t* __restrict__ code, uint32_t n, ui
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         uint32_t c = code[i];
 #pragma unroll
-        for (int p = 0; p < RS_PASSES; ++p) atomicAdd(&h[p][(c >> (8 * p)) & 255u], 1u);
+        for (int p = 0; p < RS_PASSES; ++p) atomicAdd(&h[p][(c >> (RS_BITS * p)) & RS_MASK], 1u);
     }
     __syncthreads();
     for (int t = threadIdx.x; t < RS_PASSES * RS_BINS; t += blockDim.x) {
@@ -281,9 +332,9 @@ __global__ void __launch_bounds__(RS_THREADS) k_radix_hist(const uint32_t* __res
 #pragma unroll 4
     for (int it = 0; it < RS_ITEMS; ++it) {
         uint32_t e = base + it * 32 + lane;
-        uint32_t d = e < n ? (keys[e] >> shift) & 255u : 256u;
+        uint32_t d = e < n ? (keys[e] >> shift) & RS_MASK : (uint32_t)RS_BINS;
         uint32_t peers = __match_any_sync(0xffffffffu, d);
-        if (d < 256u && lane == __ffs(peers) - 1) wh[w][d] += __popc(peers);
+        if (d < (uint32_t)RS_BINS && lane == __ffs(peers) - 1) wh[w][d] += __popc(peers);
         __syncwarp();
     }
     __syncthreads();
@@ -304,7 +355,8 @@ __global__ void __launch_bounds__(256) k_radix_scan(uint32_t* __restrict__ count
     __shared__ uint32_t s_carry;
     const int d = blockIdx.x;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    uint32_t b = (threadIdx.x < (unsigned)d) ? totals[threadIdx.x] : 0u;
+    uint32_t b = 0;
+    for (int t = threadIdx.x; t < d; t += 256) b += totals[t];
 #pragma unroll
     for (int o = 16; o; o >>= 1) b += __shfl_xor_sync(0xffffffffu, b, o);
     if (lane == 0) s_part[w] = b;
@@ -338,22 +390,28 @@ __global__ void __launch_bounds__(256) k_radix_scan(uint32_t* __restrict__ count
     }
 }
 
+// Shared memory of the scatter kernel (73,760 bytes, dynamic).
+struct ScatterSmem {
+    uint32_t wh[RS_WARPS][RS_BINS];   // per-warp digit counts, then per-warp exclusive offsets
+    uint32_t start[RS_BINS];          // tile-local start of each digit
+    uint32_t gofs[RS_BINS];           // global start of each digit's run of this tile
+    uint32_t keys[RS_TILE];
+    uint32_t vals[RS_TILE];
+    uint32_t wsum[RS_WARPS];
+};
+
 // Stable scatter: rank each key within its tile (warp-ordered, lane-ordered), stage the tile
 // in shared memory in sorted order, then write runs to their global offsets.
-__global__ void __launch_bounds__(RS_THREADS) k_radix_scatter(const uint32_t* __restrict__ keys_in,
+__global__ void __launch_bounds__(RS_THREADS, 3) k_radix_scatter(const uint32_t* __restrict__ keys_in,
                                                               const uint32_t* __restrict__ vals_in,
                                                               uint32_t* __restrict__ keys_out,
                                                               uint32_t* __restrict__ vals_out, uint32_t n, int shift,
                                                               const uint32_t* __restrict__ offsets, uint32_t num_tiles)
 {
-    __shared__ uint32_t wh[RS_WARPS][RS_BINS];
-    __shared__ uint32_t s_start[RS_BINS];
-    __shared__ uint32_t s_gofs[RS_BINS];
-    __shared__ uint32_t s_keys[RS_TILE];
-    __shared__ uint32_t s_vals[RS_TILE];
-    __shared__ uint32_t s_wsum[RS_WARPS];
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    ScatterSmem& S = *reinterpret_cast<ScatterSmem*>(smem_raw);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    for (int t = threadIdx.x; t < RS_WARPS * RS_BINS; t += RS_THREADS) (&wh[0][0])[t] = 0;
+    for (int t = threadIdx.x; t < RS_WARPS * RS_BINS; t += RS_THREADS) (&S.wh[0][0])[t] = 0;
     __syncthreads();
     const uint32_t tile = blockIdx.x;
     const uint32_t base = tile * RS_TILE + w * 32 * RS_ITEMS;
@@ -365,61 +423,66 @@ __global__ void __launch_bounds__(RS_THREADS) k_radix_scatter(const uint32_t* __
         bool valid = e < n;
         k[it] = valid ? keys_in[e] : 0u;
         v[it] = valid ? vals_in[e] : 0u;
-        uint32_t d = valid ? (k[it] >> shift) & 255u : 256u;
+        uint32_t d = valid ? (k[it] >> shift) & RS_MASK : (uint32_t)RS_BINS;
         uint32_t peers = __match_any_sync(0xffffffffu, d);
         int leader = __ffs(peers) - 1;
-        uint32_t old = (lane == leader && valid) ? wh[w][d] : 0u;
+        uint32_t old = (lane == leader && valid) ? S.wh[w][d] : 0u;
         old = __shfl_sync(0xffffffffu, old, leader);
-        if (lane == leader && valid) wh[w][d] = old + __popc(peers);
+        if (lane == leader && valid) S.wh[w][d] = old + __popc(peers);
         rank[it] = old + __popc(peers & lt);
         __syncwarp();
     }
     __syncthreads();
-    // Per digit: exclusive prefix over warps (in place) and the tile's count.
-    uint32_t cnt;
-    {
-        const int d = threadIdx.x;
+    // Digits RS_DPT * t .. RS_DPT * t + RS_DPT - 1 belong to thread t: exclusive prefix over warps
+    // (in place), the tile's count of each, and their exclusive prefix within the thread.
+    uint32_t local[RS_DPT];
+    uint32_t tsum = 0;
+#pragma unroll
+    for (int j = 0; j < RS_DPT; ++j) {
+        const int d = RS_DPT * threadIdx.x + j;
         uint32_t run = 0;
 #pragma unroll
         for (int q = 0; q < RS_WARPS; ++q) {
-            uint32_t c = wh[q][d];
-            wh[q][d] = run;
+            uint32_t c = S.wh[q][d];
+            S.wh[q][d] = run;
             run += c;
         }
-        cnt = run;
-        s_gofs[d] = offsets[(size_t)d * num_tiles + tile];
+        local[j] = tsum;
+        tsum += run;
+        S.gofs[d] = offsets[(size_t)d * num_tiles + tile];
     }
-    // Block exclusive scan of the 256 counts -> s_start.
-    uint32_t x = cnt;
+    // Block exclusive scan of the threads' sums -> S.start.
+    uint32_t x = tsum;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
         uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
         if (lane >= o) x += y;
     }
-    if (lane == 31) s_wsum[w] = x;
+    if (lane == 31) S.wsum[w] = x;
     __syncthreads();
     uint32_t wpre = 0;
-    for (int q = 0; q < w; ++q) wpre += s_wsum[q];
-    s_start[threadIdx.x] = wpre + x - cnt;
+    for (int q = 0; q < w; ++q) wpre += S.wsum[q];
+#pragma unroll
+    for (int j = 0; j < RS_DPT; ++j) S.start[RS_DPT * threadIdx.x + j] = wpre + x - tsum + local[j];
     __syncthreads();
 #pragma unroll
     for (int it = 0; it < RS_ITEMS; ++it) {
         uint32_t e = base + it * 32 + lane;
         if (e < n) {
-            uint32_t d = (k[it] >> shift) & 255u;
-            uint32_t pos = s_start[d] + wh[w][d] + rank[it];
-            s_keys[pos] = k[it];
-            s_vals[pos] = v[it];
+            uint32_t d = (k[it] >> shift) & RS_MASK;
+            uint32_t pos = S.start[d] + S.wh[w][d] + rank[it];
+            S.keys[pos] = k[it];
+            S.vals[pos] = v[it];
         }
     }
     __syncthreads();
     uint32_t tile_n = min((uint32_t)RS_TILE, n - tile * RS_TILE);
     for (uint32_t p = threadIdx.x; p < tile_n; p += RS_THREADS) {
-        uint32_t kk = s_keys[p];
-        uint32_t d = (kk >> shift) & 255u;
-        uint32_t g = s_gofs[d] + (p - s_start[d]);
+        uint32_t kk = S.keys[p];
+        uint32_t d = (kk >> shift) & RS_MASK;
+        uint32_t g = S.gofs[d] + (p - S.start[d]);
         keys_out[g] = kk;
-        vals_out[g] = s_vals[p];
+        vals_out[g] = S.vals[p];
     }
 }
 
@@ -478,139 +541,165 @@ __global__ void k_emit(const uint32_t* __restrict__ code, const uint32_t* __rest
     if (range) range[idx] = make_int2(first, last);
 }
 
-// Sorted leaf boxes and (optionally) the reference's 64-bit keys.
-__global__ void k_leaves(const uint32_t* __restrict__ code, const uint32_t* __restrict__ order, uint32_t n,
-                         const float4* __restrict__ box_unsorted, float4* __restrict__ leaf_box,
-                         uint64_t* __restrict__ keys)
-{
-    uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    uint32_t p = order[k];
-    leaf_box[2ull * k] = box_unsorted[2ull * p];
-    leaf_box[2ull * k + 1] = box_unsorted[2ull * p + 1];
-    if (keys) keys[k] = ((uint64_t)code[k] << 32) | p;
-}
-
 // ---------------------------------------------------------------- range-union refit
+// The box pyramid: level 0 is the sorted leaf boxes (n of them); level l + 1 holds
+// ceil(size(l) / 4) boxes, box j the union of boxes 4j .. 4j + 3 of level l; the levels above
+// the leaves are stored back to back (two float4 per box) down to a level of one box.
 __device__ __forceinline__ void box_union(float4& mn, float4& mx, float4 a, float4 b)
 {
     mn.x = fminf(mn.x, a.x); mn.y = fminf(mn.y, a.y); mn.z = fminf(mn.z, a.z);
     mx.x = fmaxf(mx.x, b.x); mx.y = fmaxf(mx.y, b.y); mx.z = fmaxf(mx.z, b.z);
 }
 
-// out[b] = union(in[32b .. 32b+31]); one warp per output box.
-__global__ void k_reduce32(const float4* __restrict__ in, uint32_t nin, float4* __restrict__ out, uint32_t nout)
-{
-    uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    int lane = threadIdx.x & 31;
-    if (gw >= nout) return;
-    uint32_t e = gw * 32 + lane;
-    float4 mn = make_float4(INFINITY, INFINITY, INFINITY, 0.f), mx = make_float4(-INFINITY, -INFINITY, -INFINITY, 0.f);
-    if (e < nin) { mn = in[2ull * e]; mx = in[2ull * e + 1]; }
-#pragma unroll
-    for (int o = 16; o; o >>= 1) {
-        mn.x = fminf(mn.x, __shfl_xor_sync(0xffffffffu, mn.x, o));
-        mn.y = fminf(mn.y, __shfl_xor_sync(0xffffffffu, mn.y, o));
-        mn.z = fminf(mn.z, __shfl_xor_sync(0xffffffffu, mn.z, o));
-        mx.x = fmaxf(mx.x, __shfl_xor_sync(0xffffffffu, mx.x, o));
-        mx.y = fmaxf(mx.y, __shfl_xor_sync(0xffffffffu, mx.y, o));
-        mx.z = fmaxf(mx.z, __shfl_xor_sync(0xffffffffu, mx.z, o));
-    }
-    if (lane == 0) { out[2ull * gw] = mn; out[2ull * gw + 1] = mx; }
-}
-
-struct Levels {
-    const float4* lv[MAX_LEVELS];
-    uint32_t n[MAX_LEVELS];
-    int count;
-};
-
-// Union of leaf boxes [lo, hi) (exclusive hi) from the block-union hierarchy: partial blocks
-// at each level, then move up one level with the aligned middle.
-__device__ __forceinline__ void range_union(const Levels& L, uint32_t lo, uint32_t hi, float4& mn, float4& mx)
+__device__ __forceinline__ void empty_box(float4& mn, float4& mx)
 {
     mn = make_float4(INFINITY, INFINITY, INFINITY, 0.f);
     mx = make_float4(-INFINITY, -INFINITY, -INFINITY, 0.f);
-    for (int l = 0; l < L.count; ++l) {
-        const float4* a = L.lv[l];
-        uint32_t lo_up = (lo + 31u) & ~31u, hi_dn = hi & ~31u;
-        if (l == L.count - 1 || lo_up >= hi_dn) {
-            for (uint32_t x = lo; x < hi; ++x) box_union(mn, mx, a[2ull * x], a[2ull * x + 1]);
+}
+
+__device__ __forceinline__ void shfl_union(float4& mn, float4& mx, int o)
+{
+    mn.x = fminf(mn.x, __shfl_xor_sync(0xffffffffu, mn.x, o));
+    mn.y = fminf(mn.y, __shfl_xor_sync(0xffffffffu, mn.y, o));
+    mn.z = fminf(mn.z, __shfl_xor_sync(0xffffffffu, mn.z, o));
+    mx.x = fmaxf(mx.x, __shfl_xor_sync(0xffffffffu, mx.x, o));
+    mx.y = fmaxf(mx.y, __shfl_xor_sync(0xffffffffu, mx.y, o));
+    mx.z = fmaxf(mx.z, __shfl_xor_sync(0xffffffffu, mx.z, o));
+}
+
+__device__ __forceinline__ void store_box(float4* __restrict__ a, uint32_t j, float4 mn, float4 mx)
+{
+    a[2ull * j] = mn;
+    a[2ull * j + 1] = mx;
+}
+
+constexpr int PYR_THREADS = 256;   // one block reduces 256 boxes: up to four levels per launch
+
+// Writes the next `depth` (1 to 4) pyramid levels above a level of n boxes.  Thread t of block b
+// holds box 256 b + t of that level (an empty box past n); `out` is the first level to write.
+// Every thread of the block must call it (it shuffles and synchronises); depth is uniform.
+__device__ __forceinline__ void pyramid_up(float4 mn, float4 mx, uint32_t n, float4* __restrict__ out, int depth)
+{
+    __shared__ float4 s_mn[PYR_THREADS / 16], s_mx[PYR_THREADS / 16];
+    const uint32_t t = threadIdx.x, i = blockIdx.x * PYR_THREADS + t;
+    shfl_union(mn, mx, 1);
+    shfl_union(mn, mx, 2);
+    const uint32_t n1 = (n + 3) / 4;
+    if ((t & 3u) == 0 && (i >> 2) < n1) store_box(out, i >> 2, mn, mx);
+    if (depth == 1) return;
+    float4* out2 = out + 2ull * n1;
+    shfl_union(mn, mx, 4);
+    shfl_union(mn, mx, 8);
+    const uint32_t n2 = (n1 + 3) / 4;
+    if ((t & 15u) == 0 && (i >> 4) < n2) store_box(out2, i >> 4, mn, mx);
+    if (depth == 2) return;
+    if ((t & 15u) == 0) {
+        s_mn[t >> 4] = mn;
+        s_mx[t >> 4] = mx;
+    }
+    __syncthreads();
+    if (t >= 32) return;
+    // warp 0: lane L < 16 holds group L of 16 boxes
+    if (t < PYR_THREADS / 16) {
+        mn = s_mn[t];
+        mx = s_mx[t];
+    } else {
+        empty_box(mn, mx);
+    }
+    float4* out3 = out2 + 2ull * n2;
+    const uint32_t n3 = (n2 + 3) / 4;
+    shfl_union(mn, mx, 1);
+    shfl_union(mn, mx, 2);
+    const uint32_t j3 = blockIdx.x * (PYR_THREADS / 64) + (t >> 2);
+    if ((t & 3u) == 0 && t < PYR_THREADS / 16 && j3 < n3) store_box(out3, j3, mn, mx);
+    if (depth == 3) return;
+    float4* out4 = out3 + 2ull * n3;
+    const uint32_t n4 = (n3 + 3) / 4;
+    shfl_union(mn, mx, 4);
+    shfl_union(mn, mx, 8);
+    if (t == 0 && blockIdx.x < n4) store_box(out4, blockIdx.x, mn, mx);
+}
+
+// Pyramid levels above level `in` (n boxes), `depth` of them, starting at `out`.
+__global__ void __launch_bounds__(PYR_THREADS) k_pyramid(const float4* __restrict__ in, uint32_t n,
+                                                         float4* __restrict__ out, int depth)
+{
+    const uint32_t i = blockIdx.x * PYR_THREADS + threadIdx.x;
+    float4 mn, mx;
+    empty_box(mn, mx);
+    if (i < n) {
+        mn = in[2ull * i];
+        mx = in[2ull * i + 1];
+    }
+    pyramid_up(mn, mx, n, out, depth);
+}
+
+// Sorted leaf boxes, (optionally) the reference's 64-bit keys, and (when `levels` is set) the
+// first `depth` pyramid levels above them.
+__global__ void __launch_bounds__(PYR_THREADS) k_leaves(const uint32_t* __restrict__ code,
+                                                        const uint32_t* __restrict__ order, uint32_t n,
+                                                        const float4* __restrict__ box_unsorted,
+                                                        float4* __restrict__ leaf_box, uint64_t* __restrict__ keys,
+                                                        float4* __restrict__ levels, int depth)
+{
+    const uint32_t k = blockIdx.x * PYR_THREADS + threadIdx.x;
+    float4 mn, mx;
+    empty_box(mn, mx);
+    if (k < n) {
+        const uint32_t p = order[k];
+        mn = box_unsorted[2ull * p];
+        mx = box_unsorted[2ull * p + 1];
+        leaf_box[2ull * k] = mn;
+        leaf_box[2ull * k + 1] = mx;
+        if (keys) keys[k] = ((uint64_t)code[k] << 32) | p;
+    }
+    if (levels) pyramid_up(mn, mx, n, levels, depth);
+}
+
+// Union of leaf boxes [lo, hi) (exclusive hi) from the pyramid: at each level the partial groups
+// at both ends (at most three boxes each), then up one level with the aligned middle; the last
+// level visited holds at most six boxes of the range.  All loads of a level are independent, so
+// a thread has up to six in flight at once.
+__device__ __forceinline__ void range_union(const float4* __restrict__ leaves, const float4* __restrict__ levels,
+                                            uint32_t n, int count, uint32_t lo, uint32_t hi, float4& mn, float4& mx)
+{
+    empty_box(mn, mx);
+    const float4* a = leaves;
+    const float4* next = levels;
+    uint32_t na = n;
+    for (int l = 0;; ++l) {
+        const uint32_t lo_up = (lo + 3u) & ~3u, hi_dn = hi & ~3u;
+        if (l == count || lo_up >= hi_dn) {
+#pragma unroll
+            for (uint32_t j = 0; j < 6; ++j)
+                if (lo + j < hi) box_union(mn, mx, a[2ull * (lo + j)], a[2ull * (lo + j) + 1]);
             return;
         }
-        for (uint32_t x = lo; x < lo_up; ++x) box_union(mn, mx, a[2ull * x], a[2ull * x + 1]);
-        for (uint32_t x = hi_dn; x < hi; ++x) box_union(mn, mx, a[2ull * x], a[2ull * x + 1]);
-        lo = lo_up >> 5;
-        hi = hi_dn >> 5;
-    }
-}
-
-// The same union computed by a whole warp for one range (lo and hi equal in every lane): at each
-// level the lanes load the partial blocks' boxes side by side, then one butterfly reduction.
-__device__ __forceinline__ void warp_range_union(const Levels& L, uint32_t lo, uint32_t hi, int lane, float4& mn,
-                                                 float4& mx)
-{
-    mn = make_float4(INFINITY, INFINITY, INFINITY, 0.f);
-    mx = make_float4(-INFINITY, -INFINITY, -INFINITY, 0.f);
-    for (int l = 0; l < L.count; ++l) {
-        const float4* a = L.lv[l];
-        const uint32_t lo_up = (lo + 31u) & ~31u, hi_dn = hi & ~31u;
-        const bool last = l == L.count - 1 || lo_up >= hi_dn;
-        const uint32_t lend = last ? hi : lo_up;
-        for (uint32_t x = lo + lane; x < lend; x += 32) box_union(mn, mx, a[2ull * x], a[2ull * x + 1]);
-        if (last) break;
-        for (uint32_t x = hi_dn + lane; x < hi; x += 32) box_union(mn, mx, a[2ull * x], a[2ull * x + 1]);
-        lo = lo_up >> 5;
-        hi = hi_dn >> 5;
-    }
 #pragma unroll
-    for (int o = 16; o; o >>= 1) {
-        mn.x = fminf(mn.x, __shfl_xor_sync(0xffffffffu, mn.x, o));
-        mn.y = fminf(mn.y, __shfl_xor_sync(0xffffffffu, mn.y, o));
-        mn.z = fminf(mn.z, __shfl_xor_sync(0xffffffffu, mn.z, o));
-        mx.x = fmaxf(mx.x, __shfl_xor_sync(0xffffffffu, mx.x, o));
-        mx.y = fmaxf(mx.y, __shfl_xor_sync(0xffffffffu, mx.y, o));
-        mx.z = fmaxf(mx.z, __shfl_xor_sync(0xffffffffu, mx.z, o));
+        for (uint32_t j = 0; j < 3; ++j) {
+            if (lo + j < lo_up) box_union(mn, mx, a[2ull * (lo + j)], a[2ull * (lo + j) + 1]);
+            if (hi_dn + j < hi) box_union(mn, mx, a[2ull * (hi_dn + j)], a[2ull * (hi_dn + j) + 1]);
+        }
+        lo = lo_up >> 2;
+        hi = hi_dn >> 2;
+        na = (na + 3) / 4;
+        a = next;
+        next += 2ull * na;
     }
 }
 
-// Node i's box = union of its sorted leaf range.  Ranges of up to SMALL_RANGE leaves are summed by
-// their own thread; longer ones (whose lengths differ widely between neighbouring node indices,
-// which made per-thread loops diverge) are taken one at a time by the whole warp.  Min and max
-// are exact, so the result does not depend on the grouping.
-constexpr uint32_t SMALL_RANGE = 8;
-
-__global__ void k_node_boxes(Levels L, const int2* __restrict__ range, uint32_t n_internal, float4* __restrict__ node_box)
+// Node i's box = union of its sorted leaf range (min and max are exact, so the result equals the
+// pairwise unions of the reference's bottom-up refit).
+__global__ void k_node_boxes(const float4* __restrict__ leaves, const float4* __restrict__ levels, uint32_t n,
+                             int count, const int2* __restrict__ range, float4* __restrict__ node_box)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int lane = threadIdx.x & 31;
-    const bool valid = i < n_internal;
-    uint32_t lo = 0, hi = 0;
-    if (valid) {
-        const int2 r = range[i];
-        lo = (uint32_t)r.x;
-        hi = (uint32_t)r.y + 1u;
-    }
-    const bool small = hi - lo <= SMALL_RANGE;
-    if (valid && small) {
-        float4 mn = make_float4(INFINITY, INFINITY, INFINITY, 0.f), mx = make_float4(-INFINITY, -INFINITY, -INFINITY, 0.f);
-        const float4* a = L.lv[0];
-        for (uint32_t x = lo; x < hi; ++x) box_union(mn, mx, a[2ull * x], a[2ull * x + 1]);
-        node_box[2ull * i] = mn;
-        node_box[2ull * i + 1] = mx;
-    }
-    uint32_t big = __ballot_sync(0xffffffffu, valid && !small);
-    while (big) {
-        const int src = __ffs(big) - 1;
-        big &= big - 1;
-        const uint32_t blo = __shfl_sync(0xffffffffu, lo, src), bhi = __shfl_sync(0xffffffffu, hi, src);
-        float4 mn, mx;
-        warp_range_union(L, blo, bhi, lane, mn, mx);
-        if (lane == src) {
-            node_box[2ull * i] = mn;
-            node_box[2ull * i + 1] = mx;
-        }
-    }
+    if (i >= n - 1) return;
+    const int2 r = range[i];
+    float4 mn, mx;
+    range_union(leaves, levels, n, count, (uint32_t)r.x, (uint32_t)r.y + 1u, mn, mx);
+    node_box[2ull * i] = mn;
+    node_box[2ull * i + 1] = mx;
 }
 
 // ---------------------------------------------------------------- traversal layout
@@ -699,8 +788,7 @@ inline unsigned blocks_for(uint64_t n, unsigned t) { return (unsigned)((n + t - 
 struct ScratchLayout {
     size_t code0, code1, val1, counts, totals, box_unsorted, levels, total;
     uint32_t num_tiles;
-    uint32_t level_n[MAX_LEVELS];
-    int level_count;
+    int level_count;   // pyramid levels above the leaves (0 for a single leaf)
 };
 
 ScratchLayout layout_for(uint32_t n)
@@ -711,49 +799,59 @@ ScratchLayout layout_for(uint32_t n)
     auto take = [&](size_t bytes) { size_t o = off; off = align_up(off + bytes, 256); return o; };
     L.num_tiles = (n + RS_TILE - 1) / RS_TILE;
     L.code0 = take((size_t)n * 4);
-    L.code1 = take((size_t)n * 4);
-    L.val1 = take((size_t)n * 4);
-    L.counts = take((size_t)RS_BINS * std::max(1u, L.num_tiles) * 4);
-    L.totals = take((size_t)RS_PASSES * RS_BINS * 4);
-    L.box_unsorted = take((size_t)n * 32);
-    // Block-union levels above the sorted leaf boxes: ceil(n/32), ceil(n/1024), ... down to 1.
-    uint32_t m = n;
-    L.level_count = 0;
-    size_t lv_bytes = 0;
-    while (m > 1 && L.level_count < MAX_LEVELS - 1) {
-        m = (m + 31) / 32;
-        L.level_n[L.level_count++] = m;
-        lv_bytes = align_up(lv_bytes + (size_t)m * 32, 256);
+    // The sort's second key/value buffers and its tile counts are dead once the sort has ended;
+    // the box pyramid, built after it, takes their place.
+    const size_t n4 = align_up((size_t)n * 4, 256);
+    const size_t counts = align_up((size_t)RS_BINS * std::max(1u, L.num_tiles) * 4, 256);
+    const size_t sort_bytes = 2 * n4 + counts + (size_t)RS_PASSES * RS_BINS * 4;
+    size_t lv_boxes = 0;
+    for (uint32_t m = n; m > 1;) {
+        m = (m + 3) / 4;
+        lv_boxes += m;
+        L.level_count++;
     }
-    L.levels = take(lv_bytes);
+    const size_t shared = take(std::max(sort_bytes, lv_boxes * 32));
+    L.code1 = shared;
+    L.val1 = shared + n4;
+    L.counts = shared + 2 * n4;
+    L.totals = shared + 2 * n4 + counts;
+    L.levels = shared;
+    L.box_unsorted = take((size_t)n * 32);
     L.total = off;
     return L;
 }
 
+// The pyramid above the sorted leaf boxes, from level `from` (1: the leaves' first level is
+// already in the scratch), then the node boxes.
 cpt_status refit_from_leaves(uint32_t n, const ScratchLayout& SL, char* base, const int2* range, float4* node_box,
-                             const float4* leaf_box, cudaStream_t stream)
+                             const float4* leaf_box, cudaStream_t stream, int from = 0)
 {
     if (n < 2) return CPT_OK;
-    Levels L;
-    std::memset(&L, 0, sizeof L);
-    L.lv[0] = leaf_box;
-    L.n[0] = n;
-    L.count = 1;
-    float4* lvp = (float4*)(base + SL.levels);
-    const float4* prev = leaf_box;
-    uint32_t prev_n = n;
-    for (int l = 0; l < SL.level_count; ++l) {
-        uint32_t m = SL.level_n[l];
-        k_reduce32<<<blocks_for((uint64_t)m * 32, 256), 256, 0, stream>>>(prev, prev_n, lvp, m);
-        L.lv[L.count] = lvp;
-        L.n[L.count] = m;
-        L.count++;
-        prev = lvp;
-        prev_n = m;
-        lvp = (float4*)((char*)lvp + align_up((size_t)m * 32, 256));
+    float4* levels = (float4*)(base + SL.levels);
+    // walk to level `from`
+    const float4* in = leaf_box;
+    float4* out = levels;
+    uint32_t m = n;
+    for (int l = 0; l < from; ++l) {
+        const uint32_t up = (m + 3) / 4;
+        in = out;
+        out += 2ull * up;
+        m = up;
     }
-    k_node_boxes<<<blocks_for(n - 1, 256), 256, 0, stream>>>(L, range, n - 1, node_box);
-    add_launches(SL.level_count + 1);
+    int launches = 1;
+    for (int l = from; l < SL.level_count; l += 4) {
+        const int depth = std::min(4, SL.level_count - l);
+        k_pyramid<<<blocks_for(m, PYR_THREADS), PYR_THREADS, 0, stream>>>(in, m, out, depth);
+        launches++;
+        for (int d = 0; d < depth; ++d) {
+            const uint32_t up = (m + 3) / 4;
+            in = out;
+            out += 2ull * up;
+            m = up;
+        }
+    }
+    k_node_boxes<<<blocks_for(n - 1, 256), 256, 0, stream>>>(leaf_box, levels, n, SL.level_count, range, node_box);
+    add_launches(launches);
     CPT_CUDA(cudaGetLastError());
     return CPT_OK;
 }
@@ -779,10 +877,17 @@ cpt_status lbvh_build(uint32_t n_extra, const double* extra_centroid, const floa
     if (!scratch || scratch_bytes < SL.total || ((uintptr_t)scratch & 255u))
         return fail(CPT_ERR_INVALID_ARGUMENT, "lbvh_build: scratch too small or not 256-byte aligned");
     char* base = (char*)scratch;
+    // Keys and values ping-pong between (code0, val0 = out.order) and (code1, val1); k_prep fills
+    // the pair that makes the last pass end in out.order.
     uint32_t* code0 = (uint32_t*)(base + SL.code0);
     uint32_t* code1 = (uint32_t*)(base + SL.code1);
-    uint32_t* val0 = out.order;   // the final values land in order[] after an even number of passes
+    uint32_t* val0 = out.order;
     uint32_t* val1 = (uint32_t*)(base + SL.val1);
+    constexpr bool odd = (RS_PASSES & 1) != 0;
+    uint32_t* kin = odd ? code1 : code0;
+    uint32_t* vin = odd ? val1 : val0;
+    uint32_t* kout = odd ? code0 : code1;
+    uint32_t* vout = odd ? val0 : val1;
     uint32_t* counts = (uint32_t*)(base + SL.counts);
     uint32_t* totals = (uint32_t*)(base + SL.totals);
     float4* box_unsorted = (float4*)(base + SL.box_unsorted);
@@ -811,26 +916,24 @@ cpt_status lbvh_build(uint32_t n_extra, const double* extra_centroid, const floa
     const MortonAxis ax = axis(smin.x, smax.x), ay = axis(smin.y, smax.y), az = axis(smin.z, smax.z);
     if (tri_f64)
         k_prep<double><<<blocks_for(n, 256), 256, 0, stream>>>(n_extra, extra_centroid, extra_box, n_tri, tri_f64, ax,
-                                                               ay, az, code0, val0, box_unsorted);
+                                                               ay, az, kin, vin, box_unsorted);
     else
         k_prep<float><<<blocks_for(n, 256), 256, 0, stream>>>(n_extra, extra_centroid, extra_box, n_tri, tri_f32, ax,
-                                                              ay, az, code0, val0, box_unsorted);
+                                                              ay, az, kin, vin, box_unsorted);
     CPT_CUDA(cudaGetLastError());
     add_launches(1);
     if (timings) CPT_CUDA(cudaEventRecord(ev[1], stream));
 
-    // Radix sort: 4 passes of 8 bits; keys/values ping-pong code0/val0 <-> code1/val1 and end
-    // in code0/val0 (= out.order).
+    // Radix sort: RS_PASSES passes of RS_BITS bits, ending in code0/val0 (= out.order).
     CPT_CUDA(cudaMemsetAsync(totals, 0, RS_PASSES * RS_BINS * 4, stream));
-    k_digit_totals<<<std::min(blocks_for(n, 256), 1024u), 256, 0, stream>>>(code0, n, totals);
-    uint32_t* kin = code0;
-    uint32_t* vin = val0;
-    uint32_t* kout = code1;
-    uint32_t* vout = val1;
+    k_digit_totals<<<std::min(blocks_for(n, 256), 1024u), 256, 0, stream>>>(kin, n, totals);
+    CPT_CUDA(cudaFuncSetAttribute(k_radix_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)sizeof(ScatterSmem)));
     for (int p = 0; p < RS_PASSES; ++p) {
-        k_radix_hist<<<SL.num_tiles, RS_THREADS, 0, stream>>>(kin, n, 8 * p, counts, SL.num_tiles);
+        k_radix_hist<<<SL.num_tiles, RS_THREADS, 0, stream>>>(kin, n, RS_BITS * p, counts, SL.num_tiles);
         k_radix_scan<<<RS_BINS, 256, 0, stream>>>(counts, SL.num_tiles, totals + p * RS_BINS);
-        k_radix_scatter<<<SL.num_tiles, RS_THREADS, 0, stream>>>(kin, vin, kout, vout, n, 8 * p, counts, SL.num_tiles);
+        k_radix_scatter<<<SL.num_tiles, RS_THREADS, sizeof(ScatterSmem), stream>>>(kin, vin, kout, vout, n, RS_BITS * p,
+                                                                                  counts, SL.num_tiles);
         std::swap(kin, kout);
         std::swap(vin, vout);
     }
@@ -840,12 +943,15 @@ cpt_status lbvh_build(uint32_t n_extra, const double* extra_centroid, const floa
 
     // Emission + sorted leaf boxes.
     if (n > 1) k_emit<<<blocks_for(n - 1, 256), 256, 0, stream>>>(kin, vin, (int)n, out.child, out.range);
-    k_leaves<<<blocks_for(n, 256), 256, 0, stream>>>(kin, vin, n, box_unsorted, out.leaf_box, out.keys);
+    const int depth = std::min(4, SL.level_count);
+    float4* levels = depth > 0 ? (float4*)(base + SL.levels) : nullptr;
+    k_leaves<<<blocks_for(n, PYR_THREADS), PYR_THREADS, 0, stream>>>(kin, vin, n, box_unsorted, out.leaf_box,
+                                                                    out.keys, levels, depth);
     CPT_CUDA(cudaGetLastError());
     add_launches((n > 1 ? 1 : 0) + 1);
     if (timings) CPT_CUDA(cudaEventRecord(ev[3], stream));
 
-    cpt_status st = refit_from_leaves(n, SL, base, out.range, out.node_box, out.leaf_box, stream);
+    cpt_status st = refit_from_leaves(n, SL, base, out.range, out.node_box, out.leaf_box, stream, depth);
     if (st != CPT_OK) return st;
     if (timings) {
         CPT_CUDA(cudaEventRecord(ev[4], stream));
