@@ -751,6 +751,21 @@ __global__ void k_bvh2_qnodes(const int2* __restrict__ child, const float4* __re
     nodes[2ull * i + 1] = make_float4(__uint_as_float(w0), __uint_as_float(w1), __uint_as_float(w2), __uint_as_float(split));
 }
 
+// Triangle edge b - a of FP32 vertices, rounded once from the FP64 difference.  When both are
+// normal and their exponents differ by at most 28, the difference of the two 24-bit significands
+// spans at most 53 bits, so the FP64 subtraction is exact and one FP32 subtraction rounds the same
+// exact value; so it is when either is zero.  Otherwise the FP64 sequence runs, out of line.
+__device__ __noinline__ float edge64(float b, float a) { return (float)((double)b - (double)a); }
+
+__device__ __forceinline__ float edge32(float b, float a)
+{
+    const int eb = (int)((__float_as_uint(b) >> 23) & 0xFFu), ea = (int)((__float_as_uint(a) >> 23) & 0xFFu);
+    const bool normal = eb != 0 && eb != 0xFF && ea != 0 && ea != 0xFF;
+    const bool zero = (__float_as_uint(b) << 1) == 0u || (__float_as_uint(a) << 1) == 0u;
+    const bool finite = eb != 0xFF && ea != 0xFF;
+    return ((normal && abs(eb - ea) <= 28) || (zero && finite)) ? __fsub_rn(b, a) : edge64(b, a);
+}
+
 // Leaf record k (48 bytes) for primitive order[k]:
 //   triangle: (p0, id), (p1 - p0, TRI), (p2 - p0, 0)   edges formed in double, rounded once
 //   sphere:   (centre, id), (radius, 0, 0, SPHERE), 0
@@ -771,6 +786,14 @@ __global__ void k_leaf_records(const uint32_t* __restrict__ order, uint32_t n, u
         float4 s = spheres[p - n_lights];
         r0 = make_float4(s.x, s.y, s.z, __int_as_float((int)p));
         r1 = make_float4(s.w, 0.f, 0.f, __int_as_float(CPT_KIND_SPHERE));
+    } else if (sizeof(VT) == sizeof(float)) {
+        const float* v = reinterpret_cast<const float*>(tri_v) + 9ull * (p - n_lights - n_spheres);
+        float q[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) q[k] = __ldg(v + k);
+        r0 = make_float4(q[0], q[1], q[2], __int_as_float((int)p));
+        r1 = make_float4(edge32(q[3], q[0]), edge32(q[4], q[1]), edge32(q[5], q[2]), __int_as_float(CPT_KIND_TRI));
+        r2 = make_float4(edge32(q[6], q[0]), edge32(q[7], q[1]), edge32(q[8], q[2]), 0.f);
     } else {
         double q[9];
         load_tri(tri_v, p - n_lights - n_spheres, q);

@@ -1,5 +1,6 @@
-"""The FP32 evaluation of the reference's box padding used by the LBVH prep kernel
-(csrc/lbvh.cu pad_fp32, AABB::pad AABB.cuh:30-40) restated in numpy float32, bit for bit against
+"""FP32 forms of FP64 operations in the LBVH kernels, restated in numpy float32.
+
+The box padding of the prep kernel (csrc/lbvh.cu pad_fp32, AABB::pad AABB.cuh:30-40), bit for bit against
 the FP64 sequence RD32(RN64(x - 1e-4)) / RU32(RN64(x + 1e-4)) on sweeps of float32 bit patterns.
 Values the FP32 form cannot certify take the FP64 sequence in the kernel; they are counted here and
 must not occur for coordinates of magnitude 0.01 .. 4000.  The kernel itself is checked by the
@@ -75,3 +76,25 @@ def test_pad_fp32_scene_coordinates_never_fall_back():
     mag = 10.0 ** rng.uniform(-2, np.log10(4000), 2_000_000)
     x = (mag * rng.choice([-1.0, 1.0], mag.size)).astype(np.float32)
     assert _check(x) == 0
+
+
+def test_edge_fp32_matches_fp64_difference():
+    """Triangle edges of the leaf records (csrc/lbvh.cu edge32): one FP32 subtraction where the FP64
+    difference is exact (both normal, exponents within 28, or either zero), which must equal the FP64
+    difference rounded once."""
+    rng = np.random.default_rng(9)
+    n = 2_000_000
+    a = (rng.standard_normal(n) * 10.0 ** rng.uniform(-12, 12, n)).astype(np.float32)
+    b = (rng.standard_normal(n) * 10.0 ** rng.uniform(-12, 12, n)).astype(np.float32)
+    a[::7] = 0.0
+    b[::11] = -0.0
+    ea = (a.view(np.uint32) >> 23) & 0xFF
+    eb = (b.view(np.uint32) >> 23) & 0xFF
+    normal = (ea != 0) & (ea != 255) & (eb != 0) & (eb != 255)
+    zero = ((a.view(np.uint32) << 1) == 0) | ((b.view(np.uint32) << 1) == 0)
+    fast = (normal & (np.abs(ea.astype(int) - eb.astype(int)) <= 28)) | zero
+    with np.errstate(over="ignore"):
+        got = b - a
+        ref = (b.astype(np.float64) - a.astype(np.float64)).astype(np.float32)
+    assert fast.mean() > 0.3
+    assert (got.view(np.uint32)[fast] == ref.view(np.uint32)[fast]).all()
