@@ -49,59 +49,94 @@ __device__ __forceinline__ void ref_box(int ref, const float4* node_box, const f
 
 // One level: task t is binary node tasks_in[t], whose wide node is number base + t (base = the
 // nodes of the finished levels).  Internal children are queued for the next level, whose nodes
-// start at base + n.
-__global__ void k_collapse_level(const int2* __restrict__ child, const float4* __restrict__ node_box,
-                                 const float4* __restrict__ leaf_box, const int* __restrict__ tasks_in,
-                                 const int* __restrict__ n_in, const int* __restrict__ done_levels,
-                                 int* __restrict__ tasks_out, int* __restrict__ n_out, float4* __restrict__ wide)
+// start at base + n.  The candidate children's references, boxes and areas stay in registers
+// (every array is indexed with compile-time indices only), so each box is read once: an expansion
+// costs two dependent loads (the expanded node's children, then their two boxes).
+__global__ void __launch_bounds__(128, 3) k_collapse_level(const int2* __restrict__ child,
+                                                        const float4* __restrict__ node_box,
+                                                        const float4* __restrict__ leaf_box,
+                                                        const int* __restrict__ tasks_in, const int* __restrict__ n_in,
+                                                        const int* __restrict__ done_levels,
+                                                        int* __restrict__ tasks_out, int* __restrict__ n_out,
+                                                        float4* __restrict__ wide)
 {
     const int n = *n_in;
     const int base = *done_levels;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         const int b = tasks_in[t];   // binary node
         int refs[8];
-        int2 c = child[b];
+        float4 cmn[8], cmx[8];
+        float car[8];
+        const int2 c = child[b];
+        float4 nmn, nmx;
+        ref_box(b, node_box, leaf_box, nmn, nmx);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            refs[k] = CPT_WIDE_EMPTY;
+            car[k] = -1.0f;
+        }
         refs[0] = c.x;
         refs[1] = c.y;
+        ref_box(c.x, node_box, leaf_box, cmn[0], cmx[0]);
+        ref_box(c.y, node_box, leaf_box, cmn[1], cmx[1]);
+        car[0] = area(cmn[0], cmx[0]);
+        car[1] = area(cmn[1], cmx[1]);
         int nr = 2;
-        while (nr < 8) {
-            int best = -1;
+        // Replace the internal child of largest area by its two children (the first such child in
+        // candidate order on ties) until there are 8 children or only leaves remain.
+#pragma unroll
+        for (int step = 0; step < 6; ++step) {
+            int best = -1, best_ref = 0;
             float best_a = -1.0f;
-            for (int k = 0; k < nr; ++k) {
-                if (refs[k] < 0) continue;
-                float4 mn, mx;
-                ref_box(refs[k], node_box, leaf_box, mn, mx);
-                float a = area(mn, mx);
-                if (a > best_a) {
-                    best_a = a;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                if (k < nr && refs[k] >= 0 && car[k] > best_a) {
+                    best_a = car[k];
                     best = k;
+                    best_ref = refs[k];
                 }
             }
             if (best < 0) break;
-            int2 cc = child[refs[best]];
-            refs[best] = cc.x;
-            refs[nr++] = cc.y;
+            const int2 cc = child[best_ref];
+            float4 amn, amx, bmn, bmx;
+            ref_box(cc.x, node_box, leaf_box, amn, amx);
+            ref_box(cc.y, node_box, leaf_box, bmn, bmx);
+            const float aa = area(amn, amx), ab = area(bmn, bmx);
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                if (k == best) {
+                    refs[k] = cc.x;
+                    cmn[k] = amn;
+                    cmx[k] = amx;
+                    car[k] = aa;
+                } else if (k == nr) {
+                    refs[k] = cc.y;
+                    cmn[k] = bmn;
+                    cmx[k] = bmx;
+                    car[k] = ab;
+                }
+            }
+            ++nr;
         }
-        float4 nmn, nmx;
-        ref_box(b, node_box, leaf_box, nmn, nmx);
         const float cx = 0.5f * (nmn.x + nmx.x), cy = 0.5f * (nmn.y + nmx.y), cz = 0.5f * (nmn.z + nmx.z);
-        // greedy slot assignment by direction
-        int slot_of[8];
+        // greedy slot assignment by direction: each round takes the (child, slot) pair of least cost
         float dx[8], dy[8], dz[8];
-        for (int k = 0; k < nr; ++k) {
-            float4 mn, mx;
-            ref_box(refs[k], node_box, leaf_box, mn, mx);
-            dx[k] = 0.5f * (mn.x + mx.x) - cx;
-            dy[k] = 0.5f * (mn.y + mx.y) - cy;
-            dz[k] = 0.5f * (mn.z + mx.z) - cz;
+        int slot_of[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            dx[k] = 0.5f * (cmn[k].x + cmx[k].x) - cx;
+            dy[k] = 0.5f * (cmn[k].y + cmx[k].y) - cy;
+            dz[k] = 0.5f * (cmn[k].z + cmx[k].z) - cz;
             slot_of[k] = -1;
         }
         uint32_t used = 0;
         for (int round = 0; round < nr; ++round) {
             float best = INFINITY;
             int bk = -1, bs = -1;
-            for (int k = 0; k < nr; ++k) {
-                if (slot_of[k] >= 0) continue;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                if (k >= nr || slot_of[k] >= 0) continue;
+#pragma unroll
                 for (int s = 0; s < 8; ++s) {
                     if ((used >> s) & 1u) continue;
                     float cost = -((s & 1 ? -dx[k] : dx[k]) + (s & 2 ? -dy[k] : dy[k]) + (s & 4 ? -dz[k] : dz[k]));
@@ -112,40 +147,52 @@ __global__ void k_collapse_level(const int2* __restrict__ child, const float4* _
                     }
                 }
             }
-            slot_of[bk] = bs;
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+                if (k == bk) slot_of[k] = bs;
             used |= 1u << bs;
         }
-        int at_slot[8];
-        for (int s = 0; s < 8; ++s) at_slot[s] = CPT_WIDE_EMPTY;
-        for (int k = 0; k < nr; ++k) at_slot[slot_of[k]] = refs[k];
-        // the internal children's block in the next level, in slot order
-        int n_int = 0;
-        for (int s = 0; s < 8; ++s) n_int += (at_slot[s] != CPT_WIDE_EMPTY && at_slot[s] >= 0) ? 1 : 0;
-        const int first_child = n_int ? atomicAdd(n_out, n_int) : 0;
-        int next_child = first_child;
-        uint32_t ex = grid_exponent(nmn.x, nmx.x), ey = grid_exponent(nmn.y, nmx.y), ez = grid_exponent(nmn.z, nmx.z);
-        float isx = inv_grid(ex), isy = inv_grid(ey), isz = inv_grid(ez);
-        uint32_t q[6][2];
-        for (int a = 0; a < 6; ++a) q[a][0] = q[a][1] = 0;
+        // Internal children take consecutive wide numbers in slot order: the child in slot s is
+        // number first_child + (internal children in slots below s).
         uint32_t imask = 0;
-        for (int s = 0; s < 8; ++s) {
-            int ref = at_slot[s];
-            if (ref == CPT_WIDE_EMPTY) continue;
-            float4 mn, mx;
-            ref_box(ref, node_box, leaf_box, mn, mx);
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if (k < nr && refs[k] >= 0) imask |= 1u << slot_of[k];
+        const int n_int = __popc(imask);
+        const int first_child = n_int ? atomicAdd(n_out, n_int) : 0;
+        const uint32_t ex = grid_exponent(nmn.x, nmx.x), ey = grid_exponent(nmn.y, nmx.y),
+                       ez = grid_exponent(nmn.z, nmx.z);
+        const float isx = inv_grid(ex), isy = inv_grid(ey), isz = inv_grid(ez);
+        uint32_t q[6][2];
+#pragma unroll
+        for (int a = 0; a < 6; ++a) q[a][0] = q[a][1] = 0;
+        int at_slot[8];
+#pragma unroll
+        for (int s2 = 0; s2 < 8; ++s2) at_slot[s2] = CPT_WIDE_EMPTY;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            if (k >= nr) break;
+            const int s = slot_of[k];
+            int ref = refs[k];
             if (ref >= 0) {
-                imask |= 1u << s;
-                tasks_out[next_child] = ref;
-                at_slot[s] = base + n + next_child;   // the child's wide node number
-                ++next_child;
+                const int num = first_child + __popc(imask & ((1u << s) - 1u));
+                tasks_out[num] = ref;
+                ref = base + n + num;   // the child's wide node number
             }
-            int qw = s >> 2, qs = (s & 3) * 8;
-            q[0][qw] |= q_lo(mn.x, nmn.x, isx) << qs;
-            q[1][qw] |= q_hi(mx.x, nmn.x, isx) << qs;
-            q[2][qw] |= q_lo(mn.y, nmn.y, isy) << qs;
-            q[3][qw] |= q_hi(mx.y, nmn.y, isy) << qs;
-            q[4][qw] |= q_lo(mn.z, nmn.z, isz) << qs;
-            q[5][qw] |= q_hi(mx.z, nmn.z, isz) << qs;
+#pragma unroll
+            for (int s2 = 0; s2 < 8; ++s2)
+                if (s2 == s) at_slot[s2] = ref;
+            const uint32_t sh = (uint32_t)(s & 3) * 8u;
+            const uint32_t v[6] = {q_lo(cmn[k].x, nmn.x, isx) << sh, q_hi(cmx[k].x, nmn.x, isx) << sh,
+                                   q_lo(cmn[k].y, nmn.y, isy) << sh, q_hi(cmx[k].y, nmn.y, isy) << sh,
+                                   q_lo(cmn[k].z, nmn.z, isz) << sh, q_hi(cmx[k].z, nmn.z, isz) << sh};
+#pragma unroll
+            for (int a = 0; a < 6; ++a) {
+                if (s < 4)
+                    q[a][0] |= v[a];
+                else
+                    q[a][1] |= v[a];
+            }
         }
         float4* dst = wide + CPT_WIDE_F4 * (size_t)(base + t);
         dst[0] = make_float4(nmn.x, nmn.y, nmn.z, __int_as_float((int)(ex | (ey << 8) | (ez << 16) | (imask << 24))));
@@ -153,6 +200,7 @@ __global__ void k_collapse_level(const int2* __restrict__ child, const float4* _
                              __int_as_float(at_slot[3]));
         dst[2] = make_float4(__int_as_float(at_slot[4]), __int_as_float(at_slot[5]), __int_as_float(at_slot[6]),
                              __int_as_float(at_slot[7]));
+#pragma unroll
         for (int a = 0; a < 3; ++a)
             dst[3 + a] = make_float4(__int_as_float((int)q[2 * a][0]), __int_as_float((int)q[2 * a][1]),
                                      __int_as_float((int)q[2 * a + 1][0]), __int_as_float((int)q[2 * a + 1][1]));
@@ -205,7 +253,7 @@ cpt_status build_wide(uint32_t n, const int2* child, const float4* node_box, con
     int total = 0;
     for (int level = 0; level < 72; ++level) {
         k_next_level<<<1, 1, 0, stream>>>(n_tasks + (cur ^ 1), n_tasks + 2);
-        k_collapse_level<<<std::max(1u, std::min((n + 255) / 256, 4096u)), 256, 0, stream>>>(
+        k_collapse_level<<<std::max(1u, std::min((n + 127) / 128, 8192u)), 128, 0, stream>>>(
             child, node_box, leaf_box, tasks[cur], n_tasks + cur, n_tasks + 2, tasks[cur ^ 1], n_tasks + (cur ^ 1), wide);
         add_launches(2);
         cur ^= 1;
