@@ -99,13 +99,24 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.samples)}
 
 
-class CpuReference:
-    """The reference's CPU path on a band of whole rows of the workload (its STATIC estimator,
-    1 spp, PCG32 seed 0), starting a third of the way up the image.  Runs oracle/_ref (the
-    reference's own code) where it was built, else the oracle's restatement of it, which traces
-    the same paths bit for bit (so the port's ray count is used for both)."""
+ESTIMATOR_NAMES = {0: "reference (STATIC: RR 0.7 from depth 0, no depth limit)", 1: "config"}
 
-    def __init__(self, desc, threads: int = 0):
+
+def _estimator_text(wl: dict) -> str:
+    if wl["estimator"] == 1:
+        return f"config estimator (depth <= {wl['max_depth']}, RR from depth {wl['rr_depth']} at {wl['rr_prob']})"
+    return "reference estimator (STATIC)"
+
+
+class CpuReference:
+    """The reference's bounce loop on the host cores, over a band of whole rows of the workload
+    starting a third of the way up the image, at the workload's spp and estimator and PCG32 seed 0.
+    It runs the oracle's FP64 restatement (the port), which traces the same paths as the GPU
+    integrators on the same seeds; where the estimator is the reference's own STATIC one and
+    oracle/_ref (the reference's code compiled here) was built, that runs instead, and the port's
+    ray count (bit for bit the same paths) is used for both."""
+
+    def __init__(self, desc, wl: dict, threads: int = 0):
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import oracle as O
         from cudapathtracing_gb300 import abi
@@ -113,34 +124,42 @@ class CpuReference:
         self.O, self.abi = O, abi
         self.threads = threads or os.cpu_count() or 1
         self.desc = desc
+        self.wl = dict(wl)
         self.port = O.OracleScene(desc)
-        self.ref = O.RefScene(desc) if O.ref_lib() is not None else None
+        use_ref = self.wl["estimator"] == abi.ESTIMATOR_REFERENCE and O.ref_lib() is not None
+        self.ref = O.RefScene(desc) if use_ref else None
         self.kind = "reference" if self.ref is not None else "port"
         self.r0 = desc.camera.height // 3
         self.rows = 1
         self.rays = 0
 
+    def params(self):
+        w = self.wl
+        return self.abi.render_params(spp=w["spp"], estimator=w["estimator"], max_depth=w["max_depth"],
+                                      rr_depth=w["rr_depth"], rr_prob=w["rr_prob"], seed=0, row_begin=self.r0,
+                                      row_end=self.r0 + self.rows)
+
     def _port(self):
-        prm = self.abi.render_params(spp=1, estimator=self.abi.ESTIMATOR_REFERENCE, seed=0, row_begin=self.r0,
-                                     row_end=self.r0 + self.rows)
+        prm = self.params()
         t0 = time.perf_counter()
         rays = self.port.render(prm, threads=self.threads)["rays"]
         return rays, time.perf_counter() - t0
 
     def calibrate(self, seconds: float, max_rows: int = 64) -> None:
-        """Grows the band until one run takes about `seconds`."""
+        """Sizes the band so that one run takes about `seconds` (from a one-row run)."""
         H = self.desc.camera.height
-        while True:
-            self.rays, t = self._port()
-            if t >= seconds / 2 or self.rows >= max_rows or self.r0 + 2 * self.rows > H:
-                break
-            self.rows *= 2
+        self.rows = 1
+        self.rays, t = self._port()
+        self.rows = int(max(1, min(max_rows, H - self.r0, round(seconds / max(t, 1e-3)))))
+        if self.rows > 1:
+            self.rays, _ = self._port()
 
     def run(self) -> float:
         """One timed run of the band; returns Mrays/s."""
         if self.ref is not None:
             t0 = time.perf_counter()
-            self.ref.render(1, seed=0, row_begin=self.r0, row_end=self.r0 + self.rows, threads=self.threads)
+            self.ref.render(self.wl["spp"], seed=0, row_begin=self.r0, row_end=self.r0 + self.rows,
+                            threads=self.threads)
             t = time.perf_counter() - t0
         else:
             self.rays, t = self._port()
@@ -149,33 +168,69 @@ class CpuReference:
 
     def info(self, value: float) -> dict:
         return dict(value=round(value, 4), unit="Mrays/s", cores=self.threads, kind=self.kind,
-                    sample=f"rows {self.r0}..{self.r0 + self.rows - 1} x {self.desc.camera.width} px x 1 spp of "
-                           f"the workload, reference estimator, {self.rays} rays per run")
+                    sample=f"rows {self.r0}..{self.r0 + self.rows - 1} x {self.desc.camera.width} px x "
+                           f"{self.wl['spp']} spp of the workload, {_estimator_text(self.wl)}, PCG32 seed 0, "
+                           f"{self.rays} rays per run", same_config=True, rows=[self.r0, self.r0 + self.rows])
 
 
-def cpu_reference_sample(desc, seconds: float = 15.0):
-    c = CpuReference(desc)
+def cpu_reference_sample(desc, wl: dict, seconds: float = 10.0):
+    c = CpuReference(desc, wl)
     c.calibrate(seconds)
     v = c.run()
-    info = c.info(v)
-    info["rows"] = [c.r0, c.r0 + c.rows]
-    return v, info
+    return v, c.info(v)
 
 
-def same_sample_on_gpu(scene, rows, stream, reps: int = 5) -> dict:
-    """The CPU baseline's exact sample on the GPU: the same band of rows, 1 spp, PCG32 seed 0, the
-    reference's STATIC estimator (megakernel), so the two Mrays/s figures trace the same paths."""
-    from cudapathtracing_gb300 import abi
+def cpu_trace_sample(desc, seconds: float = 8.0, seed: int = 1) -> tuple[float, dict]:
+    """Closest-hit queries on the host cores: the oracle's FP64 traversal of the reference's LBVH
+    (ordered, pruned) over the first rays of the bench's own uniform ray set, the count sized so
+    that one run takes about `seconds`."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from cudapathtracing_gb300 import procedural as P
+    O.build(ref=False)
+    threads = os.cpu_count() or 1
+    o = O.OracleScene(desc)
+    n = 1 << 16
+    rays = P.rays_as_f64(P.uniform_rays(n, seed=seed))
+    t0 = time.perf_counter()
+    o.trace(rays, threads=threads)
+    t = time.perf_counter() - t0
+    n = int(min(8_000_000, max(n, n * seconds / max(t, 1e-3))))
+    rays = P.rays_as_f64(P.uniform_rays(n, seed=seed))
+    t0 = time.perf_counter()
+    o.trace(rays, threads=threads)
+    t = time.perf_counter() - t0
+    v = n / t / 1e6
+    return v, dict(value=round(v, 4), unit="Mrays/s", cores=threads, kind="port", same_config=True,
+                   sample=f"the first {n} of the bench's uniform rays (PCG32 seed {seed}) against the same "
+                          f"{desc.num_triangles}-triangle icosphere, FP64 ordered pruned traversal")
+
+
+def reference_estimator_sample(desc, seconds: float = 6.0) -> dict:
+    """The reference's own STATIC estimator (RR 0.7 from the first bounce, no depth limit) at 1 spp
+    on a row band of the workload: the reference's integrator as it ships, beside the same-config
+    figure."""
+    c = CpuReference(desc, dict(spp=1, estimator=0, max_depth=0, rr_depth=0, rr_prob=0.7))
+    c.calibrate(seconds)
+    v = c.run()
+    return c.info(v)
+
+
+def same_sample_on_gpu(scene, wl: dict, rows, integrator: int, stream, reps: int = 3) -> dict:
+    """The CPU baseline's exact sample on the GPU: the same band of rows, spp, estimator and PCG32
+    seed 0, through the bench's integrator, so the two Mrays/s figures trace the same paths."""
     r = None
     rays, ms = 0, 0.0
     for i in range(reps + 1):
-        r = scene.render(spp=1, seed=0, estimator=abi.ESTIMATOR_REFERENCE, integrator=abi.INTEGRATOR_MEGAKERNEL,
-                         rows=tuple(rows), stream=stream, want_rgba8=False)
+        r = scene.render(spp=wl["spp"], seed=0, estimator=wl["estimator"], max_depth=wl["max_depth"],
+                         rr_depth=wl["rr_depth"], rr_prob=wl["rr_prob"], integrator=integrator, rows=tuple(rows),
+                         stream=stream, want_rgba8=False)
         if i:
             rays += r["rays"]
             ms += r["ms"]
     return {"value": round(rays / (ms / 1e3) / 1e6, 2), "unit": "Mrays/s", "rows": list(rows),
-            "rays_per_run": rays // reps, "estimator": "reference (STATIC)", "integrator": "megakernel",
+            "rays_per_run": rays // reps, "estimator": ESTIMATOR_NAMES[wl["estimator"]],
+            "integrator": "wavefront" if integrator == 1 else "megakernel",
             "timing": "device time of the render, scene resident"}
 
 
@@ -184,22 +239,37 @@ def run_reference_arm(args):
     if rank != 0:
         return
     desc = make_scene(args.workload)
-    cref = CpuReference(desc)
-    cref.calibrate(seconds=8.0, max_rows=16)
-    vals = []
-    for step in range(args.warmup + args.steps):
-        v = cref.run()
-        if step >= args.warmup:
-            vals.append(v)
-    value = float(np.mean(vals))
-    info = cref.info(value)
-    line = {"impl": "reference", "metric": "Mrays/s @1080p", "value": round(value, 4), "unit": "Mrays/s",
+    wl = dict(WORKLOADS[args.workload])
+    if args.spp > 0:
+        wl["spp"] = args.spp
+    if args.workload == "icosphere_10M":
+        vals = [cpu_trace_sample(desc, seconds=4.0)[0] for _ in range(args.warmup + args.steps)][args.warmup:]
+        value = float(np.mean(vals))
+        info = cpu_trace_sample(desc, seconds=4.0)[1]
+        info["value"] = round(value, 4)
+    else:
+        cref = CpuReference(desc, wl)
+        cref.calibrate(seconds=6.0)
+        vals = []
+        for step in range(args.warmup + args.steps):
+            v = cref.run()
+            if step >= args.warmup:
+                vals.append(v)
+        value = float(np.mean(vals))
+        info = cref.info(value)
+    metric = "Mrays/s (10M closest-hit queries, 1.31M triangles)" if args.workload == "icosphere_10M" else \
+        "Mrays/s @1080p"
+    line = {"impl": "reference", "metric": metric, "value": round(value, 4), "unit": "Mrays/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": args.workload, "width": desc.camera.width, "height": desc.camera.height,
-                       "triangles": desc.num_triangles, "sample": info["sample"]},
+                       "triangles": desc.num_triangles, "spp": wl["spp"],
+                       "estimator": ESTIMATOR_NAMES[wl["estimator"]] if wl["spp"] else None,
+                       "sample": info["sample"]},
             "cpu_baseline": info,
             "e2e": {"value": round(value, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if wl["estimator"] != 0 and wl["spp"]:
+        line["reference_estimator_sample"] = reference_estimator_sample(desc)
     print(json.dumps(line), flush=True)
 
 
@@ -492,8 +562,13 @@ def main():
     same_gpu = None
     if not args.no_cpu_baseline:
         try:
-            _, cpu = cpu_reference_sample(desc, seconds=15.0)
-            same_gpu = same_sample_on_gpu(scene, cpu["rows"], stream.cuda_stream)
+            if trace_only:
+                _, cpu = cpu_trace_sample(desc)
+            else:
+                _, cpu = cpu_reference_sample(desc, wl, seconds=10.0)
+                same_gpu = same_sample_on_gpu(scene, wl, cpu["rows"], integ, stream.cuda_stream)
+                if wl["estimator"] != 0:
+                    cpu["reference_estimator_sample"] = reference_estimator_sample(desc)
         except Exception as e:  # the baseline is reported, never required
             cpu = {"value": None, "unit": "Mrays/s", "cores": 0, "kind": "port", "sample": f"failed: {e}"}
 

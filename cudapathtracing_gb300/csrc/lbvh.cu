@@ -28,8 +28,8 @@ namespace {
 
 constexpr int RS_THREADS = 256;
 constexpr int RS_WARPS = RS_THREADS / 32;
-constexpr int RS_ITEMS = 16;
-constexpr int RS_TILE = RS_THREADS * RS_ITEMS;   // 4096 keys per tile
+constexpr int RS_ITEMS = 8;
+constexpr int RS_TILE = RS_THREADS * RS_ITEMS;   // 2048 keys per tile
 constexpr int RS_BITS = 10;
 constexpr int RS_BINS = 1 << RS_BITS;            // 1024 digits
 constexpr uint32_t RS_MASK = RS_BINS - 1;
@@ -85,13 +85,23 @@ struct MortonAxis {
 //   2. Otherwise the same in FP64 (s and min exact as in the reference, tol with 2^-48).
 //   3. Otherwise the reference's own sequence with IEEE divisions.
 // Non-finite intermediates (a degenerate axis) always take step 3.
+// floor(x) for 0 <= x < 2^23 without a conversion instruction (those share the scarce FP64
+// pipe): x + 2^23 rounded down is 2^23 + floor(x) exactly, and its low mantissa bits are the integer.
+__device__ __forceinline__ int floor_small(float x, float& f)
+{
+    const float y = __fadd_rd(x, 8388608.0f);
+    f = __fsub_rn(y, 8388608.0f);
+    return __float_as_int(y) - 0x4B000000;
+}
+
 __device__ __forceinline__ int cell_of(float x, float tol)
 {
-    if (!(tol < 0.25f) || !isfinite(x)) return -1;
+    if (!(tol < 0.25f) || !(fabsf(x) < 1e30f)) return -1;   // also rejects NaN and infinities
     if (x < 1.0f - tol) return 0;
     if (x > 1023.0f + tol) return 1023;
-    const float f = floorf(x);
-    return (x - f > tol && f + 1.0f - x > tol) ? (int)f : -1;
+    float f;
+    const int c = floor_small(x, f);   // here 1 - tol <= x <= 1023 + tol
+    return (x - f > tol && f + 1.0f - x > tol) ? c : -1;
 }
 
 __device__ __forceinline__ int cell_of(double x, double tol)
@@ -390,7 +400,7 @@ __global__ void __launch_bounds__(256) k_radix_scan(uint32_t* __restrict__ count
     }
 }
 
-// Shared memory of the scatter kernel (73,760 bytes, dynamic).
+// Shared memory of the scatter kernel (57,376 bytes, dynamic: four blocks per SM).
 struct ScatterSmem {
     uint32_t wh[RS_WARPS][RS_BINS];   // per-warp digit counts, then per-warp exclusive offsets
     uint32_t start[RS_BINS];          // tile-local start of each digit
@@ -402,7 +412,7 @@ struct ScatterSmem {
 
 // Stable scatter: rank each key within its tile (warp-ordered, lane-ordered), stage the tile
 // in shared memory in sorted order, then write runs to their global offsets.
-__global__ void __launch_bounds__(RS_THREADS, 3) k_radix_scatter(const uint32_t* __restrict__ keys_in,
+__global__ void __launch_bounds__(RS_THREADS, 4) k_radix_scatter(const uint32_t* __restrict__ keys_in,
                                                               const uint32_t* __restrict__ vals_in,
                                                               uint32_t* __restrict__ keys_out,
                                                               uint32_t* __restrict__ vals_out, uint32_t n, int shift,

@@ -1,7 +1,8 @@
 // wide.cu — collapses the binary LBVH into a compressed 8-wide BVH for traversal.
 //
-// The collapse runs level by level from the root.  Wide nodes are numbered compactly in that
-// breadth-first order: level l occupies [base_l, base_l + n_l), and the internal children of a node
+// The collapse runs level by level from the root, one launch per level with no host round trip
+// in between (the level counts and bases live on the device).  Wide nodes are numbered compactly
+// in that breadth-first order: level l occupies [base_l, base_l + n_l), and the internal children of a node
 // are numbered consecutively (one atomic per node reserves their block in the next level), so the
 // reachable nodes fill [0, num_wide) with siblings side by side and the top levels packed together
 // (the hot part of the tree stays within a few megabytes).  Leaves stay in sorted Morton order in the
@@ -47,23 +48,29 @@ __device__ __forceinline__ void ref_box(int ref, const float4* node_box, const f
 }
 
 
-// One level: task t is binary node tasks_in[t], whose wide node is number base + t (base = the
-// nodes of the finished levels).  Internal children are queued for the next level, whose nodes
-// start at base + n.  The candidate children's references, boxes and areas stay in registers
-// (every array is indexed with compile-time indices only), so each box is read once: an expansion
-// costs two dependent loads (the expanded node's children, then their two boxes).
-__global__ void __launch_bounds__(128, 3) k_collapse_level(const int2* __restrict__ child,
-                                                        const float4* __restrict__ node_box,
-                                                        const float4* __restrict__ leaf_box,
-                                                        const int* __restrict__ tasks_in, const int* __restrict__ n_in,
-                                                        const int* __restrict__ done_levels,
-                                                        int* __restrict__ tasks_out, int* __restrict__ n_out,
-                                                        float4* __restrict__ wide)
+// Level l: the wide nodes [base, base + n) with base = level_base[l], n = level_count[l]; wide node
+// w stands for binary node tasks[w].  Internal children get the next numbers in level l + 1, which
+// starts at base + n (one atomic per node reserves their consecutive block).  The candidate
+// children's references, boxes and areas stay in registers (every array is indexed with
+// compile-time indices only), so each box is read once: an expansion costs two dependent loads
+// (the expanded node's children, then their two boxes).
+constexpr int COLLAPSE_THREADS = 128;
+constexpr int MAX_WIDE_LEVELS = 80;
+
+__global__ void __launch_bounds__(COLLAPSE_THREADS, 3) k_collapse_level(const int2* __restrict__ child,
+                                                                     const float4* __restrict__ node_box,
+                                                                     const float4* __restrict__ leaf_box,
+                                                                     int* __restrict__ tasks,
+                                                                     int* __restrict__ level_count,
+                                                                     int* __restrict__ level_base, int l,
+                                                                     float4* __restrict__ wide)
 {
-    const int n = *n_in;
-    const int base = *done_levels;
+    const int n = level_count[l];
+    const int base = level_base[l];
+    if (blockIdx.x == 0 && threadIdx.x == 0) level_base[l + 1] = base + n;
+    int* n_out = level_count + l + 1;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-        const int b = tasks_in[t];   // binary node
+        const int b = tasks[base + t];   // binary node
         int refs[8];
         float4 cmn[8], cmx[8];
         float car[8];
@@ -176,8 +183,8 @@ __global__ void __launch_bounds__(128, 3) k_collapse_level(const int2* __restric
             int ref = refs[k];
             if (ref >= 0) {
                 const int num = first_child + __popc(imask & ((1u << s) - 1u));
-                tasks_out[num] = ref;
                 ref = base + n + num;   // the child's wide node number
+                tasks[ref] = refs[k];
             }
 #pragma unroll
             for (int s2 = 0; s2 < 8; ++s2)
@@ -207,27 +214,21 @@ __global__ void __launch_bounds__(128, 3) k_collapse_level(const int2* __restric
     }
 }
 
-__global__ void k_collapse_init(int* tasks, int* n_tasks)
+__global__ void k_collapse_init(int* tasks, int* level_count, int* level_base)
 {
-    tasks[0] = 0;   // the binary root is task 0 of level 0: wide node 0
-    n_tasks[0] = 1;
-    n_tasks[1] = 0;
-    n_tasks[2] = 0;   // wide nodes written by finished levels
-}
-
-// Clears the next level's queue size after adding the finished level it held to the total.
-__global__ void k_next_level(int* p, int* total)
-{
-    *total += *p;
-    *p = 0;
+    for (int i = threadIdx.x; i < MAX_WIDE_LEVELS; i += blockDim.x) {
+        level_count[i] = i == 0 ? 1 : 0;   // level 0: the root
+        level_base[i] = 0;
+    }
+    if (threadIdx.x == 0) tasks[0] = 0;   // wide node 0 stands for the binary root
 }
 
 }  // namespace
 
 size_t wide_scratch_bytes(uint32_t n)
 {
-    // two task queues of up to n entries and their counts
-    return align_up((size_t)n * 4, 256) * 2 + 256;
+    // the binary node of every wide node (at most n - 1 of them), and the level counts and bases
+    return align_up((size_t)n * 4, 256) + align_up(2 * MAX_WIDE_LEVELS * 4, 256);
 }
 
 cpt_status build_wide(uint32_t n, const int2* child, const float4* node_box, const float4* leaf_box, float4* wide,
@@ -239,39 +240,41 @@ cpt_status build_wide(uint32_t n, const int2* child, const float4* node_box, con
     }
     if (scratch_bytes < wide_scratch_bytes(n)) return fail(CPT_ERR_INVALID_ARGUMENT, "build_wide: scratch too small");
     char* p = (char*)scratch;
-    int* tasks[2];
-    tasks[0] = (int*)p;
+    int* tasks = (int*)p;
     p += align_up((size_t)n * 4, 256);
-    tasks[1] = (int*)p;
-    p += align_up((size_t)n * 4, 256);
-    int* n_tasks = (int*)p;   // [0,1] task counts, [2] wide nodes written
-    k_collapse_init<<<1, 1, 0, stream>>>(tasks[0], n_tasks);
+    int* level_count = (int*)p;
+    int* level_base = level_count + MAX_WIDE_LEVELS;
+    k_collapse_init<<<1, 128, 0, stream>>>(tasks, level_count, level_base);
     add_launches(1);
-    // Level by level; a level whose queue is empty returns at once.  The wide tree is no deeper
-    // than the binary one (at most 65 levels for 64-bit keys); check the queue every 8 levels.
-    int cur = 0;
-    int total = 0;
-    for (int level = 0; level < 72; ++level) {
-        k_next_level<<<1, 1, 0, stream>>>(n_tasks + (cur ^ 1), n_tasks + 2);
-        k_collapse_level<<<std::max(1u, std::min((n + 127) / 128, 8192u)), 128, 0, stream>>>(
-            child, node_box, leaf_box, tasks[cur], n_tasks + cur, n_tasks + 2, tasks[cur ^ 1], n_tasks + (cur ^ 1), wide);
-        add_launches(2);
-        cur ^= 1;
-        if ((level & 7) == 7) {
-            int h = 0;
-            CPT_CUDA(cudaMemcpyAsync(&h, n_tasks + cur, sizeof(int), cudaMemcpyDeviceToHost, stream));
-            CPT_CUDA(cudaStreamSynchronize(stream));
-            if (h == 0) break;
-        }
-        total++;
+    // A grid that is resident at once; each thread takes nodes of its level in turn.  The host
+    // looks at the level counts once every 16 levels (the wide tree of a few million primitives
+    // has about a dozen; a level whose count is zero returns at once).
+    static int resident = 0;
+    if (resident == 0) {
+        int dev = 0, sms = 0, per_sm = 0;
+        CPT_CUDA(cudaGetDevice(&dev));
+        CPT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        CPT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_collapse_level, COLLAPSE_THREADS, 0));
+        resident = std::max(1, sms * std::max(1, per_sm));
     }
-    CPT_CUDA(cudaGetLastError());
-    (void)total;
-    int hc[3] = {0, 0, 0};
-    CPT_CUDA(cudaMemcpyAsync(hc, n_tasks, sizeof hc, cudaMemcpyDeviceToHost, stream));
-    CPT_CUDA(cudaStreamSynchronize(stream));
-    if (hc[cur] != 0) return fail(CPT_ERR_STACK_OVERFLOW, "build_wide: collapse did not finish");
-    if (num_wide) *num_wide = (uint32_t)(hc[2] + hc[0] + hc[1]);
+    const unsigned grid = std::max(1u, std::min((n + COLLAPSE_THREADS - 1) / COLLAPSE_THREADS, (unsigned)resident));
+    int l = 0;
+    int hc[2] = {0, 0};
+    for (;;) {
+        const int first = l, stop = std::min(l + 16, MAX_WIDE_LEVELS - 1);
+        for (; l < stop; ++l)
+            k_collapse_level<<<grid, COLLAPSE_THREADS, 0, stream>>>(child, node_box, leaf_box, tasks, level_count,
+                                                                    level_base, l, wide);
+        add_launches(stop - first);
+        CPT_CUDA(cudaGetLastError());
+        // level l: its count (wide nodes still to collapse) and base (= wide nodes written)
+        CPT_CUDA(cudaMemcpyAsync(&hc[0], level_count + l, sizeof(int), cudaMemcpyDeviceToHost, stream));
+        CPT_CUDA(cudaMemcpyAsync(&hc[1], level_base + l, sizeof(int), cudaMemcpyDeviceToHost, stream));
+        CPT_CUDA(cudaStreamSynchronize(stream));
+        if (hc[0] == 0 || l >= MAX_WIDE_LEVELS - 1) break;
+    }
+    if (hc[0] != 0) return fail(CPT_ERR_STACK_OVERFLOW, "build_wide: collapse did not finish");
+    if (num_wide) *num_wide = (uint32_t)hc[1];
     return CPT_OK;
 }
 

@@ -1336,9 +1336,14 @@ ORC_API uint64_t orc_render(void* p, const cpt_render_params* prm, double* rgb, 
     int r0 = prm->row_begin, r1 = prm->row_end;
     if (r0 == 0 && r1 == 0) r1 = s.height;
     std::atomic<uint64_t> total(0);
-    parallelRows(r0, r1, threads, [&](int j) {
+    // pixels of the band in chunks of 16, so that a band of few rows still uses every thread
+    const int64_t npix = (int64_t)(r1 > r0 ? r1 - r0 : 0) * s.width;
+    const int chunk = 16;
+    parallelRows(0, (int)((npix + chunk - 1) / chunk), threads, [&](int chunk_id) {
         uint64_t local = 0;
-        for (int i = 0; i < s.width; ++i) {
+        const int64_t p_end = std::min<int64_t>(npix, (int64_t)(chunk_id + 1) * chunk);
+        for (int64_t q = (int64_t)chunk_id * chunk; q < p_end; ++q) {
+            const int j = r0 + (int)(q / s.width), i = (int)(q % s.width);
             PixelOut o = ref ? renderPixelReference(s, i, j, prm->spp, prm->seed) : renderPixelConfig(s, i, j, *prm);
             size_t off = (size_t)j * s.width + i;
             rgb[3 * off] = o.rgb.x;
