@@ -251,3 +251,35 @@ def test_barrier_wait_limit_reports_timeout(ctx):
     net.check()
     want = K.Net(net.params).forward(rgb, g)
     assert (np.abs(out - want) / np.maximum(1.0, np.abs(want))).max() < 1e-3
+
+
+@pytest.mark.parametrize("k", range(8))
+def test_denoise_eval_reference_is_the_fp64_oracle_render(ctx, oracle_mod, k):
+    """The wall-time-to-RMSE evaluation (bench.py denoise, training.evaluate) measures RMSE against
+    the library's own high-spp render of each held-out 512x512 scene.  On the same PCG32 streams that
+    render equals the FP64 oracle's: here a 4-row band at 64 spp with the evaluation's estimator and
+    the reference's seed, through the evaluation's integrator (wavefront).  Every pixel within
+    2e-3 * max(1, ref) of the oracle on at least 99% of pixels, and the display-space RMSE between the
+    two (the quantity the evaluation thresholds at 0.01) below 1e-3.  By the triangle inequality an
+    RMSE against the library's reference is then within 1e-3 of the RMSE against the oracle's (less at
+    the evaluation's 16384 spp, where a path that FP32 and FP64 round apart weighs 1/16384)."""
+    import torch
+    from cudapathtracing_gb300 import abi, api, procedural as P, training as T
+    d = P.random_scene(T.EVAL_SEED0 + k, width=512)
+    s = api.Scene(ctx, d).init()
+    rows = (200, 204)
+    prm = dict(spp=64, seed=18, **T.RENDER)
+    rgb = torch.zeros((s.height, s.width, 3), device="cuda")
+    s.render(integrator=abi.INTEGRATOR_WAVEFRONT, rows=rows, rgb=rgb, **prm)
+    torch.cuda.synchronize()
+    g = rgb.cpu().numpy()[rows[0]:rows[1]].astype(np.float64)
+    o = oracle_mod.OracleScene(d).render(abi.render_params(row_begin=rows[0], row_end=rows[1], **prm))
+    r = o["rgb"][rows[0]:rows[1]]
+    assert np.isfinite(g).all()
+    ok = (np.abs(g - r) <= 2e-3 * np.maximum(1.0, np.abs(r))).all(-1)
+    disp = lambda x: np.minimum(np.sqrt(np.maximum(x, 0.0)), 1.0)   # noqa: E731
+    drmse = float(np.sqrt(((disp(g) - disp(r)) ** 2).mean()))
+    print(f"scene {k}: match {ok.mean():.5f}, display RMSE vs oracle {drmse:.2e}")
+    assert ok.mean() >= 0.99, ok.mean()
+    assert drmse < 1e-3, drmse
+    s.close()
