@@ -28,8 +28,8 @@ namespace {
 
 constexpr int RS_THREADS = 256;
 constexpr int RS_WARPS = RS_THREADS / 32;
-constexpr int RS_ITEMS = 8;
-constexpr int RS_TILE = RS_THREADS * RS_ITEMS;   // 2048 keys per tile
+constexpr int RS_ITEMS = 16;
+constexpr int RS_TILE = RS_THREADS * RS_ITEMS;   // 4096 keys per tile
 constexpr int RS_BITS = 10;
 constexpr int RS_BINS = 1 << RS_BITS;            // 1024 digits
 constexpr uint32_t RS_MASK = RS_BINS - 1;
@@ -113,10 +113,12 @@ __device__ __forceinline__ int cell_of(double x, double tol)
     return (x - f > tol && f + 1.0 - x > tol) ? (int)f : -1;
 }
 
-// Steps 2 and 3.  Out of line, so that the compiler cannot evaluate them speculatively beside the
-// FP32 step: they run for a fraction of a percent of the coordinates.
-__device__ __noinline__ uint32_t morton_tri_axis_fp64(double a, double b, double c, MortonAxis m)
+// Steps 2 and 3.  Out of line, with the widening inside, so that the compiler cannot evaluate any
+// of it speculatively beside the FP32 step: they run for a fraction of a percent of the coordinates.
+template <typename VT>
+__device__ __noinline__ uint32_t morton_tri_axis_fp64(VT a_, VT b_, VT c_, MortonAxis m)
 {
+    const double a = (double)a_, b = (double)b_, c = (double)c_;
     const double s = __dadd_rn(__dadd_rn(a, b), c);   // the reference's sum
     const double x64 = __dmul_rn(__dsub_rn(__dmul_rn(s, 1.0 / 3.0), m.mn), m.k64);
     const double tol64 = 0x1p-48 * (m.k64 * (fabs(s) + fabs(m.mn)) + 2.0 * fabs(x64));
@@ -134,7 +136,7 @@ __device__ __forceinline__ uint32_t morton_tri_axis(VT a, VT b, VT c, const Mort
     const float tol32 = 0x1p-20f * (m.k32 * mag + 2.0f * fabsf(x32));
     const int cell = cell_of(x32, tol32);
     if (cell >= 0) return (uint32_t)cell;
-    return morton_tri_axis_fp64((double)a, (double)b, (double)c, m);
+    return morton_tri_axis_fp64<VT>(a, b, c, m);
 }
 
 // Triangle centroid and padded box (Hittable.cuh:459-461, AABB.cuh:30-40), boxes rounded
@@ -400,7 +402,7 @@ __global__ void __launch_bounds__(256) k_radix_scan(uint32_t* __restrict__ count
     }
 }
 
-// Shared memory of the scatter kernel (57,376 bytes, dynamic: four blocks per SM).
+// Shared memory of the scatter kernel (73,760 bytes, dynamic: three blocks per SM).
 struct ScatterSmem {
     uint32_t wh[RS_WARPS][RS_BINS];   // per-warp digit counts, then per-warp exclusive offsets
     uint32_t start[RS_BINS];          // tile-local start of each digit
@@ -412,7 +414,7 @@ struct ScatterSmem {
 
 // Stable scatter: rank each key within its tile (warp-ordered, lane-ordered), stage the tile
 // in shared memory in sorted order, then write runs to their global offsets.
-__global__ void __launch_bounds__(RS_THREADS, 4) k_radix_scatter(const uint32_t* __restrict__ keys_in,
+__global__ void __launch_bounds__(RS_THREADS, 3) k_radix_scatter(const uint32_t* __restrict__ keys_in,
                                                               const uint32_t* __restrict__ vals_in,
                                                               uint32_t* __restrict__ keys_out,
                                                               uint32_t* __restrict__ vals_out, uint32_t n, int shift,
@@ -497,17 +499,23 @@ __global__ void __launch_bounds__(RS_THREADS, 4) k_radix_scatter(const uint32_t*
 }
 
 // ---------------------------------------------------------------- Karras emission
-__device__ __forceinline__ uint64_t key_at(const uint32_t* __restrict__ code, const uint32_t* __restrict__ order, int j)
+// The reference's keys are code << 32 | primitive (Device.cuh:187-189), so the length of the common
+// prefix of keys i and j (delta, BVH.cuh:120-128) is clz(code_i ^ code_j) when the codes differ and
+// 32 + clz(prim_i ^ prim_j) when they are equal: the primitive word is read only then.
+__device__ __forceinline__ int prefix_len(uint32_t ci, uint32_t oi, const uint32_t* __restrict__ code,
+                                          const uint32_t* __restrict__ order, int j)
 {
-    return ((uint64_t)code[j] << 32) | (uint64_t)order[j];
+    const uint32_t cj = code[j];
+    if (cj != ci) return __clz(ci ^ cj);
+    const uint32_t oj = order[j];
+    return oi == oj ? 64 : 32 + __clz(oi ^ oj);
 }
 
-__device__ __forceinline__ int delta_k(const uint32_t* code, const uint32_t* order, int n, uint64_t ki, int j)   // BVH.cuh:120-128
+__device__ __forceinline__ int delta_k(const uint32_t* code, const uint32_t* order, int n, uint32_t ci, uint32_t oi,
+                                       int j)   // BVH.cuh:120-128
 {
     if (j < 0 || j >= n) return -1;
-    uint64_t kj = key_at(code, order, j);
-    if (ki == kj) return 64;
-    return __clzll((long long)(ki ^ kj));
+    return prefix_len(ci, oi, code, order, j);
 }
 
 __global__ void k_emit(const uint32_t* __restrict__ code, const uint32_t* __restrict__ order, int n,
@@ -516,32 +524,33 @@ __global__ void k_emit(const uint32_t* __restrict__ code, const uint32_t* __rest
     int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= n - 1) return;
     // determineRange (BVH.cuh:130-172)
-    uint64_t ki = key_at(code, order, idx);
-    int dn = delta_k(code, order, n, ki, idx + 1);
-    int dp = delta_k(code, order, n, ki, idx - 1);
+    const uint32_t ci = code[idx], oi = order[idx];
+    int dn = delta_k(code, order, n, ci, oi, idx + 1);
+    int dp = delta_k(code, order, n, ci, oi, idx - 1);
     int d = (dn > dp) ? 1 : -1;
-    int dmin_ = delta_k(code, order, n, ki, idx - d);
+    int dmin_ = delta_k(code, order, n, ci, oi, idx - d);
     int lmax = 2;
-    while (delta_k(code, order, n, ki, idx + lmax * d) > dmin_) lmax *= 2;
+    while (delta_k(code, order, n, ci, oi, idx + lmax * d) > dmin_) lmax *= 2;
     int l = 0;
     for (int t = lmax / 2; t >= 1; t /= 2)
-        if (delta_k(code, order, n, ki, idx + (l + t) * d) > dmin_) l += t;
+        if (delta_k(code, order, n, ci, oi, idx + (l + t) * d) > dmin_) l += t;
     int j = idx + l * d;
     int first = min(idx, j), last = max(idx, j);
-    // findSplit (BVH.cuh:81-118)
-    uint64_t fc = key_at(code, order, first), lc = key_at(code, order, last);
+    // findSplit (BVH.cuh:81-118): equal keys split in the middle, otherwise binary search for the
+    // last position that shares more than the range's common prefix with the first key
+    const uint32_t cf = code[first], of = order[first];
+    const int common = prefix_len(cf, of, code, order, last);
     int split;
-    if (fc == lc) {
+    if (common == 64) {
         split = (first + last) >> 1;
     } else {
-        int common = __clzll((long long)(fc ^ lc));
         split = first;
         int step = last - first;
         do {
             step = (step + 1) >> 1;
             int ns = split + step;
             if (ns < last) {
-                if (__clzll((long long)(fc ^ key_at(code, order, ns))) > common) split = ns;
+                if (prefix_len(cf, of, code, order, ns) > common) split = ns;
             }
         } while (step > 1);
     }
@@ -962,6 +971,10 @@ cpt_status lbvh_build(uint32_t n_extra, const double* extra_centroid, const floa
     k_digit_totals<<<std::min(blocks_for(n, 256), 1024u), 256, 0, stream>>>(kin, n, totals);
     CPT_CUDA(cudaFuncSetAttribute(k_radix_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)sizeof(ScatterSmem)));
+    CPT_CUDA(cudaFuncSetAttribute(k_radix_scatter, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                  cudaSharedmemCarveoutMaxShared));
+    CPT_CUDA(cudaFuncSetAttribute(k_radix_hist, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                  cudaSharedmemCarveoutMaxShared));
     for (int p = 0; p < RS_PASSES; ++p) {
         k_radix_hist<<<SL.num_tiles, RS_THREADS, 0, stream>>>(kin, n, RS_BITS * p, counts, SL.num_tiles);
         k_radix_scan<<<RS_BINS, 256, 0, stream>>>(counts, SL.num_tiles, totals + p * RS_BINS);
