@@ -325,7 +325,7 @@ __global__ void k_wf_finish(JobGeo jg, RenderArgs a, int groups)
 // At most 48 registers (5 blocks of 256 per SM): 62 % occupancy instead of 50 % for a few spilled
 // values, +5.7 % on the 1080p spheres render (the shadow kernel is faster uncapped).
 template <bool WIDE, int SHORT, bool SORT, bool MULTI>
-__global__ void __launch_bounds__(256, WIDE ? 3 : 5) k_wf_trace(const __grid_constant__ SceneView s, Wf w, int par)
+__global__ void __launch_bounds__(256, WIDE ? 4 : 5) k_wf_trace(const __grid_constant__ SceneView s, Wf w, int par)
 {
     const int n = w.cnt[par];
     const int nq = par ^ 1;

@@ -342,7 +342,8 @@ def random_scene(seed: int, width: int = 256, aspect: float = 1.0, max_level: in
     icospheres in [1, max_objects]; per sphere a subdivision level in [4, max_level], radius
     [0.4, 1.4], position x, z in [-4, 4] resting on the ground, a noise offset, a colour, and a
     material (Lambertian / GGX with roughness U[0.05, 0.8] / dielectric IOR 1.5, equal odds);
-    with odds 0.3 a homogeneous volume box (sigma_t U[0.3, 1.0], albedo 0.8); one or two area
+    with odds 0.3 a homogeneous volume box (sigma_t U[0.3, 1.0], albedo 0.8; side 2, its bottom
+    0.01 above the ground); one or two area
     lights 8-12 units up (side 2-4, radiance 8-20); a camera orbiting at distance 8-12, height
     1.5-6, looking at (0, 0.8, 0) with a 35-50 degree field of view.  Ground: [-30, 30]^2 at y = 0."""
     g = PCG32Streams(seed, np.array([0], dtype=np.uint64))
@@ -372,7 +373,9 @@ def random_scene(seed: int, width: int = 256, aspect: float = 1.0, max_level: in
         mats.extend([m] * t.shape[0])
     if u() < 0.3:
         vol = d.add_material((1.0, 1.0, 1.0), 0.5, 0.5, M_VOLUME, sigma_t=0.3 + 0.7 * u(), albedo=0.8)
-        c = (u() * 6.0 - 3.0, 1.0, u() * 6.0 - 3.0)
+        # 0.01 above the ground: a bottom face coplanar with the ground would make every ground hit
+        # inside the box's footprint a tie between two triangles at the same distance
+        c = (u() * 6.0 - 3.0, 1.01, u() * 6.0 - 3.0)
         for q in _box_quads(c, (2.0, 2.0, 2.0), 360.0 * u()):
             for t in _quad(*q):
                 parts.append(np.asarray(t, np.float64)[None, :])
