@@ -85,13 +85,20 @@ struct MortonAxis {
 //   2. Otherwise the same in FP64 (s and min exact as in the reference, tol with 2^-48).
 //   3. Otherwise the reference's own sequence with IEEE divisions.
 // Non-finite intermediates (a degenerate axis) always take step 3.
-// floor(x) for 0 <= x < 2^23 without a conversion instruction (those share the scarce FP64
-// pipe): x + 2^23 rounded down is 2^23 + floor(x) exactly, and its low mantissa bits are the integer.
+// floor(x) for 0 <= x < 2^23 on the integer units, without conversion or directed-rounding
+// instructions: f = x with its fractional mantissa bits cleared, and the integer from the
+// significand shifted by the exponent.
 __device__ __forceinline__ int floor_small(float x, float& f)
 {
-    const float y = __fadd_rd(x, 8388608.0f);
-    f = __fsub_rn(y, 8388608.0f);
-    return __float_as_int(y) - 0x4B000000;
+    const uint32_t b = __float_as_uint(x);
+    const int e = (int)(b >> 23) - 127;
+    if (e < 0) {
+        f = 0.0f;
+        return 0;
+    }
+    const uint32_t sh = 23u - (uint32_t)e;
+    f = __uint_as_float(b & ~((1u << sh) - 1u));
+    return (int)(((b & 0x7FFFFFu) | 0x800000u) >> sh);
 }
 
 __device__ __forceinline__ int cell_of(float x, float tol)
