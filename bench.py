@@ -538,10 +538,17 @@ def main():
     k_ms = float(np.mean(kernel_ms))
     rays_per_launch = rays / world / args.steps
     achieved = rays_per_launch * bpr / (k_ms / 1e3) / 1e9
+    # DRAM bytes per launch from the committed ncu capture: measured bytes per traced ray of the
+    # integrator (every launch of a 2-spp render, one-pass metrics) times this run's rays per launch
     traffic = None
     tpath = os.path.join(ROOT, "profiles", f"traffic_{args.workload}.json")
     if os.path.exists(tpath):
-        traffic = json.load(open(tpath)).get("bytes_per_launch")
+        tj = json.load(open(tpath))
+        src = tj.get("megakernel", {}) if args.integrator == "megakernel" else tj
+        if "bytes_per_ray" in src:
+            traffic = int(src["bytes_per_ray"] * rays_per_launch)
+        else:
+            traffic = src.get("bytes_per_launch")
 
     # second half of the metric: wall time to display-space RMSE 0.01, denoised vs plain spp
     denoise = None
