@@ -81,8 +81,10 @@ class Choice:
         return Choice(knobs=knobs, score=d["score"], default_score=d["default_score"], trials=d.get("trials", []))
 
 
-def workload_key(device: dict, scene, params: dict, integrator: int) -> str:
-    """scene: anything with num_triangles, num_spheres, num_lights, width, height (api.Scene)."""
+def workload_key(device: dict, scene, params: dict, integrator: int, probe_spp: int = 0) -> str:
+    """scene: anything with num_triangles, num_spheres, num_lights, width, height (api.Scene).
+    probe_spp: the samples per pixel the choice was timed at (the best slot count depends on the
+    number of items, which grows with it)."""
     sig = {
         "device": device,
         "triangles": int(scene.num_triangles),
@@ -93,6 +95,7 @@ def workload_key(device: dict, scene, params: dict, integrator: int) -> str:
         "estimator": int(params.get("estimator", abi.ESTIMATOR_REFERENCE)),
         "max_depth": int(params.get("max_depth", 0)),
         "rr_depth": int(params.get("rr_depth", 0)),
+        "probe_spp": int(probe_spp),
     }
     return hashlib.sha1(json.dumps(sig, sort_keys=True).encode()).hexdigest()[:16]
 
@@ -183,7 +186,7 @@ class Autotuner:
 
     def tune(self, scene, params: dict, integrator: int = abi.INTEGRATOR_WAVEFRONT, retune: bool = False) -> Choice:
         """Returns the choice for this workload (from the cache unless retune) and applies it."""
-        key = workload_key(self.device_info(), scene, params, integrator)
+        key = workload_key(self.device_info(), scene, params, integrator, self.probe_spp)
         cache = load_cache(self.cache_path)
         if key in cache and not retune:
             ch = Choice.from_json(cache[key])

@@ -66,25 +66,15 @@ __device__ __forceinline__ void load_tri(const VT* __restrict__ v, uint32_t t, d
     for (int k = 0; k < 9; ++k) p[k] = (double)v[9ull * t + k];
 }
 
-// Constants of the fast Morton path for one axis: the reference's bounds and the scale
-// k = 1024 / (max - min) in FP64 and FP32.
+// Constants of the fast Morton paths for one axis: the reference's bounds, the scale
+// k = 1024 / (max - min) in FP64, and min and k as FP32 (hi) and as unevaluated FP32 pairs
+// (hi + lo, within 2^-48 relative of the FP64 values).
 struct MortonAxis {
     double mn, mx, k64;
-    float mn32, k32;
+    float mn32, k32;      // RN32(min), RN32(k)
+    float mn_lo, k_lo;    // RN32(min - mn32), RN32(k - k32)
 };
 
-// Morton cell of a triangle-centroid coordinate, equal to the reference's exactly rounded FP64
-// sequence morton_axis(RN((p0 + p1 + p2) / 3), min, max) (BVH.cuh:23-33 on the centroid of
-// Hittable.cuh:459-461), computed without its two FP64 divisions where that is provably safe:
-//   1. FP32: x = (s * (1/3) - min) * k with s = p0 + p1 + p2.  Its distance to the reference's
-//      x is below tol = 2^-20 (k (|p0| + |p1| + |p2| + |min| + |x / k|) + |x|), four times the
-//      worst-case sum of the rounding errors (conversions, two additions, the multiplications
-//      and the rounded 1/3 and k, each at most 2^-24 relative).  The cell is floor(x) when x is
-//      farther than tol from every cell boundary (the integers 1 .. 1023; below 1 the cell is 0,
-//      at or above 1023 it is 1023).
-//   2. Otherwise the same in FP64 (s and min exact as in the reference, tol with 2^-48).
-//   3. Otherwise the reference's own sequence with IEEE divisions.
-// Non-finite intermediates (a degenerate axis) always take step 3.
 // floor(x) for 0 <= x < 2^23 on the integer units, without conversion or directed-rounding
 // instructions: f = x with its fractional mantissa bits cleared, and the integer from the
 // significand shifted by the exponent.
@@ -101,6 +91,20 @@ __device__ __forceinline__ int floor_small(float x, float& f)
     return (int)(((b & 0x7FFFFFu) | 0x800000u) >> sh);
 }
 
+// Morton cell of a triangle-centroid coordinate, equal to the reference's exactly rounded FP64
+// sequence morton_axis(RN((p0 + p1 + p2) / 3), min, max) (BVH.cuh:23-33 on the centroid of
+// Hittable.cuh:459-461), computed without its two FP64 divisions where that is provably safe:
+//   1. FP32: x = (s * (1/3) - min) * k with s = p0 + p1 + p2.  Its distance to the reference's
+//      x is below tol = 2^-20 (k (|p0| + |p1| + |p2| + |min|) + 2 |x|), four times the worst-case
+//      sum of the rounding errors (two additions, the multiplications and the rounded 1/3 and
+//      k, each at most 2^-24 relative).  The cell is floor(x) when x is farther than tol from
+//      every cell boundary (the integers 1 .. 1023; below 1 the cell is 0, at or above 1023 it
+//      is 1023).
+//   2. Otherwise the same in unevaluated pairs of FP32 numbers (TwoSum and FMA-based TwoProd,
+//      about 44 significant bits), with tol = 2^-40 (...): still on the FP32 units, whereas one
+//      lane on an FP64 path costs its whole warp the part's low FP64 issue rate.
+//   3. Otherwise the reference's own sequence with IEEE divisions, in FP64.
+// Non-finite intermediates (a degenerate axis) always take step 3.
 __device__ __forceinline__ int cell_of(float x, float tol)
 {
     if (!(tol < 0.25f) || !(fabsf(x) < 1e30f)) return -1;   // also rejects NaN and infinities
@@ -111,27 +115,69 @@ __device__ __forceinline__ int cell_of(float x, float tol)
     return (x - f > tol && f + 1.0f - x > tol) ? c : -1;
 }
 
-__device__ __forceinline__ int cell_of(double x, double tol)
-{
-    if (!(tol < 0.25) || !isfinite(x)) return -1;
-    if (x < 1.0 - tol) return 0;
-    if (x > 1023.0 + tol) return 1023;
-    const double f = floor(x);
-    return (x - f > tol && f + 1.0 - x > tol) ? (int)f : -1;
-}
-
-// Steps 2 and 3.  Out of line, with the widening inside, so that the compiler cannot evaluate any
-// of it speculatively beside the FP32 step: they run for a fraction of a percent of the coordinates.
+// Step 3.  Out of line, with the widening inside, so that the compiler cannot evaluate any of it
+// speculatively beside the FP32 steps.
 template <typename VT>
 __device__ __noinline__ uint32_t morton_tri_axis_fp64(VT a_, VT b_, VT c_, MortonAxis m)
 {
     const double a = (double)a_, b = (double)b_, c = (double)c_;
-    const double s = __dadd_rn(__dadd_rn(a, b), c);   // the reference's sum
-    const double x64 = __dmul_rn(__dsub_rn(__dmul_rn(s, 1.0 / 3.0), m.mn), m.k64);
-    const double tol64 = 0x1p-48 * (m.k64 * (fabs(s) + fabs(m.mn)) + 2.0 * fabs(x64));
-    const int cell = cell_of(x64, tol64);
-    if (cell >= 0) return (uint32_t)cell;
-    return morton_axis(__ddiv_rn(s, 3.0), m.mn, m.mx);
+    return morton_axis(__ddiv_rn(__dadd_rn(__dadd_rn(a, b), c), 3.0), m.mn, m.mx);
+}
+
+// Error-free transformations on FP32 (Knuth's TwoSum; the product's error from one FMA).
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e)
+{
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+__device__ __forceinline__ void two_prod(float a, float b, float& p, float& e)
+{
+    p = __fmul_rn(a, b);
+    e = __fmaf_rn(a, b, -p);
+}
+
+constexpr float THIRD_HI = 0x1.555556p-2f;    // RN32(1/3)
+constexpr float THIRD_LO = -0x1.555556p-27f;  // RN32(1/3 - THIRD_HI); the rest is below 2^-50
+
+// Step 2 (and 3 where it cannot decide).  Out of line: it runs for a fraction of a percent of the
+// coordinates.
+__device__ __noinline__ uint32_t morton_tri_axis_ff(float a, float b, float c, MortonAxis m)
+{
+    // s = a + b + c as hi + lo
+    float s1, e1, s2, e2;
+    two_sum(a, b, s1, e1);
+    two_sum(s1, c, s2, e2);
+    const float slo = __fadd_rn(e1, e2);
+    // y = s / 3
+    float y, ye;
+    two_prod(s2, THIRD_HI, y, ye);
+    ye = __fadd_rn(ye, __fadd_rn(__fmul_rn(s2, THIRD_LO), __fmul_rn(slo, THIRD_HI)));
+    // z = y - min
+    float z, ze;
+    two_sum(y, -m.mn32, z, ze);
+    ze = __fadd_rn(ze, __fsub_rn(ye, m.mn_lo));
+    // x = z * k
+    float x, xe;
+    two_prod(z, m.k32, x, xe);
+    xe = __fadd_rn(xe, __fadd_rn(__fmul_rn(z, m.k_lo), __fmul_rn(ze, m.k32)));
+    const float mag = fabsf(a) + fabsf(b) + fabsf(c) + fabsf(m.mn32);
+    const float tol = 0x1p-40f * (m.k32 * mag + 2.0f * fabsf(x));
+    if (isfinite(x) && isfinite(xe) && isfinite(tol) && tol < 0.25f) {
+        const float xs = __fadd_rn(x, xe);
+        if (xs < 1.0f - tol) return 0u;
+        if (xs > 1023.0f + tol) return 1023u;
+        float f;
+        const int cell = floor_small(fminf(fmaxf(x, 0.0f), 1024.0f), f);
+        // signed distances of x + xe above floor(x) and below floor(x) + 1 (x - f and f + 1 - x are
+        // exact); xe can move the sum across either integer
+        const float below = __fadd_rn(__fsub_rn(x, f), xe), above = __fsub_rn(__fsub_rn(__fadd_rn(f, 1.0f), x), xe);
+        if (below > tol && above > tol) return (uint32_t)min(cell, 1023);
+        if (below < -tol && cell >= 1) return (uint32_t)min(cell - 1, 1023);
+        if (above < -tol) return (uint32_t)min(cell + 1, 1023);
+    }
+    return morton_tri_axis_fp64<float>(a, b, c, m);
 }
 
 template <typename VT>
@@ -143,7 +189,7 @@ __device__ __forceinline__ uint32_t morton_tri_axis(VT a, VT b, VT c, const Mort
     const float tol32 = 0x1p-20f * (m.k32 * mag + 2.0f * fabsf(x32));
     const int cell = cell_of(x32, tol32);
     if (cell >= 0) return (uint32_t)cell;
-    return morton_tri_axis_fp64<VT>(a, b, c, m);
+    return morton_tri_axis_ff(a32, b32, c32, m);
 }
 
 // Triangle centroid and padded box (Hittable.cuh:459-461, AABB.cuh:30-40), boxes rounded
@@ -960,6 +1006,8 @@ cpt_status lbvh_build(uint32_t n_extra, const double* extra_centroid, const floa
         m.k64 = 1024.0 / (mx - mn);
         m.mn32 = (float)mn;
         m.k32 = (float)m.k64;
+        m.mn_lo = (float)(mn - (double)m.mn32);
+        m.k_lo = (float)(m.k64 - (double)m.k32);
         return m;
     };
     const MortonAxis ax = axis(smin.x, smax.x), ay = axis(smin.y, smax.y), az = axis(smin.z, smax.z);

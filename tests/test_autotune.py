@@ -49,6 +49,7 @@ def test_cache_round_trip_and_key_stability(tmp_path):
     k1 = T.workload_key(dev, scene, prm, abi.INTEGRATOR_WAVEFRONT)
     assert k1 == T.workload_key(dev, scene, dict(prm), abi.INTEGRATOR_WAVEFRONT)
     assert k1 != T.workload_key(dev, scene, prm, abi.INTEGRATOR_MEGAKERNEL)
+    assert k1 != T.workload_key(dev, scene, prm, abi.INTEGRATOR_WAVEFRONT, probe_spp=2)   # timed at other spp
     scene.width = 65
     assert k1 != T.workload_key(dev, scene, prm, abi.INTEGRATOR_WAVEFRONT)
     assert T.load_cache(str(tmp_path / "missing.json")) == {}

@@ -98,3 +98,88 @@ def test_edge_fp32_matches_fp64_difference():
         ref = (b.astype(np.float64) - a.astype(np.float64)).astype(np.float32)
     assert fast.mean() > 0.3
     assert (got.view(np.uint32)[fast] == ref.view(np.uint32)[fast]).all()
+
+
+THIRD_HI = np.float32(float.fromhex("0x1.555556p-2"))
+THIRD_LO = np.float32(float.fromhex("-0x1.555556p-27"))
+
+
+def _morton_ref(a, b, c, mn, mx):
+    """The reference's FP64 sequence (BVH.cuh:23-33 on the centroid, Hittable.cuh:459-461)."""
+    s = (a.astype(np.float64) + b) + c
+    cen = s / 3.0
+    with np.errstate(invalid="ignore"):
+        x = (cen - mn) / (mx - mn) * 1024.0
+    x = np.where(x > 0.0, x, 0.0)
+    x = np.where(x < 1023.0, x, 1023.0)
+    return x.astype(np.int64)
+
+
+def _two_sum(a, b):
+    s = a + b
+    bb = s - a
+    return s, (a - (s - bb)) + (b - bb)
+
+
+def _two_prod(a, b):
+    p = a * b
+    return p, (a.astype(np.float64) * b.astype(np.float64) - p.astype(np.float64)).astype(np.float32)
+
+
+def _morton_ff(a, b, c, mn, mx):
+    """csrc/lbvh.cu morton_tri_axis_ff restated: the cell, or -1 where it defers to FP64."""
+    f32 = np.float32
+    k64 = 1024.0 / (mx - mn)
+    mn32, k32 = f32(mn), f32(k64)
+    mn_lo, k_lo = f32(mn - float(mn32)), f32(k64 - float(k32))
+    s1, e1 = _two_sum(a, b)
+    s2, e2 = _two_sum(s1, c)
+    slo = e1 + e2
+    y, ye = _two_prod(s2, np.full_like(s2, THIRD_HI))
+    ye = ye + (s2 * THIRD_LO + slo * THIRD_HI)
+    z, ze = _two_sum(y, np.full_like(y, -mn32))
+    ze = ze + (ye - mn_lo)
+    x, xe = _two_prod(z, np.full_like(z, k32))
+    xe = xe + (z * k_lo + ze * k32)
+    mag = np.abs(a) + np.abs(b) + np.abs(c) + np.abs(mn32)
+    tol = f32(2.0 ** -40) * (k32 * mag + f32(2) * np.abs(x))
+    xs = x + xe
+    f = np.floor(np.clip(x, 0, 1024)).astype(np.float32)
+    below = (x - f) + xe
+    above = ((f + f32(1)) - x) - xe
+    fi = f.astype(np.int64)
+    out = np.where((below > tol) & (above > tol), np.minimum(fi, 1023), -1)
+    out = np.where((below < -tol) & (fi >= 1), np.minimum(fi - 1, 1023), out)
+    out = np.where(above < -tol, np.minimum(fi + 1, 1023), out)
+    out = np.where(xs > f32(1023) + tol, 1023, out)
+    out = np.where(xs < f32(1) - tol, 0, out)
+    return out
+
+
+def test_morton_float_float_step_matches_fp64():
+    """The Morton cell's second step (csrc/lbvh.cu morton_tri_axis_ff, pairs of FP32 numbers) against
+    the reference's FP64 sequence, on triangles whose centroid coordinate lies within about 1e-6
+    cell of a cell boundary (where the FP32 first step defers) and on random ones: every decided cell
+    equal; deferred to FP64 only within 1e-8 cell of a boundary, and for fewer than one in a million
+    random coordinates."""
+    rng = np.random.default_rng(11)
+    n = 1_000_000
+    mn, mx = -2.1, 2.3
+    k = 1024.0 / (mx - mn)
+    target = rng.integers(1, 1023, n) + rng.uniform(-1e-6, 1e-6, n)
+    cen = mn + target / k
+    a = (cen + rng.uniform(-0.05, 0.05, n)).astype(np.float32)
+    b = (cen + rng.uniform(-0.05, 0.05, n)).astype(np.float32)
+    c = (3.0 * cen - a.astype(np.float64) - b.astype(np.float64)).astype(np.float32)
+    for near, (A, B, Cc) in ((True, (a, b, c)), (False, tuple(rng.uniform(mn, mx, (3, n)).astype(np.float32)))):
+        got = _morton_ff(A, B, Cc, mn, mx)
+        ref = _morton_ref(A, B, Cc, mn, mx)
+        decided = got >= 0
+        assert (got[decided] == ref[decided]).all()
+        if near:
+            # deferred only where the exact coordinate is within 1e-8 cell of a boundary (here about
+            # a fifth of the cases land exactly on one: the sum's grid meets the integers)
+            x = ((A.astype(np.float64) + B + Cc) / 3.0 - mn) * k
+            assert (np.abs(x[~decided] - np.round(x[~decided])) < 1e-8).all()
+        else:
+            assert (~decided).mean() < 1e-6, (~decided).mean()
