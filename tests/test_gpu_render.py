@@ -183,7 +183,8 @@ def test_gbuffer_and_device_outputs(ctx):
 
 def test_autotuner_cache_reproducible(ctx, tmp_path):
     """Tuning picks a configuration no slower than the defaults on its probe (margin rule), stores
-    it, and a second tuner with the same cache applies the same choice without timing."""
+    it, and a second tuner with the same cache and probe applies the same choice without timing
+    (a choice timed at another probe spp is a different cache entry)."""
     from cudapathtracing_gb300 import autotune
     d = P.cornell_box(width=48)
     s = api.Scene(ctx, d).init()
@@ -194,8 +195,8 @@ def test_autotuner_cache_reproducible(ctx, tmp_path):
         ch = t1.tune(s, prm, abi.INTEGRATOR_WAVEFRONT)
         assert ch.trials and ch.trials[0]["config"]["slots"] == autotune.DEFAULTS["slots"]
         assert ch.score >= ch.default_score
-        ch2 = autotune.Autotuner(ctx, cache_path=path).tune(s, prm, abi.INTEGRATOR_WAVEFRONT)
-        assert ch2.knobs == ch.knobs
+        ch2 = autotune.Autotuner(ctx, cache_path=path, probe_spp=2).tune(s, prm, abi.INTEGRATOR_WAVEFRONT)
+        assert ch2.knobs == ch.knobs and ch2.trials == ch.trials   # from the cache, not re-timed
         r = s.render(integrator=abi.INTEGRATOR_WAVEFRONT, **prm)
         assert r["rays"] > 0
     finally:
