@@ -427,7 +427,7 @@ def main():
         from cudapathtracing_gb300 import autotune
         tuner = autotune.Autotuner(ctx, cache_path=os.path.join(ROOT, "cudapathtracing_gb300", "_build",
                                                                 "tune_cache.json"),
-                                   probe_spp=min(16, wl["spp"]), repeats=2)
+                                   probe_spp=min(64, wl["spp"]), repeats=2)
         tuned = tuner.tune(scene, dict(wl, seed=seed), integ)
     if args.material_sort >= 0:
         ctx.set_material_sort(bool(args.material_sort))

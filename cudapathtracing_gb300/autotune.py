@@ -39,7 +39,7 @@ DEFAULTS = {
 
 CANDIDATES = {
     "render_block": [(16, 8), (32, 4), (8, 8), (8, 16), (32, 8), (16, 16)],
-    "slots": [1 << 19, 1 << 20, 1 << 21, 1 << 22],
+    "slots": [1 << 19, 1 << 20, 1 << 21, 1 << 22, 1 << 23, 1 << 24],
     "block_trace": [64, 128, 256],
     "block_shade": [64, 128, 256],
     "short_stack": [8, 16, 24, 32],
