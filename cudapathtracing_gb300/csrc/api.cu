@@ -58,8 +58,8 @@ namespace cpt {
 cpt_status wavefront_grids(int sm_count, int block_trace, int block_shade, int short_entries, int* grid_trace,
                            int* grid_trace_wide, int* grid_shade);
 size_t wide_scratch_bytes(uint32_t n);
-cpt_status build_wide(uint32_t n, const float4* nodes, float4* wide, void* scratch, size_t scratch_bytes,
-                      cudaStream_t stream, uint32_t* num_wide);
+cpt_status build_wide(uint32_t n, const int2* child, const float4* node_box, const float4* leaf_box, float4* wide,
+                      void* scratch, size_t scratch_bytes, cudaStream_t stream, uint32_t* num_wide);
 }
 
 struct cpt_scene {
@@ -444,19 +444,14 @@ cpt_status make_layout(cpt_scene* s, cudaStream_t stream, uint32_t* num_wide)
             cpt_status st = dalloc(&s->wide, CPT_WIDE_F4 * (size_t)ni);
             if (st != CPT_OK) return st;
         }
-        if (!s->nodes) {
-            cpt_status st = dalloc(&s->nodes, 4 * (size_t)ni);
-            if (st != CPT_OK) return st;
-        }
         if (wide_scratch_bytes(n) > s->scratch_bytes) return fail(CPT_ERR_INVALID_ARGUMENT, "wide scratch too small");
         s->width = 8;
-        s->node_q = 0;
-        // leaf records in sorted (Morton) order, shared with the binary layout, and the 64-byte BVH2
-        // records the collapse reads (both children's boxes in one record)
+        // leaf records in sorted (Morton) order, shared with the binary layout
         cpt_status st = build_trace_layout(n, s->n_lights, s->n_spheres, s->child, s->node_box, s->leaf_box, s->order,
-                                           s->tri_f32, s->tri_f64, s->spheres, s->nodes, s->leaf_rec, stream, false);
+                                           s->tri_f32, s->tri_f64, s->spheres, nullptr, s->leaf_rec, stream);
         if (st != CPT_OK) return st;
-        return build_wide(n, s->nodes, s->wide, s->scratch, s->scratch_bytes, stream, num_wide);
+        return build_wide(n, s->child, s->node_box, s->leaf_box, s->wide, s->scratch, s->scratch_bytes, stream,
+                          num_wide);
     }
     if (!s->nodes && ni) {
         cpt_status st = dalloc(&s->nodes, 4 * (size_t)ni);

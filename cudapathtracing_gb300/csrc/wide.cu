@@ -40,30 +40,26 @@ __device__ __forceinline__ float area(float4 mn, float4 mx)
     return dx * dy + dy * dz + dz * dx;
 }
 
+__device__ __forceinline__ void ref_box(int ref, const float4* node_box, const float4* leaf_box, float4& mn, float4& mx)
+{
+    const float4* b = ref < 0 ? leaf_box + 2 * (size_t)(~ref) : node_box + 2 * (size_t)ref;
+    mn = b[0];
+    mx = b[1];
+}
+
+
 // Level l: the wide nodes [base, base + n) with base = level_base[l], n = level_count[l]; wide node
 // w stands for binary node tasks[w].  Internal children get the next numbers in level l + 1, which
 // starts at base + n (one atomic per node reserves their consecutive block).  The candidate
 // children's references, boxes and areas stay in registers (every array is indexed with
-// compile-time indices only), and an expansion reads the expanded node's BVH2 record (both
-// children's references and boxes, 64 bytes): one dependent load per expansion.
+// compile-time indices only), so each box is read once: an expansion costs two dependent loads
+// (the expanded node's children, then their two boxes).
 constexpr int COLLAPSE_THREADS = 128;
 constexpr int MAX_WIDE_LEVELS = 80;
 
-// BVH2 node record i (lbvh.cu k_bvh2_nodes): both children's references and FP32 boxes.
-__device__ __forceinline__ void load_record(const float4* __restrict__ nodes, int i, int& a, int& b, float4& amn,
-                                            float4& amx, float4& bmn, float4& bmx)
-{
-    const float4* p = nodes + 4 * (size_t)i;
-    const float4 r0 = __ldg(p), r1 = __ldg(p + 1), r2 = __ldg(p + 2), r3 = __ldg(p + 3);
-    amn = make_float4(r0.x, r0.z, r2.x, 0.f);
-    amx = make_float4(r0.y, r0.w, r2.y, 0.f);
-    bmn = make_float4(r1.x, r1.z, r2.z, 0.f);
-    bmx = make_float4(r1.y, r1.w, r2.w, 0.f);
-    a = __float_as_int(r3.x);
-    b = __float_as_int(r3.y);
-}
-
-__global__ void __launch_bounds__(COLLAPSE_THREADS, 3) k_collapse_level(const float4* __restrict__ nodes,
+__global__ void __launch_bounds__(COLLAPSE_THREADS, 3) k_collapse_level(const int2* __restrict__ child,
+                                                                     const float4* __restrict__ node_box,
+                                                                     const float4* __restrict__ leaf_box,
                                                                      int* __restrict__ tasks,
                                                                      int* __restrict__ level_count,
                                                                      int* __restrict__ level_base, int l,
@@ -78,15 +74,18 @@ __global__ void __launch_bounds__(COLLAPSE_THREADS, 3) k_collapse_level(const fl
         int refs[8];
         float4 cmn[8], cmx[8];
         float car[8];
+        const int2 c = child[b];
+        float4 nmn, nmx;
+        ref_box(b, node_box, leaf_box, nmn, nmx);
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
             refs[k] = CPT_WIDE_EMPTY;
             car[k] = -1.0f;
         }
-        load_record(nodes, b, refs[0], refs[1], cmn[0], cmx[0], cmn[1], cmx[1]);
-        // the node's box: the union of its children's (min and max are exact)
-        const float4 nmn = make_float4(fminf(cmn[0].x, cmn[1].x), fminf(cmn[0].y, cmn[1].y), fminf(cmn[0].z, cmn[1].z), 0.f);
-        const float4 nmx = make_float4(fmaxf(cmx[0].x, cmx[1].x), fmaxf(cmx[0].y, cmx[1].y), fmaxf(cmx[0].z, cmx[1].z), 0.f);
+        refs[0] = c.x;
+        refs[1] = c.y;
+        ref_box(c.x, node_box, leaf_box, cmn[0], cmx[0]);
+        ref_box(c.y, node_box, leaf_box, cmn[1], cmx[1]);
         car[0] = area(cmn[0], cmx[0]);
         car[1] = area(cmn[1], cmx[1]);
         int nr = 2;
@@ -105,9 +104,10 @@ __global__ void __launch_bounds__(COLLAPSE_THREADS, 3) k_collapse_level(const fl
                 }
             }
             if (best < 0) break;
-            int2 cc;
+            const int2 cc = child[best_ref];
             float4 amn, amx, bmn, bmx;
-            load_record(nodes, best_ref, cc.x, cc.y, amn, amx, bmn, bmx);
+            ref_box(cc.x, node_box, leaf_box, amn, amx);
+            ref_box(cc.y, node_box, leaf_box, bmn, bmx);
             const float aa = area(amn, amx), ab = area(bmn, bmx);
 #pragma unroll
             for (int k = 0; k < 8; ++k) {
@@ -231,8 +231,8 @@ size_t wide_scratch_bytes(uint32_t n)
     return align_up((size_t)n * 4, 256) + align_up(2 * MAX_WIDE_LEVELS * 4, 256);
 }
 
-cpt_status build_wide(uint32_t n, const float4* nodes, float4* wide, void* scratch, size_t scratch_bytes,
-                      cudaStream_t stream, uint32_t* num_wide)
+cpt_status build_wide(uint32_t n, const int2* child, const float4* node_box, const float4* leaf_box, float4* wide,
+                      void* scratch, size_t scratch_bytes, cudaStream_t stream, uint32_t* num_wide)
 {
     if (n < 2) {
         if (num_wide) *num_wide = 0;
@@ -263,7 +263,8 @@ cpt_status build_wide(uint32_t n, const float4* nodes, float4* wide, void* scrat
     for (;;) {
         const int first = l, stop = std::min(l + 16, MAX_WIDE_LEVELS - 1);
         for (; l < stop; ++l)
-            k_collapse_level<<<grid, COLLAPSE_THREADS, 0, stream>>>(nodes, tasks, level_count, level_base, l, wide);
+            k_collapse_level<<<grid, COLLAPSE_THREADS, 0, stream>>>(child, node_box, leaf_box, tasks, level_count,
+                                                                    level_base, l, wide);
         add_launches(stop - first);
         CPT_CUDA(cudaGetLastError());
         // level l: its count (wide nodes still to collapse) and base (= wide nodes written)
