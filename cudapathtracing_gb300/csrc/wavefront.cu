@@ -270,7 +270,11 @@ __device__ __forceinline__ void start_item(const SceneView& s0, const Wf& w, con
 template <bool MULTI>
 __device__ __forceinline__ void next_item(const SceneView& s0, const Wf& w, const RenderArgs& a0, int slot, int nq)
 {
-    int item = atomicAdd(&w.cnt[6], 1);
+    // the lanes of the warp that take an item now share one atomic on the item counter
+    cg::coalesced_group g = cg::coalesced_threads();
+    int first = 0;
+    if (g.thread_rank() == 0) first = atomicAdd(&w.cnt[6], (int)g.size());
+    const int item = g.shfl(first, 0) + (int)g.thread_rank();
     if (item >= w.n_items) {
         w.pixel[slot] = -1;
         return;
