@@ -64,8 +64,7 @@ enum : uint32_t {
 struct WfJob;
 
 struct Wf {
-    int M, L, first_pix, npix, S, n_items;   // S: samples per work item
-    int G;                  // samples per estimator group (sample_group(spp)); S is G or 1
+    int M, L, first_pix, npix, S, n_items;
     int* pixel;
     int* sample;            // index of the sample in flight (within the pixel)
     uint32_t* flags;
@@ -79,7 +78,7 @@ struct Wf {
     float4* rad;
     float4* radp;
     float4* pix;            // sum of the item's finished samples
-    float4* part;           // item sums (a group's, or one sample's), [item group][pixel - first_pix]
+    float4* part;           // group sums, [group][pixel - first_pix]
     float2* med;
     float4* hit;
     int* q;                 // 2 * M
@@ -300,24 +299,17 @@ __global__ void k_wf_init(const __grid_constant__ SceneView s, Wf w, const __gri
 }
 
 // Pixel = (sum of its group sums in group order) / spp, as the megakernel adds them (one render,
-// or one job of a batch).  `items` item sums per pixel; an estimator group is G / S consecutive
-// items: with one sample per item the group sum is re-formed here from the samples in sample order
-// (0 + r0 + r1 + ..., as a slot adds them), so the image is the same as with whole groups per item.
-__global__ void k_wf_finish(JobGeo jg, RenderArgs a, int items, int G)
+// or one job of a batch).
+__global__ void k_wf_finish(JobGeo jg, RenderArgs a, int groups)
 {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= jg.npix) return;
-    const int per = G / jg.S;
     float3 sum = f3(0.f, 0.f, 0.f);
     float sum_y2 = 0.f;
-    for (int g = 0; g < items; g += per) {
-        float4 gs = make_float4(0.f, 0.f, 0.f, 0.f);
-        for (int j = 0; j < per && g + j < items; ++j) {
-            const float4 part = jg.part[(size_t)(g + j) * jg.npix + p];
-            gs = make_float4(gs.x + part.x, gs.y + part.y, gs.z + part.z, gs.w + part.w);
-        }
-        sum = sum + xyz(gs);
-        sum_y2 += gs.w;
+    for (int g = 0; g < groups; ++g) {
+        const float4 part = jg.part[(size_t)g * jg.npix + p];
+        sum = sum + xyz(part);
+        sum_y2 += part.w;
     }
     float3 v = sum / (float)a.spp;
     size_t off = (size_t)(jg.first_pix + p);
@@ -757,12 +749,7 @@ cpt_status run_wavefront(const SceneView& view, const RenderArgs& args, const st
         if (w.npix <= 0) return CPT_OK;
         if (view.n_lights > 30) return fail(CPT_ERR_UNSUPPORTED, "wavefront integrator: at most 30 lights");
         if (args.spp <= 0) return fail(CPT_ERR_INVALID_ARGUMENT, "spp must be positive");
-        // Work items of one sample where no G-buffer is wanted and the per-sample sums fit in 4 GB:
-        // a slot then holds one short path instead of a group's samples back to back, so the
-        // frame's last iterations (slots still working through long groups) shrink.  With a
-        // G-buffer an item is a whole group (group 0 writes the first surface of the pixel).
-        w.G = sample_group(args.spp);
-        w.S = (!args.gbuf && (size_t)args.spp * (size_t)w.npix * sizeof(float4) <= (4ull << 30)) ? 1 : w.G;
+        w.S = sample_group(args.spp);
         n_items = n_parts = (size_t)((args.spp + w.S - 1) / w.S) * (size_t)w.npix;
         L = std::max(view.n_lights, 1);
     } else {
@@ -868,16 +855,16 @@ cpt_status run_wavefront(const SceneView& view, const RenderArgs& args, const st
     if (exec) cudaGraphExecDestroy(exec);
     if (drained) {
         if (!MULTI) {
-            const int items = (args.spp + w.S - 1) / w.S;
+            const int groups = (args.spp + w.S - 1) / w.S;
             k_wf_finish<<<(w.npix + 255) / 256, 256, 0, stream>>>(JobGeo{w.first_pix, w.npix, w.S, w.part}, args,
-                                                                  items, w.G);
+                                                                  groups);
             add_launches(1);
         } else {
             for (const WfJob& j : J) {
                 if (j.npix <= 0) continue;
-                const int items = (j.args.spp + j.S - 1) / j.S;
+                const int groups = (j.args.spp + j.S - 1) / j.S;
                 k_wf_finish<<<(j.npix + 255) / 256, 256, 0, stream>>>(
-                    JobGeo{j.first_pix, j.npix, j.S, w.part + j.part_base}, j.args, items, j.S);
+                    JobGeo{j.first_pix, j.npix, j.S, w.part + j.part_base}, j.args, groups);
                 add_launches(1);
             }
         }
