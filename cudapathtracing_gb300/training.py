@@ -8,7 +8,7 @@ display space (sqrt, clamped to [0, 1], per channel over all pixels, as pic2RGBW
 Render.cu:462-481) against a high-spp render of a held-out scene, for the plain render, the
 reference's bilateral filter and the denoiser, and the wall time each needs to reach a target RMSE.
 
-    python -m cudapathtracing_gb300.training --scenes 2000 --steps 20000 --out weights.npz
+    python -m cudapathtracing_gb300.training --scenes 2000 --steps 40000 --batch 16 --out weights.npz
 """
 from __future__ import annotations
 
@@ -148,8 +148,8 @@ def main():
     ap.add_argument("--scenes", type=int, default=2000)
     ap.add_argument("--size", type=int, default=256)
     ap.add_argument("--spp-ref", type=int, default=4096)
-    ap.add_argument("--steps", type=int, default=20000)
-    ap.add_argument("--batch", type=int, default=8)
+    ap.add_argument("--steps", type=int, default=40000)
+    ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--out", default=DEFAULT_WEIGHTS)
