@@ -6,13 +6,18 @@ roulette from depth 3, survival 0.8), 200 displaced level-5 icospheres (4,096,00
 LBVH build over the resident triangles + the full 64-spp render.  Synthetic, seeded inputs
 (PCG32); scene data (~0.5 GB of BVH + leaf records) is larger than L2.
 
-  value      Mrays/s with the scene resident in HBM (closest-hit queries / device time)
+  value      Mrays/s with the scene resident in HBM (closest-hit queries / device time); launch
+             shapes from the autotuner, timed (untimed here) at the workload's own spp up to 64
   e2e        same metric through the C ABI with host buffers: scene upload from pinned host
              memory, build, render, image read-back, scene release — every step
   roofline   the render kernel: algorithmic bytes per ray (oracle-counted traversal work of the
-             workload, cudapathtracing_gb300/workload_constants.json) x rays / kernel time
-  cpu_baseline  the reference's CPU implementation (oracle/_ref where built, else the oracle
-             port) on a bounded sample of the same workload
+             workload, cudapathtracing_gb300/workload_constants.json) x rays / kernel time;
+             traffic = measured DRAM bytes per traced ray (profiles/traffic_<workload>.json) x rays
+  cpu_baseline  the reference's bounce loop on the host cores with the workload's own estimator
+             and spp on a band of rows (the oracle's FP64 restatement; oracle/_ref, the reference's
+             own code, for its STATIC estimator where built), plus the STATIC estimator at 1 spp
+  megakernel_same_run, lbvh_traversal_microbench, denoise (wall time to RMSE 0.01, and the
+             denoiser at 1080p on 1/4/16 spp): see the line's keys
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl cpt|reference] [--workload ...]
 """
