@@ -185,30 +185,42 @@ def cpu_reference_sample(desc, wl: dict, seconds: float = 10.0):
     return v, c.info(v)
 
 
-def cpu_trace_sample(desc, seconds: float = 8.0, seed: int = 1) -> tuple[float, dict]:
+class CpuTrace:
     """Closest-hit queries on the host cores: the oracle's FP64 traversal of the reference's LBVH
     (ordered, pruned) over the first rays of the bench's own uniform ray set, the count sized so
-    that one run takes about `seconds`."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle as O
-    from cudapathtracing_gb300 import procedural as P
-    O.build(ref=False)
-    threads = os.cpu_count() or 1
-    o = O.OracleScene(desc)
-    n = 1 << 16
-    rays = P.rays_as_f64(P.uniform_rays(n, seed=seed))
-    t0 = time.perf_counter()
-    o.trace(rays, threads=threads)
-    t = time.perf_counter() - t0
-    n = int(min(8_000_000, max(n, n * seconds / max(t, 1e-3))))
-    rays = P.rays_as_f64(P.uniform_rays(n, seed=seed))
-    t0 = time.perf_counter()
-    o.trace(rays, threads=threads)
-    t = time.perf_counter() - t0
-    v = n / t / 1e6
-    return v, dict(value=round(v, 4), unit="Mrays/s", cores=threads, kind="port", same_config=True,
-                   sample=f"the first {n} of the bench's uniform rays (PCG32 seed {seed}) against the same "
-                          f"{desc.num_triangles}-triangle icosphere, FP64 ordered pruned traversal")
+    that one run takes about `seconds` (the scene is built once)."""
+
+    def __init__(self, desc, seconds: float = 8.0, seed: int = 1):
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        from cudapathtracing_gb300 import procedural as P
+        O.build(ref=False)
+        self.threads = os.cpu_count() or 1
+        self.desc, self.seed = desc, seed
+        self.o = O.OracleScene(desc)
+        n = 1 << 16
+        t = self._run(P.rays_as_f64(P.uniform_rays(n, seed=seed)))
+        self.n = int(min(8_000_000, max(n, n * seconds / max(t, 1e-3))))
+        self.rays = P.rays_as_f64(P.uniform_rays(self.n, seed=seed))
+
+    def _run(self, rays) -> float:
+        t0 = time.perf_counter()
+        self.o.trace(rays, threads=self.threads)
+        return time.perf_counter() - t0
+
+    def run(self) -> float:
+        return self.n / self._run(self.rays) / 1e6
+
+    def info(self, value: float) -> dict:
+        return dict(value=round(value, 4), unit="Mrays/s", cores=self.threads, kind="port", same_config=True,
+                    sample=f"the first {self.n} of the bench's uniform rays (PCG32 seed {self.seed}) against the "
+                           f"same {self.desc.num_triangles}-triangle icosphere, FP64 ordered pruned traversal")
+
+
+def cpu_trace_sample(desc, seconds: float = 8.0, seed: int = 1) -> tuple[float, dict]:
+    c = CpuTrace(desc, seconds, seed)
+    v = c.run()
+    return v, c.info(v)
 
 
 def reference_estimator_sample(desc, seconds: float = 6.0) -> dict:
@@ -248,10 +260,10 @@ def run_reference_arm(args):
     if args.spp > 0:
         wl["spp"] = args.spp
     if args.workload == "icosphere_10M":
-        vals = [cpu_trace_sample(desc, seconds=4.0)[0] for _ in range(args.warmup + args.steps)][args.warmup:]
+        ct = CpuTrace(desc, seconds=4.0)
+        vals = [ct.run() for _ in range(args.warmup + args.steps)][args.warmup:]
         value = float(np.mean(vals))
-        info = cpu_trace_sample(desc, seconds=4.0)[1]
-        info["value"] = round(value, 4)
+        info = ct.info(value)
     else:
         cref = CpuReference(desc, wl)
         cref.calibrate(seconds=6.0)

@@ -249,13 +249,17 @@ cpt_status build_wide(uint32_t n, const int2* child, const float4* node_box, con
     // A grid that is resident at once; each thread takes nodes of its level in turn.  The host
     // looks at the level counts once every 16 levels (the wide tree of a few million primitives
     // has about a dozen; a level whose count is zero returns at once).
-    static int resident = 0;
+    // per device (the first 64 ordinals; others are queried on every call)
+    static int resident_of[64] = {};
+    int dev = 0;
+    CPT_CUDA(cudaGetDevice(&dev));
+    int resident = (dev >= 0 && dev < 64) ? resident_of[dev] : 0;
     if (resident == 0) {
-        int dev = 0, sms = 0, per_sm = 0;
-        CPT_CUDA(cudaGetDevice(&dev));
+        int sms = 0, per_sm = 0;
         CPT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
         CPT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_collapse_level, COLLAPSE_THREADS, 0));
         resident = std::max(1, sms * std::max(1, per_sm));
+        if (dev >= 0 && dev < 64) resident_of[dev] = resident;
     }
     const unsigned grid = std::max(1u, std::min((n + COLLAPSE_THREADS - 1) / COLLAPSE_THREADS, (unsigned)resident));
     int l = 0;
