@@ -326,8 +326,9 @@ __global__ void k_wf_finish(JobGeo jg, RenderArgs a, int groups)
     if (a.rgba8) reinterpret_cast<uchar4*>(a.rgba8)[off] = make_uchar4(to_u8(v.x), to_u8(v.y), to_u8(v.z), 255);
 }
 
-// At most 48 registers (5 blocks of 256 per SM): 62 % occupancy instead of 50 % for a few spilled
-// values, +5.7 % on the 1080p spheres render (the shadow kernel is faster uncapped).
+// BVH2: at most 48 registers (5 blocks of 256 per SM): 62 % occupancy instead of 50 % for a few
+// spilled values, +5.7 % on the 1080p spheres render (the shadow kernel is faster uncapped).
+// 8-wide: at most 64 registers (4 blocks of 256): +4.7 % against 72; 51 registers spill (-9 %).
 template <bool WIDE, int SHORT, bool SORT, bool MULTI>
 __global__ void __launch_bounds__(256, WIDE ? 4 : 5) k_wf_trace(const __grid_constant__ SceneView s, Wf w, int par)
 {
